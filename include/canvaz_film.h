@@ -1,0 +1,240 @@
+/*
+ * canvaz_film.h — C ABI of the GB300 (sm_103a) thin-film step.
+ *
+ * This library replaces the wgpu film pass of Canvaz (lukaszkujawa/paint-sim-3d):
+ * the Herschel–Bulkley lubrication height update (shaders/film.wgsl), the upwind
+ * strata/pigment transport (shaders/film.wgsl strata_split + shaders/strata.wgsl),
+ * cure/rheology (shaders/cure.wgsl) and the Kubelka–Munk shade
+ * (shaders/km.wgsl + shaders/shade.wgsl).  Every entry point below names the
+ * Rust method of `impl Film` (src/film/mod.rs) it stands in for.
+ *
+ * Conventions
+ *  - Every function returns cf_status; no exception or abort crosses the ABI.
+ *  - A cf_film handle is used by one host thread at a time (the reference's
+ *    Film lives on the winit thread and is not shared either).
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default
+ *    stream.  Work is enqueued; call cf_sync (or synchronise the stream) before
+ *    reading results on the host, exactly like wgpu's queue.submit + map_async.
+ *  - All per-cell planes are row-major, cell (i, j) at index j * w + i.
+ */
+#ifndef CANVAZ_FILM_H
+#define CANVAZ_FILM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CF_ABI_VERSION 1
+#define CF_STRATA 4        /* shaders/common.wgsl:43 STRATA   */
+#define CF_NPIG 12         /* shaders/common.wgsl:44 NPIG     */
+#define CF_PIG_SLOTS 16    /* 12 pigments, 12 thinner, 13 yield, 14 ln(mu)+10, 15 flow index n */
+#define CF_NBAND 16        /* shaders/common.wgsl:45 NBAND    */
+#define CF_PIG_STRIDE 40   /* shaders/common.wgsl:46 PIG_STRIDE */
+#define CF_TILE 16         /* 16x16 activity tiles, shaders/film.wgsl:1365-1425 */
+#define CF_STATS_TILE 64   /* reduce_tiles tile, shaders/common.wgsl:47 TILE */
+
+typedef enum cf_status {
+    CF_OK = 0,
+    CF_ERR_INVALID_ARG = 1,
+    CF_ERR_OUT_OF_MEMORY = 2,
+    CF_ERR_CUDA = 3,
+    CF_ERR_TIMEOUT = 4,
+    CF_ERR_NAN = 5,
+    CF_ERR_UNSUPPORTED = 6,
+    CF_ERR_NOT_READY = 7
+} cf_status;
+
+/* Storage precision of the pigment strata and of the rheology plane.
+ * Height, flux, K/S and all arithmetic stay FP32 in every mode. */
+typedef enum cf_precision {
+    CF_PREC_REFERENCE = 0, /* f16 pigment slots, f32 rheology: the reference layout */
+    CF_PREC_FP32 = 1,      /* f32 pigment slots, f32 rheology                       */
+    CF_PREC_BF16 = 2       /* bf16 pigment slots, bf16 rheology                     */
+} cf_precision;
+
+/* Element format of the strata_pig plane handed to cf_write_state / cf_read_state. */
+typedef enum cf_pig_format {
+    CF_PIG_F16 = 0,  /* 4 strata x 16 slots x IEEE half: 128 B per cell (reference layout) */
+    CF_PIG_F32 = 1,  /* 4 strata x 16 slots x float:     256 B per cell                    */
+    CF_PIG_BF16 = 2  /* 4 strata x 16 slots x bfloat16:  128 B per cell                    */
+} cf_pig_format;
+
+/* FilmSettings (src/film/mod.rs:281-350).  The reference reads its ablation
+ * switches from environment variables inside update_params
+ * (src/film/mod.rs:870-915); here they are plain fields. */
+typedef struct cf_settings {
+    float width_m;            /* canvas width; dx = width_m / w          */
+    float height_m;
+    float rho;                /* density kg/m^3                          */
+    float sigma;              /* surface tension N/m                     */
+    float n_index;            /* global power-law index (slot 15 = 0)    */
+    float m_cap;              /* capillary mobility cap                  */
+    float contact_angle_deg;
+    float hysteresis_deg;
+    float h_star;             /* precursor / disjoining thickness        */
+    int32_t raw_canvas;       /* substrate reflectance at cf_create      */
+    float weave_um;           /* canvas weave amplitude at cf_create     */
+    float cure_rate;
+    float tau_cure;
+    float lnmu_cure;
+    float v_cap;
+    float tilt_deg;
+    float tilt_dir_deg;
+    float gravity;
+    float medium_mu;
+    uint32_t debug_view;      /* 1 = invariant view in the shade        */
+    float h_min;
+    float m_cap_hydro;
+    uint32_t max_substeps;
+    uint32_t min_substeps;
+    uint32_t implicit_iters;
+    int32_t implicit_hydro;   /* implicit CG hydrostatic solve: only 0 is supported */
+    int32_t slump;            /* slump pass: only 0 is supported (reference default) */
+    int32_t capillary;
+    int32_t capillary_implicit;
+    /* environment toggles of update_params */
+    int32_t no_hold;          /* PAINT_NO_HOLD     */
+    int32_t no_transl;        /* PAINT_NO_TRANSL   */
+    int32_t no_shape;         /* PAINT_NO_SHAPE    */
+    int32_t no_cap;           /* PAINT_NO_CAP      */
+    float kshape;             /* PAINT_KSHAPE (1)  */
+    float kline;              /* PAINT_KLINE (0)   */
+    float hyst_deg;           /* PAINT_HYST; < 0 means use hysteresis_deg */
+    float fcap_exp;           /* PAINT_FCAP (2.5)  */
+    float cap_cond;           /* PAINT_CAPCOND (80) */
+    /* extension: 1 = every 16x16 tile is active every frame (compact_tiles
+     * marks all tiles); 0 = the reference's moved-tile activity. */
+    int32_t all_active;
+} cf_settings;
+
+/* Params uniform (src/film/mod.rs:5-23, shaders/common.wgsl:1-17), 176 bytes. */
+typedef struct cf_params {
+    uint32_t size[2];
+    uint32_t tiles[2];
+    float dx, dt, inv_dx, frame_dt;
+    float g[4];      /* (gx, gy, gz, |g|)                               */
+    float phys[4];   /* (rho, sigma, n, m_cap)                          */
+    float ein[4];    /* (tan theta, l_c sin(theta/2), Pi_A, h_min)      */
+    float cure[4];   /* (rate, tau_cure, lnmu_cure, h_star)             */
+    float misc[4];   /* (tiny stratum, merge distance, medium mu, m_hyd)*/
+    uint32_t flags[4];
+    float front[4];  /* (H_c, dx / l_c,z, m_imp_max, dt_i)              */
+    float front2[4]; /* (hysteresis rad, kshape, kline, toggles)        */
+    float front3[4]; /* (cc, kc, m_c, fcap exponent)                    */
+} cf_params;
+
+/* The eight persistent planes of Film::state_buffers (src/film/mod.rs:1277-1279),
+ * plus an optional per-cell rheology flow index. Host or device pointers. */
+typedef struct cf_state_view {
+    void* h;            /* float[N]                  */
+    void* m;            /* float[N]                  */
+    void* rheo;         /* float2[N] (mu Pa s, tau_y Pa) */
+    void* strata_h;     /* float4[N]                 */
+    void* strata_pig;   /* 64 slots per cell, element type = pig_format */
+    void* strata_cure;  /* float4[N]                 */
+    void* sub_refl;     /* 16 x IEEE half per cell   */
+    void* lay;          /* uint32[N]                 */
+    int32_t pig_format; /* cf_pig_format             */
+    int32_t device;     /* 0: host pointers, 1: device pointers */
+} cf_state_view;
+
+/* Host-side statistics (poll_stats src/film/mod.rs:935-973, compute_stats
+ * src/main.rs:1679-1819).  Mass sums are FP64 on the device. */
+typedef struct cf_stats {
+    float h_max;           /* reduce_tiles: max h over cells with h > 4 h_min */
+    float mu_min;          /* reduce_tiles: min mu over the same cells        */
+    uint32_t active_tiles; /* compact_tiles count of the last frame           */
+    uint32_t frames;       /* frames stepped since create                     */
+    double wet_volume;     /* sum(h) dx^2                                     */
+    double relief_volume;  /* sum(m) dx^2                                     */
+    double last_dt;        /* substep dt of the last frame                    */
+    uint64_t nan_cells;    /* non-finite h                                    */
+    uint64_t wet_cells;
+} cf_stats;
+
+typedef struct cf_film cf_film;
+
+/* --- lifecycle ---------------------------------------------------------- */
+
+/* FilmSettings::default (src/film/mod.rs:315-350). */
+cf_status cf_settings_default(cf_settings* out);
+
+/* Film::new (src/film/mod.rs:578-859): allocates the per-cell planes,
+ * writes the substrate reflectance (substrate_refl :188-210), the weave relief
+ * (weave :212-233) and rheo = (1, 0), then packs the params (update_params). */
+cf_status cf_create(const cf_settings* settings, uint32_t w, uint32_t h,
+                    int32_t precision, cf_film** out);
+cf_status cf_destroy(cf_film* film);
+
+/* Film::new :604-610 uploads pigment_table (src/color/mod.rs:243-258,
+ * 12 x 40 floats) and cmf_table (src/color/mod.rs:150-171, 16 x 3 floats). */
+cf_status cf_set_tables(cf_film* film, const float* pigtab, const float* cmf);
+
+/* --- state I/O ------------------------------------------------------------ */
+
+/* Film::write_state (src/film/mod.rs:1303-1320): uploads the planes, clears the
+ * scratch planes (pres, flux, acc, alpha, delta, tmp, acc_s, strata_h2,
+ * strata_pig2, alpha_s) and marks every activity tile moved.  A NULL plane
+ * pointer leaves that plane unchanged.  Synchronous. */
+cf_status cf_write_state(cf_film* film, const cf_state_view* state);
+
+/* Film::read_state (src/film/mod.rs:1281-1301).  A NULL plane is skipped.
+ * Synchronous. */
+cf_status cf_read_state(cf_film* film, const cf_state_view* state);
+
+/* --- per frame ------------------------------------------------------------ */
+
+/* Film::update_params (src/film/mod.rs:869-917). */
+cf_status cf_update_params(cf_film* film, float frame_dt, uint32_t substeps);
+
+/* Film::choose_substeps (src/film/mod.rs:919-933) from the stats of the last
+ * frame (read back synchronously, the reference reads them 1-2 frames late). */
+cf_status cf_choose_substeps(cf_film* film, float frame_dt, uint32_t* substeps);
+
+/* Film::encode_frame (src/film/mod.rs:1322-1462), simulation portion: tile
+ * activity, cure, `substeps` x {laplacian, plug, fluxes, limiter, apply, nose},
+ * strata split/limit/update/copy/fill x 6, tile stats and the full KM shade.
+ * Uses the params of the last cf_update_params. */
+cf_status cf_encode_frame(cf_film* film, uint32_t substeps, void* stream);
+
+/* One adaptive step: the substep dt is derived on the device from the
+ * h_max / mu_min of the previous frame with the formulas of choose_substeps
+ * (dt = min(dt_max, dt_cfl, dt_hyd, dt_cap)), the dt-dependent params are
+ * re-derived on the device, and one frame with one substep is run.  No host
+ * round trip; graph-capturable. */
+cf_status cf_step_adaptive(cf_film* film, float dt_max, void* stream);
+
+/* Film::dry_now (src/film/mod.rs:1230-1244): one cure pass with rate
+ * 4 / frame_dt so every stratum commits. */
+cf_status cf_dry_now(cf_film* film, void* stream);
+
+/* --- outputs ------------------------------------------------------------- */
+
+/* color_tex (rgba16float: linear sRGB + roughness) written by shade_full.
+ * Device pointer, valid for the life of the film. */
+cf_status cf_color_device_ptr(cf_film* film, void** ptr);
+
+/* Copies the colour plane (4 x IEEE half per cell) to host memory. Synchronous. */
+cf_status cf_read_color(cf_film* film, uint16_t* rgba16f_host);
+
+/* Statistics of the last frame; synchronous. */
+cf_status cf_get_stats(cf_film* film, cf_stats* out);
+
+/* Params of the last update (for parity checks of update_params). */
+cf_status cf_get_params(cf_film* film, cf_params* out);
+
+/* Waits for all work of this film. */
+cf_status cf_sync(cf_film* film);
+
+/* Human-readable text of the last error on this film (or of the last failed
+ * cf_create when film is NULL). */
+const char* cf_last_error(const cf_film* film);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CANVAZ_FILM_H */

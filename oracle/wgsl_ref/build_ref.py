@@ -1,0 +1,36 @@
+"""Builds oracle/_ref/libwgslref.so from the reference shaders.
+
+TEST INFRASTRUCTURE.  Needs the reference checkout (argument or REFERENCE env
+var, default /root/reference); does nothing when it is absent.  Steps:
+translate.py writes oracle/_ref/ref_shaders.inc (FP64), then g++ compiles
+driver.cpp against it.  Everything it writes stays in oracle/_ref/, which is
+git-ignored.
+Usage: python build_ref.py [reference_root]
+"""
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE.parent / "_ref"
+
+
+def build(ref=None):
+    ref = Path(ref or os.environ.get("REFERENCE", "/root/reference"))
+    if not (ref / "shaders" / "film.wgsl").exists():
+        print("reference shaders not found at %s; skipping" % ref)
+        return None
+    OUT.mkdir(exist_ok=True)
+    subprocess.run([sys.executable, str(HERE / "translate.py"), str(ref), str(OUT / "ref_shaders.inc"), "double"],
+                   check=True)
+    shutil.copy(HERE / "wgsl_rt_types.inc", OUT / "wgsl_rt_types.inc")
+    lib = OUT / "libwgslref.so"
+    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "driver.cpp"),
+                    "-o", str(lib)], check=True)
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -1,0 +1,292 @@
+// driver.cpp — runs the mechanically translated reference shaders.
+//
+// TEST INFRASTRUCTURE.  Compiled (by build_ref.py, only where the reference
+// checkout exists) together with the translation generated by translate.py
+// into oracle/_ref/libwgslref.so.  It dispatches the translated WGSL entry
+// points in the order of Film::encode_frame (src/film/mod.rs:1322-1462):
+//  - tile-list dispatches iterate the active tiles that the translated
+//    compact_tiles appended, 16x16 invocations each;
+//  - full-grid dispatches (cure_step, shade_full) iterate every invocation;
+//  - mark_tiles runs barrier phase by barrier phase;
+//  - apply's begin/end_motion workgroup flag and reduce_tiles' shared-memory
+//    tree (a max/min) are emulated here around the translated per-cell code;
+//  - nose and strata_fill read `__old` snapshots (Jacobi semantics).
+// One film per process (the translated buffers are module globals).
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../film_oracle.hpp"
+#include "ref_shaders.inc"
+
+using namespace wg;
+
+namespace {
+u32 W = 0, H = 0, TW = 0, TH = 0;
+size_t N = 0;
+
+template <class T>
+void sz(RtBuf<T>& b, size_t n) { b.v.assign(n, T{}); }
+
+void dispatch_tiles(void (*fn)(vec3<u32>, vec3<u32>)) {
+  u32 n = active_count[0];
+  for (u32 w = 0; w < n; ++w)
+    for (u32 ly = 0; ly < 16; ++ly)
+      for (u32 lx = 0; lx < 16; ++lx) fn(vec3<u32>(w, 0, 0), vec3<u32>(lx, ly, 0));
+}
+
+void dispatch_full(void (*fn)(vec3<u32>)) {
+  for (u32 y = 0; y < TH * 16; ++y)
+    for (u32 x = 0; x < TW * 16; ++x) fn(vec3<u32>(x, y, 0));
+}
+
+void run_mark_tiles() {
+  for (u32 ty = 0; ty < TH; ++ty)
+    for (u32 tx = 0; tx < TW; ++tx) {
+      vec3<u32> wid(tx, ty, 0);
+      for (int ph = 0; ph < 3; ++ph)
+        for (u32 ly = 0; ly < 16; ++ly)
+          for (u32 lx = 0; lx < 16; ++lx) {
+            vec3<u32> lid(lx, ly, 0);
+            u32 li = ly * 16 + lx;
+            if (ph == 0) mark_tiles__p0(wid, lid, li);
+            else if (ph == 1) mark_tiles__p1(wid, lid, li);
+            else mark_tiles__p2(wid, lid, li);
+          }
+    }
+}
+
+void run_compact_tiles() {
+  u32 nt = TW * TH;
+  for (u32 x = 0; x < ((nt + 255) / 256) * 256; ++x) compact_tiles(vec3<u32>(x, 0, 0));
+}
+
+void run_apply() {
+  u32 n = active_count[0];
+  for (u32 w = 0; w < n; ++w) {
+    bool any = false;
+    for (u32 ly = 0; ly < 16; ++ly)
+      for (u32 lx = 0; lx < 16; ++lx) {
+        vec3<u32> id = tile_cell(vec3<u32>(w, 0, 0), vec3<u32>(lx, ly, 0));
+        if (in_grid(id)) any = apply_cell(id) || any;
+      }
+    if (any) tile_moved[tile_list[w]] = 1u;
+  }
+}
+
+void run_reduce_tiles() {
+  u32 tw = P.tiles.x, th = P.tiles.y;
+  for (u32 ty = 0; ty < th; ++ty)
+    for (u32 tx = 0; tx < tw; ++tx) {
+      f32 hm = 0, mm = f32(1e9f);
+      for (u32 j = ty * 64; j < std::min(H, ty * 64 + 64); ++j)
+        for (u32 i = tx * 64; i < std::min(W, tx * 64 + 64); ++i) {
+          u32 c = idx(i, j);
+          f32 v = h[c];
+          if (v > f32(4.0f) * P.ein.w) { hm = std::max(hm, v); mm = std::min(mm, rheo[c].x); }
+        }
+      stats_out[tx + ty * tw] = vec2<f32>(hm, mm);
+    }
+}
+
+void run_nose() {
+  delta__old.v = delta.v;
+  dispatch_tiles(nose);
+}
+
+void run_strata_fill() {
+  strata_h__old.v = strata_h.v;
+  strata_pig__old.v = strata_pig.v;
+  strata_cure__old.v = strata_cure.v;
+  dispatch_tiles(strata_fill);
+}
+
+void encode_frame(u32 substeps) {
+  active_count[0] = 0;
+  run_mark_tiles();
+  run_compact_tiles();
+  dispatch_full(cure_step);
+  dispatch_tiles(clear_acc);
+  for (u32 s = 0; s < substeps; ++s) {
+    dispatch_tiles(laplacian);
+    dispatch_tiles(plug);
+    dispatch_tiles(fluxes);
+    dispatch_tiles(limiter);
+    run_apply();
+    run_nose();
+  }
+  dispatch_tiles(laplacian);
+  dispatch_tiles(strata_split);
+  run_reduce_tiles();
+  dispatch_tiles(strata_limit);
+  dispatch_tiles(strata_update);
+  dispatch_tiles(strata_copy_back);
+  for (int r = 0; r < 6; ++r) run_strata_fill();
+  dispatch_full(shade_full);
+}
+
+f32 hv(uint16_t b) { return (f32)cfo::f16_value(b); }
+uint16_t hb(double x) { return cfo::f16_bits(cfo::round_f16(x)); }
+
+}  // namespace
+
+extern "C" {
+
+void wgr_create(uint32_t w, uint32_t h_) {
+  W = w; H = h_; TW = (w + 15) / 16; TH = (h_ + 15) / 16; N = (size_t)w * h_;
+  sz(h, N); sz(m, N); sz(rheo, N); sz(pres, N); sz(flux, N); sz(acc, N); sz(alpha, N); sz(delta, N);
+  sz(tmp, N); sz(acc_s, 4 * N); sz(strata_h, N); sz(strata_pig, 8 * N); sz(strata_cure, N);
+  sz(sub_refl, 8 * N); sz(pigtab, 12 * 40); sz(cmf, 48); sz(strata_h2, N); sz(strata_pig2, 8 * N);
+  sz(alpha_s, N); sz(strata_cure2, N); sz(tile_flags, TW * TH); sz(tile_list, TW * TH);
+  sz(active_count, 4); sz(tile_moved, TW * TH); sz(lay, N);
+  sz(stats_out, ((w + 63) / 64) * ((h_ + 63) / 64)); sz(h_frame, N); sz(fnorm, N);
+  color_out.w = w; color_out.v.assign(N, vec4<f32>(f32(0)));
+  detail_out.w = w; detail_out.v.assign(N, vec4<f32>(f32(0)));
+}
+
+void wgr_set_params(const cf_params* p) {
+  P.size = vec2<u32>(p->size[0], p->size[1]);
+  P.tiles = vec2<u32>(p->tiles[0], p->tiles[1]);
+  P.dx = p->dx; P.dt = p->dt; P.inv_dx = p->inv_dx; P.frame_dt = p->frame_dt;
+  auto v4 = [](const float* a) { return vec4<f32>(a[0], a[1], a[2], a[3]); };
+  P.g = v4(p->g); P.phys = v4(p->phys); P.ein = v4(p->ein); P.cure = v4(p->cure); P.misc = v4(p->misc);
+  P.flags = vec4<u32>(p->flags[0], p->flags[1], p->flags[2], p->flags[3]);
+  P.front = v4(p->front); P.front2 = v4(p->front2); P.front3 = v4(p->front3);
+}
+
+void wgr_set_tables(const float* pt, const float* cm) {
+  for (int i = 0; i < 480; ++i) pigtab[i] = pt[i];
+  for (int i = 0; i < 48; ++i) cmf[i] = cm[i];
+}
+
+void wgr_encode_frame(uint32_t substeps) { encode_frame(substeps); }
+
+// write_state scratch clearing (src/film/mod.rs:1307-1317)
+void wgr_after_write_state() {
+  for (auto& v : pres.v) v = vec2<f32>(f32(0));
+  for (auto& v : flux.v) v = vec4<f32>(f32(0));
+  for (auto& v : acc.v) v = vec4<f32>(f32(0));
+  for (auto& v : alpha.v) v = 0;
+  for (auto& v : delta.v) v = 0;
+  for (auto& v : tmp.v) v = 0;
+  for (auto& v : acc_s.v) v = vec4<f32>(f32(0));
+  for (auto& v : strata_h2.v) v = vec4<f32>(f32(0));
+  for (auto& v : strata_pig2.v) v = vec4<u32>(0u);
+  for (auto& v : alpha_s.v) v = vec4<f32>(f32(0));
+  for (auto& v : tile_moved.v) v = 1u;
+}
+
+int wgr_run(const char* k) {
+  std::string s(k);
+  if (s == "mark_tiles") { active_count[0] = 0; run_mark_tiles(); }
+  else if (s == "compact_tiles") run_compact_tiles();
+  else if (s == "cure_step") dispatch_full(cure_step);
+  else if (s == "clear_acc") dispatch_tiles(clear_acc);
+  else if (s == "laplacian") dispatch_tiles(laplacian);
+  else if (s == "plug") dispatch_tiles(plug);
+  else if (s == "fluxes") dispatch_tiles(fluxes);
+  else if (s == "limiter") dispatch_tiles(limiter);
+  else if (s == "apply") run_apply();
+  else if (s == "nose") run_nose();
+  else if (s == "strata_split") dispatch_tiles(strata_split);
+  else if (s == "reduce_tiles") run_reduce_tiles();
+  else if (s == "strata_limit") dispatch_tiles(strata_limit);
+  else if (s == "strata_update") dispatch_tiles(strata_update);
+  else if (s == "strata_copy_back") dispatch_tiles(strata_copy_back);
+  else if (s == "strata_fill") run_strata_fill();
+  else if (s == "shade_full") dispatch_full(shade_full);
+  else return 0;
+  return 1;
+}
+
+uint32_t wgr_active_count() { return active_count[0]; }
+
+// Exchange a plane in the oracle's layout (float64 values):
+//  rheo 3/cell (mu, tau, n: n is not stored by the reference), strata_* 4/cell,
+//  strata_pig 64 slots/cell, sub_refl 16 bands/cell, pres 2, flux/acc 4,
+//  acc_s 16, fnorm 2, delta/tile words as integers, color 4/cell.
+int wgr_buffer(const char* name, double* io, int write) {
+  std::string n(name);
+  auto scal = [&](RtBuf<f32>& b) {
+    for (size_t i = 0; i < b.v.size(); ++i) { if (write) b.v[i] = (f32)io[i]; else io[i] = (double)b.v[i]; }
+  };
+  auto uns = [&](RtBuf<u32>& b) {
+    for (size_t i = 0; i < b.v.size(); ++i) { if (write) b.v[i] = (u32)io[i]; else io[i] = (double)b.v[i]; }
+  };
+  auto v2 = [&](RtBuf<vec2<f32>>& b) {
+    for (size_t i = 0; i < b.v.size(); ++i)
+      for (int k = 0; k < 2; ++k) { if (write) b.v[i][k] = (f32)io[2 * i + k]; else io[2 * i + k] = (double)b.v[i][k]; }
+  };
+  auto v4 = [&](RtBuf<vec4<f32>>& b) {
+    for (size_t i = 0; i < b.v.size(); ++i)
+      for (int k = 0; k < 4; ++k) { if (write) b.v[i][k] = (f32)io[4 * i + k]; else io[4 * i + k] = (double)b.v[i][k]; }
+  };
+  auto halves = [&](auto& words, size_t per) {  // per = u32 words per cell
+    for (size_t i = 0; i < words.size(); ++i)
+      for (int k = 0; k < 2; ++k) {
+        size_t slot = 2 * i + k;
+        if (write) {
+          uint16_t b = hb(io[slot]);
+          words[i] = k == 0 ? ((words[i] & 0xffff0000u) | b) : ((words[i] & 0xffffu) | ((u32)b << 16));
+        } else {
+          io[slot] = (double)hv((uint16_t)(k == 0 ? (words[i] & 0xffffu) : (words[i] >> 16)));
+        }
+      }
+    (void)per;
+  };
+  if (n == "h") scal(h);
+  else if (n == "m") scal(m);
+  else if (n == "alpha") scal(alpha);
+  else if (n == "tmp") scal(tmp);
+  else if (n == "h_frame") scal(h_frame);
+  else if (n == "rheo") {
+    for (size_t i = 0; i < N; ++i) {
+      if (write) rheo.v[i] = vec2<f32>((f32)io[3 * i], (f32)io[3 * i + 1]);
+      else { io[3 * i] = rheo.v[i].x; io[3 * i + 1] = rheo.v[i].y; io[3 * i + 2] = P.phys.z; }
+    }
+  }
+  else if (n == "pres") v2(pres);
+  else if (n == "fnorm") v2(fnorm);
+  else if (n == "flux") v4(flux);
+  else if (n == "acc") v4(acc);
+  else if (n == "acc_s") v4(acc_s);
+  else if (n == "alpha_s") v4(alpha_s);
+  else if (n == "strata_h") v4(strata_h);
+  else if (n == "strata_cure") v4(strata_cure);
+  else if (n == "strata_h2") v4(strata_h2);
+  else if (n == "strata_cure2") v4(strata_cure2);
+  else if (n == "strata_pig" || n == "strata_pig2") {
+    auto& b = n == "strata_pig" ? strata_pig : strata_pig2;
+    std::vector<u32> words(b.v.size() * 4);
+    for (size_t i = 0; i < b.v.size(); ++i) for (int k = 0; k < 4; ++k) words[4 * i + k] = b.v[i][k];
+    halves(words, 32);
+    if (write) for (size_t i = 0; i < b.v.size(); ++i) for (int k = 0; k < 4; ++k) b.v[i][k] = words[4 * i + k];
+  }
+  else if (n == "sub_refl") halves(sub_refl.v, 8);
+  else if (n == "delta") {
+    for (size_t i = 0; i < N; ++i) {
+      if (write) delta.v[i] = bitcast<f32>((u32)io[i]);
+      else io[i] = (double)bitcast<u32>(delta.v[i]);
+    }
+  }
+  else if (n == "lay") uns(lay);
+  else if (n == "tile_flags") uns(tile_flags);
+  else if (n == "tile_moved") uns(tile_moved);
+  else if (n == "stats") {
+    for (size_t i = 0; i < stats_out.v.size(); ++i)
+      for (int k = 0; k < 2; ++k) { if (write) stats_out.v[i][k] = (f32)io[2 * i + k]; else io[2 * i + k] = stats_out.v[i][k]; }
+  }
+  else if (n == "color") {
+    for (size_t i = 0; i < N; ++i)
+      for (int k = 0; k < 4; ++k) { if (write) color_out.v[i][k] = (f32)io[4 * i + k]; else io[4 * i + k] = color_out.v[i][k]; }
+  }
+  else return 0;
+  return 1;
+}
+
+}  // extern "C"
