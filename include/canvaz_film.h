@@ -190,6 +190,12 @@ cf_status cf_read_state(cf_film* film, const cf_state_view* state);
 /* Film::update_params (src/film/mod.rs:869-917). */
 cf_status cf_update_params(cf_film* film, float frame_dt, uint32_t substeps);
 
+/* The packing of Film::update_params (src/film/mod.rs:869-917) without a film:
+ * pure host arithmetic (f32, as the reference), usable without a GPU.
+ * h_max / mu_min are the stats the reference polls (poll_stats :935-973). */
+cf_status cf_pack_params(const cf_settings* settings, uint32_t w, uint32_t h, float frame_dt, uint32_t substeps,
+                         float h_max, float mu_min, cf_params* out, uint32_t* implicit_steps);
+
 /* Film::choose_substeps (src/film/mod.rs:919-933) from the stats of the last
  * frame (read back synchronously, the reference reads them 1-2 frames late). */
 cf_status cf_choose_substeps(cf_film* film, float frame_dt, uint32_t* substeps);

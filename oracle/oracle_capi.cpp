@@ -60,6 +60,14 @@ extern "C" {
 
 void cfo_settings_default(cf_settings* s) { cfo::settings_default(s); }
 
+// update_params packing without a film (host stats given explicitly).
+void cfo_pack_params(const cf_settings* s, uint32_t w, uint32_t h, float frame_dt, uint32_t substeps, float h_max,
+                     float mu_min, cf_params* out, uint32_t* implicit_steps) {
+  cfo::ParamsF pf = cfo::update_params(*s, w, h, frame_dt, substeps, h_max, 0.0f, mu_min);
+  *out = pf.p;
+  if (implicit_steps) *implicit_steps = pf.implicit_steps;
+}
+
 void* cfo_create(uint32_t w, uint32_t h, const cf_settings* s, int pig_mode, int bits) {
   Handle* hd = new Handle;
   hd->bits = bits;

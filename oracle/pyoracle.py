@@ -240,3 +240,13 @@ class RefShaders:
 
 def make_settings(overrides):
     return Settings.default(**overrides)
+
+
+def pack_params(settings, w, h, frame_dt, substeps, h_max=0.0, mu_min=1.0):
+    """The oracle's update_params packing for explicit host stats."""
+    L = lib()
+    L.cfo_pack_params.argtypes = [C.POINTER(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.c_float,
+                                  C.c_float, C.POINTER(Params), C.POINTER(C.c_uint32)]
+    p, n = Params(), C.c_uint32()
+    L.cfo_pack_params(C.byref(settings), w, h, frame_dt, substeps, h_max, mu_min, C.byref(p), C.byref(n))
+    return p, n.value

@@ -1,0 +1,221 @@
+"""Python host mirror of the reference's `impl Film` over the C ABI.
+
+Method names, argument meaning and order follow src/film/mod.rs (Film::new,
+update_params, choose_substeps, encode_frame, write_state, read_state,
+dry_now).  Every call goes through libcanvaz_film.so (the sm_103a kernels);
+a missing library or device raises: there is no CPU fallback.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import FilmError, Params, Settings, StateView, Stats
+
+_f32p = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+
+# Elements per cell of the debug planes (include/canvaz_film_debug.h)
+DEBUG_PER_CELL = {
+    "h": 1, "m": 1, "mu": 1, "tau": 1, "nn": 1, "delta": 1, "lay": 1, "pres": 2, "fnorm": 2, "flux": 4, "acc": 4,
+    "acc_s": 16, "alpha_s": 4, "alpha": 1, "tmp": 1, "h_frame": 1, "strata_h": 4, "strata_cure": 4,
+    "strata_h2": 4, "strata_cure2": 4, "strata_pig": 64, "strata_pig2": 64, "sub_refl": 16, "color": 4,
+    "fill_src": 1,
+}
+_ELEM_DTYPE = {0: np.float32, 1: np.uint32, 2: np.float16, 3: "bf16", 4: np.int32}
+
+
+def _bf16_to_f32(u16):
+    return (u16.astype(np.uint32) << 16).view(np.float32)
+
+
+def _f32_to_bf16(x):
+    """Round-to-nearest-even f32 -> bf16 bits."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32)
+    r = ((u >> 16) & 1) + 0x7FFF
+    return ((u + r) >> 16).astype(np.uint16)
+
+
+def _lib():
+    L = capi.load_library()
+    if not hasattr(L, "_debug_bound"):
+        vp, i32 = C.c_void_p, C.c_int32
+        for name, args in {
+            "cf_debug_plane_info": [vp, C.c_char_p, C.POINTER(C.c_size_t), C.POINTER(i32)],
+            "cf_debug_read": [vp, C.c_char_p, vp, C.c_size_t],
+            "cf_debug_write": [vp, C.c_char_p, vp, C.c_size_t],
+            "cf_debug_run": [vp, C.c_char_p, vp],
+            "cf_debug_set_params": [vp, C.POINTER(Params)],
+        }.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = i32
+        L.cf_pack_params.argtypes = [C.POINTER(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.c_float,
+                                     C.c_float, C.POINTER(Params), C.POINTER(C.c_uint32)]
+        L.cf_pack_params.restype = i32
+        L._debug_bound = True
+    return L
+
+
+def pack_params(settings, w, h, frame_dt, substeps, h_max=0.0, mu_min=1.0):
+    """cf_pack_params: update_params' packing, host only."""
+    L = _lib()
+    p, n = Params(), C.c_uint32()
+    st = L.cf_pack_params(C.byref(settings), w, h, frame_dt, substeps, h_max, mu_min, C.byref(p), C.byref(n))
+    if st != capi.CF_OK:
+        raise FilmError(st, "cf_pack_params")
+    return p, n.value
+
+
+class Film:
+    """One canvas on the GPU (Film::new, src/film/mod.rs:578)."""
+
+    def __init__(self, settings, w, h, precision=capi.CF_PREC_REFERENCE):
+        self.L = _lib()
+        self.w, self.h, self.n = w, h, w * h
+        self.settings = settings
+        self.precision = precision
+        self.p = C.c_void_p()
+        st = self.L.cf_create(C.byref(settings), w, h, precision, C.byref(self.p))
+        if st != capi.CF_OK:
+            raise FilmError(st, self.L.cf_last_error(None).decode())
+
+    def _check(self, st, what):
+        if st != capi.CF_OK:
+            raise FilmError(st, "%s: %s" % (what, self.L.cf_last_error(self.p).decode()))
+
+    def close(self):
+        if self.p:
+            self.L.cf_destroy(self.p)
+            self.p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tables(self, pigtab, cmf):
+        a = np.ascontiguousarray(pigtab, np.float32)
+        b = np.ascontiguousarray(cmf, np.float32)
+        self._check(self.L.cf_set_tables(self.p, _f32p(a), _f32p(b)), "cf_set_tables")
+
+    def write_state(self, planes, pig_format=None):
+        """Film::write_state: planes is a dict of numpy arrays (oracle layout);
+        strata_pig values are converted to `pig_format` (default: the film's)."""
+        fmt = capi.PREC_TO_PIG[self.precision] if pig_format is None else pig_format
+        keep = {}
+        v = StateView(pig_format=fmt, device=0)
+        for k, dt in (("h", np.float32), ("m", np.float32), ("rheo", np.float32), ("strata_h", np.float32),
+                      ("strata_cure", np.float32), ("lay", np.uint32)):
+            if k in planes:
+                a = np.ascontiguousarray(planes[k], dt)
+                keep[k] = a
+                setattr(v, k, a.ctypes.data)
+        if "sub_refl" in planes:
+            a = np.ascontiguousarray(planes["sub_refl"], np.float32).astype(np.float16)
+            keep["sub_refl"] = a
+            v.sub_refl = a.ctypes.data
+        if "strata_pig" in planes:
+            x = np.ascontiguousarray(planes["strata_pig"], np.float32)
+            if fmt == capi.CF_PIG_F32:
+                a = x
+            elif fmt == capi.CF_PIG_F16:
+                a = x.astype(np.float16)
+            else:
+                a = _f32_to_bf16(x)
+            a = np.ascontiguousarray(a)
+            keep["strata_pig"] = a
+            v.strata_pig = a.ctypes.data
+        self._check(self.L.cf_write_state(self.p, C.byref(v)), "cf_write_state")
+
+    def read_state(self, pig_format=capi.CF_PIG_F32):
+        """Film::read_state as a dict of numpy arrays (pigments as float32)."""
+        n = self.n
+        out = {"h": np.zeros(n, np.float32), "m": np.zeros(n, np.float32), "rheo": np.zeros((n, 2), np.float32),
+               "strata_h": np.zeros((n, 4), np.float32), "strata_cure": np.zeros((n, 4), np.float32),
+               "sub_refl": np.zeros((n, 16), np.float16), "lay": np.zeros(n, np.uint32)}
+        pig = np.zeros((n, 64), np.float32 if pig_format == capi.CF_PIG_F32 else np.uint16)
+        v = StateView(pig_format=pig_format, device=0)
+        for k, a in out.items():
+            setattr(v, k, a.ctypes.data)
+        v.strata_pig = pig.ctypes.data
+        self._check(self.L.cf_read_state(self.p, C.byref(v)), "cf_read_state")
+        if pig_format == capi.CF_PIG_F16:
+            pig = pig.view(np.float16).astype(np.float32)
+        elif pig_format == capi.CF_PIG_BF16:
+            pig = _bf16_to_f32(pig)
+        out["strata_pig"] = pig
+        out["sub_refl"] = out["sub_refl"].astype(np.float32)
+        return out
+
+    def update_params(self, frame_dt, substeps):
+        self._check(self.L.cf_update_params(self.p, frame_dt, substeps), "cf_update_params")
+
+    def choose_substeps(self, frame_dt):
+        n = C.c_uint32()
+        self._check(self.L.cf_choose_substeps(self.p, frame_dt, C.byref(n)), "cf_choose_substeps")
+        return n.value
+
+    def encode_frame(self, substeps=1, stream=None):
+        self._check(self.L.cf_encode_frame(self.p, substeps, stream), "cf_encode_frame")
+
+    def step_adaptive(self, dt_max, stream=None):
+        self._check(self.L.cf_step_adaptive(self.p, dt_max, stream), "cf_step_adaptive")
+
+    def dry_now(self, stream=None):
+        self._check(self.L.cf_dry_now(self.p, stream), "cf_dry_now")
+
+    def sync(self):
+        self._check(self.L.cf_sync(self.p), "cf_sync")
+
+    def params(self):
+        p = Params()
+        self._check(self.L.cf_get_params(self.p, C.byref(p)), "cf_get_params")
+        return p
+
+    def set_params(self, p):
+        self._check(self.L.cf_debug_set_params(self.p, C.byref(p)), "cf_debug_set_params")
+
+    def stats(self):
+        s = Stats()
+        self._check(self.L.cf_get_stats(self.p, C.byref(s)), "cf_get_stats")
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def color(self):
+        """color_tex as float32 (n, 4): linear sRGB + roughness (rgba16f)."""
+        out = np.zeros((self.n, 4), np.uint16)
+        self._check(self.L.cf_read_color(self.p, out.ctypes.data_as(C.POINTER(C.c_uint16))), "cf_read_color")
+        return out.view(np.float16).astype(np.float32)
+
+    def color_device_ptr(self):
+        p = C.c_void_p()
+        self._check(self.L.cf_color_device_ptr(self.p, C.byref(p)), "cf_color_device_ptr")
+        return p.value
+
+    # ---- inspection (include/canvaz_film_debug.h) ----
+    def plane(self, name):
+        """A named device plane as float64/uint32 values (pig/rheo converted)."""
+        nb, el = C.c_size_t(), C.c_int32()
+        self._check(self.L.cf_debug_plane_info(self.p, name.encode(), C.byref(nb), C.byref(el)), name)
+        dt = _ELEM_DTYPE[el.value]
+        raw = np.zeros(nb.value, np.uint8)
+        self._check(self.L.cf_debug_read(self.p, name.encode(), raw.ctypes.data, nb.value), name)
+        if dt == "bf16":
+            return _bf16_to_f32(raw.view(np.uint16)).astype(np.float64)
+        a = raw.view(dt)
+        return a.astype(np.uint64) if dt in (np.uint32,) else a.astype(np.float64)
+
+    def set_plane(self, name, values):
+        nb, el = C.c_size_t(), C.c_int32()
+        self._check(self.L.cf_debug_plane_info(self.p, name.encode(), C.byref(nb), C.byref(el)), name)
+        dt = _ELEM_DTYPE[el.value]
+        v = np.asarray(values).reshape(-1)
+        if dt == "bf16":
+            a = _f32_to_bf16(v.astype(np.float32))
+        else:
+            a = np.ascontiguousarray(v.astype(dt))
+        assert a.nbytes == nb.value, (name, a.nbytes, nb.value)
+        self._check(self.L.cf_debug_write(self.p, name.encode(), a.ctypes.data, a.nbytes), name)
+
+    def run(self, kernel, stream=None):
+        self._check(self.L.cf_debug_run(self.p, kernel.encode(), stream), kernel)

@@ -1,0 +1,673 @@
+// capi.cu — the C ABI of include/canvaz_film.h over the sm_103a kernels.
+//
+// A cf_film owns one device arena holding every per-cell plane (the
+// reference's buffers of Film::new, src/film/mod.rs:586-628, in the same
+// layout) plus the device-resident params and stats.  All entry points return
+// cf_status; CUDA errors are caught and reported through cf_last_error.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/canvaz_film.h"
+#include "film_kernels.h"
+
+using cfk::DevParams;
+using cfk::DevStats;
+
+struct cf_film {
+  cf_settings S;
+  uint32_t w = 0, h = 0, tw = 0, th = 0;
+  int prec = 0;
+  size_t n = 0;
+  cfk::Film F{};
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  DevParams* d_params = nullptr;
+  DevStats* d_stats = nullptr;
+  DevParams* h_params = nullptr;  // pinned staging of the host-packed params
+  cudaEvent_t params_ev = nullptr;  // recorded after the last staging copy
+  float* d_tables = nullptr;
+  cf_params P{};
+  uint32_t implicit_steps = 0;
+  bool params_dirty = true;
+  float h_max_stat = 0.f, mu_min_stat = 1.f, h_max_pending = 0.f;
+  uint32_t frames = 0;
+  int device = 0, sms = 0;
+  std::string err;
+};
+
+static std::string g_create_err;
+
+#define CUDA_TRY(film, expr)                                                           \
+  do {                                                                                 \
+    cudaError_t e_ = (expr);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      (film)->err = std::string(#expr) + ": " + cudaGetErrorString(e_);                \
+      return e_ == cudaErrorMemoryAllocation ? CF_ERR_OUT_OF_MEMORY : CF_ERR_CUDA;     \
+    }                                                                                  \
+  } while (0)
+
+static cf_status fail(cf_film* f, cf_status s, const char* msg) {
+  if (f) f->err = msg;
+  return s;
+}
+
+static float to_rad(float d) { return d * (3.14159265358979323846f / 180.0f); }
+
+static void gravity_vec(const cf_settings& s, float g[3]) {  // src/film/mod.rs:861-867
+  float tilt = to_rad(s.tilt_deg), dir = to_rad(s.tilt_dir_deg);
+  float gxy = s.gravity * std::sin(tilt);
+  g[0] = gxy * std::cos(dir);
+  g[1] = gxy * std::sin(dir);
+  g[2] = std::fmax(s.gravity * std::cos(tilt), 0.0f);
+}
+
+// Film::update_params, src/film/mod.rs:869-917 (f32 arithmetic as in Rust).
+static void pack_params_impl(const cf_settings& s, uint32_t w, uint32_t h, float frame_dt, uint32_t substeps,
+                             float h_max_stat, float h_max_pending, float mu_min_stat, cf_params& P,
+                             uint32_t& implicit_steps) {
+  std::memset(&P, 0, sizeof(P));
+  float dx = s.width_m / (float)w;
+  P.size[0] = w; P.size[1] = h;
+  P.tiles[0] = (w + 63) / 64; P.tiles[1] = (h + 63) / 64;
+  P.dx = dx; P.inv_dx = 1.0f / dx;
+  float g[3];
+  gravity_vec(s, g);
+  float theta = to_rad(s.contact_angle_deg);
+  float pi_a = 3.0f * s.sigma * (1.0f - std::cos(theta)) / s.h_star;
+  float dt = frame_dt / (float)substeps;
+  float m_cap_exp = 0.5f * dx * dx * dx * dx / (32.0f * s.sigma * dt);
+  float m_cap = std::fmax(std::fmin(s.m_cap, m_cap_exp), 1e-14f);
+  float m_exp = 0.1f * dx * dx / (dt * s.rho * std::fmax(g[2], 0.1f));
+  P.dt = dt; P.frame_dt = frame_dt;
+  P.g[0] = g[0]; P.g[1] = g[1]; P.g[2] = g[2]; P.g[3] = s.gravity;
+  P.phys[0] = s.rho; P.phys[1] = s.sigma; P.phys[2] = s.n_index;
+  P.phys[3] = (s.capillary && !s.no_cap) ? m_cap : 0.0f;
+  float lc = std::sqrt(s.sigma / (s.rho * 9.81f));
+  P.ein[0] = std::fmax(std::tan(theta), 0.05f);
+  P.ein[1] = lc * std::sin(0.5f * theta);
+  P.ein[2] = pi_a;
+  P.ein[3] = s.h_min;
+  P.cure[0] = s.cure_rate; P.cure[1] = s.tau_cure; P.cure[2] = s.lnmu_cure; P.cure[3] = s.h_star;
+  P.misc[0] = 2.0e-6f; P.misc[1] = 0.12f; P.misc[2] = s.medium_mu; P.misc[3] = std::fmin(m_exp, s.m_cap_hydro);
+  P.flags[0] = s.debug_view; P.flags[1] = (uint32_t)(s.slump != 0);
+  float lc_z = std::sqrt(s.sigma / (s.rho * std::fmax(g[2], 0.1f)));
+  float cap_explicit = std::fmin(m_exp, s.m_cap_hydro);
+  float h_big = std::fmax(std::fmax(h_max_stat, h_max_pending), 1e-4f);
+  float m_phys = h_big * h_big * h_big / (3.0f * std::fmax(mu_min_stat, 1e-3f)) - cap_explicit;
+  float kappa_frame = frame_dt * s.rho * std::fmax(g[2], 0.1f) / (dx * dx);
+  uint32_t n_i = 0;
+  if (m_phys > 0.0f) {
+    float v = std::fmax(std::ceil(kappa_frame * m_phys / 40.0f), 1.0f);
+    n_i = std::min((uint32_t)v, 4u);
+  }
+  float dt_i = frame_dt / (float)std::max(n_i, 1u);
+  P.front[2] = 40.0f * dx * dx / (dt_i * s.rho * std::fmax(g[2], 0.1f));
+  P.front[3] = dt_i;
+  implicit_steps = s.implicit_hydro ? n_i : 0;
+  float m_phys_cap = h_big * h_big * h_big / (3.0f * std::fmax(mu_min_stat, 1e-3f));
+  float dx2 = dx * dx, dx4 = dx2 * dx2;
+  float m_cap_impl = (s.cap_cond / 28.0f) * dx4 / (dt_i * s.sigma);
+  float m_c = s.capillary_implicit ? std::fmin(m_phys_cap, m_cap_impl) : 0.0f;
+  P.front3[0] = dt_i * s.sigma * m_c / dx4;
+  P.front3[1] = m_c * s.sigma / (dx * dx * dx);
+  P.front3[2] = m_c;
+  P.front3[3] = s.fcap_exp;
+  P.front[0] = s.no_hold ? 0.0f : 2.0f * lc_z * std::sin(0.5f * theta);
+  P.front[1] = dx / lc_z;
+  float hyst = s.hyst_deg >= 0.0f ? s.hyst_deg : s.hysteresis_deg;
+  uint32_t fl = (uint32_t)(s.no_transl != 0) | ((uint32_t)(s.no_shape != 0) << 1);
+  P.front2[0] = to_rad(hyst); P.front2[1] = s.kshape; P.front2[2] = s.kline; P.front2[3] = (float)fl;
+}
+
+static void pack_params(cf_film* f, float frame_dt, uint32_t substeps) {
+  pack_params_impl(f->S, f->w, f->h, frame_dt, substeps, f->h_max_stat, f->h_max_pending, f->mu_min_stat, f->P,
+                   f->implicit_steps);
+  f->params_dirty = true;
+}
+
+static void fill_devparams(cf_film* f, DevParams& D, float dt_max) {
+  std::memset(&D, 0, sizeof(D));
+  D.p = f->P;
+  float g[3];
+  gravity_vec(f->S, g);
+  D.gxy = std::sqrt(g[0] * g[0] + g[1] * g[1]);
+  D.s_rho = f->S.rho; D.s_sigma = f->S.sigma; D.s_vcap = f->S.v_cap; D.s_mcap = f->S.m_cap;
+  D.s_mcap_hydro = f->S.m_cap_hydro; D.s_cap_cond = f->S.cap_cond; D.s_gz = g[2];
+  D.s_capillary = f->S.capillary && !f->S.no_cap;
+  D.s_cap_implicit = f->S.capillary_implicit;
+  D.s_implicit = f->S.implicit_hydro;
+  D.dt_max = dt_max;
+  D.implicit_steps = f->implicit_steps;
+  D.frames = f->frames;
+}
+
+// Copies the host-packed params to the device on `st`.  The pinned staging
+// buffer is rewritten only after the previous copy out of it has executed.
+static cf_status upload_params(cf_film* f, cudaStream_t st, float dt_max = 0.f) {
+  if (!f->params_dirty) return CF_OK;
+  CUDA_TRY(f, cudaEventSynchronize(f->params_ev));
+  fill_devparams(f, *f->h_params, dt_max);
+  CUDA_TRY(f, cudaMemcpyAsync(f->d_params, f->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(f, cudaEventRecord(f->params_ev, st));
+  f->params_dirty = false;
+  return CF_OK;
+}
+
+static cf_status check_launch(cf_film* f) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    f->err = std::string("kernel launch: ") + cudaGetErrorString(e);
+    return CF_ERR_CUDA;
+  }
+  return CF_OK;
+}
+
+extern "C" {
+
+cf_status cf_settings_default(cf_settings* s) {  // FilmSettings::default, src/film/mod.rs:315-350
+  if (!s) return CF_ERR_INVALID_ARG;
+  std::memset(s, 0, sizeof(*s));
+  s->width_m = 1.2f; s->height_m = 0.8f; s->rho = 1000.0f; s->sigma = 0.035f; s->n_index = 1.0f;
+  s->m_cap = 1.0e-8f; s->contact_angle_deg = 45.0f; s->hysteresis_deg = 15.0f; s->h_star = 2.0e-5f;
+  s->raw_canvas = 1; s->weave_um = 25.0f; s->cure_rate = 1.0f / 600.0f; s->tau_cure = 300.0f;
+  s->lnmu_cure = 5.0f; s->v_cap = 1.0f; s->tilt_deg = 0.0f; s->tilt_dir_deg = -90.0f; s->gravity = 9.81f;
+  s->medium_mu = 0.08f; s->debug_view = 0; s->h_min = 1.5e-5f; s->m_cap_hydro = 1.0e-7f;
+  s->max_substeps = 64; s->min_substeps = 4; s->implicit_iters = 40; s->implicit_hydro = 1; s->slump = 0;
+  s->capillary = 1; s->capillary_implicit = 0; s->kshape = 1.0f; s->kline = 0.0f; s->hyst_deg = -1.0f;
+  s->fcap_exp = 2.5f; s->cap_cond = 80.0f; s->all_active = 0;
+  return CF_OK;
+}
+
+const char* cf_last_error(const cf_film* f) { return f ? f->err.c_str() : g_create_err.c_str(); }
+
+cf_status cf_pack_params(const cf_settings* s, uint32_t w, uint32_t h, float frame_dt, uint32_t substeps,
+                         float h_max, float mu_min, cf_params* out, uint32_t* implicit_steps) {
+  if (!s || !out || w == 0 || h == 0 || !(frame_dt > 0.f) || substeps == 0) return CF_ERR_INVALID_ARG;
+  uint32_t ni = 0;
+  pack_params_impl(*s, w, h, frame_dt, substeps, h_max, 0.0f, mu_min, *out, ni);
+  if (implicit_steps) *implicit_steps = ni;
+  return CF_OK;
+}
+
+cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precision, cf_film** out) {
+  if (!s || !out || w == 0 || h == 0 || w > 65536 || h > 65536 || precision < 0 || precision > 2) {
+    g_create_err = "cf_create: invalid argument";
+    return CF_ERR_INVALID_ARG;
+  }
+  if (s->width_m <= 0.f || s->rho <= 0.f || s->sigma <= 0.f || s->h_star <= 0.f) {
+    g_create_err = "cf_create: non-positive physical setting";
+    return CF_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  cf_film* f = new (std::nothrow) cf_film;
+  if (!f) return CF_ERR_OUT_OF_MEMORY;
+  f->S = *s;
+  f->w = w; f->h = h; f->tw = (w + 15) / 16; f->th = (h + 15) / 16; f->prec = precision;
+  f->n = (size_t)w * h;
+  auto bail = [&](cf_status st) {
+    g_create_err = f->err;
+    cf_destroy(f);
+    return st;
+  };
+  if (cudaGetDevice(&f->device) != cudaSuccess) { f->err = "no CUDA device"; return bail(CF_ERR_CUDA); }
+  cudaDeviceGetAttribute(&f->sms, cudaDevAttrMultiProcessorCount, f->device);
+  size_t n = f->n, nt = (size_t)f->tw * f->th, n64 = (size_t)((w + 63) / 64) * ((h + 63) / 64);
+  size_t pig_b = precision == CF_PREC_FP32 ? 4 : 2, rh_b = precision == CF_PREC_BF16 ? 2 : 4;
+  // carve the arena (256-byte aligned planes)
+  struct Slot { void** p; size_t bytes; };
+  std::vector<Slot> slots;
+  cfk::Film& F = f->F;
+  auto add = [&](void** p, size_t b) { slots.push_back({p, b}); };
+  add((void**)&F.hh, 4 * n); add((void**)&F.m, 4 * n); add(&F.mu, rh_b * n); add(&F.tau, rh_b * n);
+  add(&F.nn, rh_b * n); add((void**)&F.delta, 4 * n); add((void**)&F.delta_old, 4 * n);
+  add((void**)&F.lay, 4 * n); add((void**)&F.pres, 8 * n); add((void**)&F.fnorm, 8 * n);
+  add((void**)&F.flux, 16 * n); add((void**)&F.acc, 16 * n); add((void**)&F.acc_s, 64 * n);
+  add((void**)&F.alpha_s, 16 * n); add((void**)&F.alpha, 4 * n); add((void**)&F.tmp, 4 * n);
+  add((void**)&F.h_frame, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
+  add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add(&F.pig, 64 * pig_b * n);
+  add(&F.pig2, 64 * pig_b * n); add((void**)&F.refl, 32 * n); add((void**)&F.color, 8 * n);
+  add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt); add((void**)&F.stats64, 8 * n64);
+  add((void**)&F.fill_src, 4 * n);
+  size_t total = 0;
+  for (auto& sl : slots) total += (sl.bytes + 255) & ~(size_t)255;
+  cudaError_t e = cudaMalloc(&f->arena, total);
+  if (e != cudaSuccess) {
+    f->err = std::string("cudaMalloc arena: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    return bail(CF_ERR_OUT_OF_MEMORY);
+  }
+  f->arena_bytes = total;
+  size_t off = 0;
+  for (auto& sl : slots) {
+    *sl.p = (char*)f->arena + off;
+    off += (sl.bytes + 255) & ~(size_t)255;
+  }
+  if (cudaMalloc(&f->d_params, sizeof(DevParams)) != cudaSuccess ||
+      cudaMalloc(&f->d_stats, sizeof(DevStats)) != cudaSuccess ||
+      cudaMalloc(&f->d_tables, sizeof(float) * (480 + 48)) != cudaSuccess ||
+      cudaMallocHost(&f->h_params, sizeof(DevParams)) != cudaSuccess ||
+      cudaEventCreateWithFlags(&f->params_ev, cudaEventDisableTiming) != cudaSuccess) {
+    f->err = "cudaMalloc params/stats/tables";
+    cudaGetLastError();
+    return bail(CF_ERR_OUT_OF_MEMORY);
+  }
+  F.w = w; F.h = h; F.tw = f->tw; F.th = f->th;
+  F.P = f->d_params; F.stats = f->d_stats;
+  F.pigtab = f->d_tables; F.cmf = f->d_tables + 480;
+  // Film::new: zeroed buffers, substrate refl, weave relief, rheo = (1, 0)
+  if (cudaMemset(f->arena, 0, total) != cudaSuccess || cudaMemset(f->d_tables, 0, sizeof(float) * 528) != cudaSuccess ||
+      cudaMemset(f->d_stats, 0, sizeof(DevStats)) != cudaSuccess) {
+    f->err = "cudaMemset";
+    return bail(CF_ERR_CUDA);
+  }
+  {
+    std::vector<uint16_t> refl(16 * n);
+    float bands[16];
+    for (int b = 0; b < 16; ++b) {
+      float t = (float)b / 15.0f;
+      bands[b] = s->raw_canvas ? 0.50f + 0.16f * t : 0.84f + 0.04f * t;
+    }
+    uint16_t hb[16];
+    for (int b = 0; b < 16; ++b) {  // f32 -> f16 round to nearest even (normal range)
+      uint32_t u;
+      std::memcpy(&u, &bands[b], 4);
+      uint32_t sign = (u >> 16) & 0x8000u;
+      int e8 = (int)((u >> 23) & 0xff) - 127 + 15;
+      uint32_t mant = u & 0x7fffffu;
+      uint32_t r = ((uint32_t)e8 << 10) | (mant >> 13);
+      uint32_t rem = mant & 0x1fffu;
+      if (rem > 0x1000u || (rem == 0x1000u && (r & 1u))) r += 1;
+      hb[b] = (uint16_t)(sign | r);
+    }
+    for (size_t c = 0; c < n; ++c) std::memcpy(&refl[16 * c], hb, 32);
+    std::vector<float> wv(n, 0.0f);
+    float dx = s->width_m / (float)w, amp = s->weave_um * 1e-6f;
+    if (amp > 0.0f) {  // weave, src/film/mod.rs:212-233
+      float k = 6.28318530717958647692f / 1.4e-3f;
+      for (uint32_t j = 0; j < h; ++j) {
+        float y = ((float)j + 0.5f) * dx;
+        for (uint32_t i = 0; i < w; ++i) {
+          float x = ((float)i + 0.5f) * dx;
+          uint32_t hsh = (i * 73856093u) ^ (j * 19349663u);
+          hsh ^= hsh >> 13;
+          hsh *= 0x5bd1e995u;
+          hsh ^= hsh >> 15;
+          float r = (float)(hsh & 0xffff) / 65535.0f * 2.0f - 1.0f;
+          float sv = std::sin(k * x) * std::sin(k * y);
+          wv[(size_t)j * w + i] = amp * (1.0f + 0.6f * sv + 0.4f * r);
+        }
+      }
+    }
+    std::vector<float2> rh(n, make_float2(1.0f, 0.0f));
+    float2* d_rh = nullptr;
+    if (cudaMemcpy(F.refl, refl.data(), 32 * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(F.m, wv.data(), 4 * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMalloc(&d_rh, 8 * n) != cudaSuccess ||
+        cudaMemcpy(d_rh, rh.data(), 8 * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+      f->err = "initial upload";
+      if (d_rh) cudaFree(d_rh);
+      return bail(CF_ERR_CUDA);
+    }
+    cfk::launch_rheo_import(F, precision, d_rh, s->n_index, n, 0);
+    cudaError_t e2 = cudaDeviceSynchronize();
+    cudaFree(d_rh);
+    if (e2 != cudaSuccess) { f->err = cudaGetErrorString(e2); return bail(CF_ERR_CUDA); }
+  }
+  pack_params(f, 1.0f / 60.0f, 1);
+  cf_status st = upload_params(f, 0);
+  if (st != CF_OK) return bail(st);
+  if (cudaDeviceSynchronize() != cudaSuccess) { f->err = "sync"; return bail(CF_ERR_CUDA); }
+  *out = f;
+  return CF_OK;
+}
+
+cf_status cf_destroy(cf_film* f) {
+  if (!f) return CF_ERR_INVALID_ARG;
+  cudaDeviceSynchronize();
+  if (f->arena) cudaFree(f->arena);
+  if (f->d_params) cudaFree(f->d_params);
+  if (f->d_stats) cudaFree(f->d_stats);
+  if (f->d_tables) cudaFree(f->d_tables);
+  if (f->h_params) cudaFreeHost(f->h_params);
+  if (f->params_ev) cudaEventDestroy(f->params_ev);
+  delete f;
+  return CF_OK;
+}
+
+cf_status cf_set_tables(cf_film* f, const float* pigtab, const float* cmf) {
+  if (!f || !pigtab || !cmf) return fail(f, CF_ERR_INVALID_ARG, "cf_set_tables: null");
+  CUDA_TRY(f, cudaMemcpy(f->d_tables, pigtab, sizeof(float) * 480, cudaMemcpyHostToDevice));
+  CUDA_TRY(f, cudaMemcpy(f->d_tables + 480, cmf, sizeof(float) * 48, cudaMemcpyHostToDevice));
+  return CF_OK;
+}
+
+static cf_status copy_plane(cf_film* f, void* dst, const void* src, size_t bytes, int device, bool to_dev) {
+  cudaMemcpyKind k = device ? cudaMemcpyDeviceToDevice : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+  CUDA_TRY(f, cudaMemcpy(dst, src, bytes, k));
+  return CF_OK;
+}
+
+cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
+  if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: null");
+  if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: pig_format");
+  cfk::Film& F = f->F;
+  size_t n = f->n;
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  cf_status st;
+  if (v->h && (st = copy_plane(f, F.hh, v->h, 4 * n, v->device, true)) != CF_OK) return st;
+  if (v->m && (st = copy_plane(f, F.m, v->m, 4 * n, v->device, true)) != CF_OK) return st;
+  if (v->strata_h && (st = copy_plane(f, F.sh, v->strata_h, 16 * n, v->device, true)) != CF_OK) return st;
+  if (v->strata_cure && (st = copy_plane(f, F.scu, v->strata_cure, 16 * n, v->device, true)) != CF_OK) return st;
+  if (v->sub_refl && (st = copy_plane(f, F.refl, v->sub_refl, 32 * n, v->device, true)) != CF_OK) return st;
+  if (v->lay && (st = copy_plane(f, F.lay, v->lay, 4 * n, v->device, true)) != CF_OK) return st;
+  size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2;
+  if (v->rheo || v->strata_pig) {
+    void* tmp = nullptr;
+    size_t need = std::max(v->strata_pig ? 64 * esz * n : 0, v->rheo ? 8 * n : 0);
+    CUDA_TRY(f, cudaMalloc(&tmp, need));
+    if (v->strata_pig) {
+      cudaError_t e = cudaMemcpy(tmp, v->strata_pig, 64 * esz * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) cfk::launch_pig_import(F, f->prec, tmp, v->pig_format, 64 * n, 0);
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
+    }
+    if (v->rheo) {
+      cudaError_t e = cudaMemcpy(tmp, v->rheo, 8 * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) cfk::launch_rheo_import(F, f->prec, (const float2*)tmp, f->S.n_index, n, 0);
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
+    }
+    cudaFree(tmp);
+  }
+  // write_state :1307-1317 — clear scratch, mark every tile moved
+  size_t pig_b = f->prec == CF_PREC_FP32 ? 4 : 2;
+  CUDA_TRY(f, cudaMemset(F.pres, 0, 8 * n));
+  CUDA_TRY(f, cudaMemset(F.flux, 0, 16 * n));
+  CUDA_TRY(f, cudaMemset(F.acc, 0, 16 * n));
+  CUDA_TRY(f, cudaMemset(F.alpha, 0, 4 * n));
+  CUDA_TRY(f, cudaMemset(F.delta, 0, 4 * n));
+  CUDA_TRY(f, cudaMemset(F.tmp, 0, 4 * n));
+  CUDA_TRY(f, cudaMemset(F.acc_s, 0, 64 * n));
+  CUDA_TRY(f, cudaMemset(F.sh2, 0, 16 * n));
+  CUDA_TRY(f, cudaMemset(F.pig2, 0, 64 * pig_b * n));
+  CUDA_TRY(f, cudaMemset(F.alpha_s, 0, 16 * n));
+  cfk::launch_fill_u32(F.tile_moved, 1u, (size_t)f->tw * f->th, 0);
+  // current stats so that the first adaptive step sees this state
+  cfk::launch_reduce(F, f->prec, 0);
+  CUDA_TRY(f, cudaGetLastError());
+  DevStats ds;
+  CUDA_TRY(f, cudaMemcpy(&ds, f->d_stats, sizeof(ds), cudaMemcpyDeviceToHost));
+  float hm, mm;
+  std::memcpy(&hm, &ds.h_max_bits, 4);
+  std::memcpy(&mm, &ds.mu_min_bits, 4);
+  f->h_max_stat = hm;
+  f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  return CF_OK;
+}
+
+cf_status cf_read_state(cf_film* f, const cf_state_view* v) {
+  if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state: null");
+  if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state: pig_format");
+  cfk::Film& F = f->F;
+  size_t n = f->n;
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  cf_status st;
+  if (v->h && (st = copy_plane(f, v->h, F.hh, 4 * n, v->device, false)) != CF_OK) return st;
+  if (v->m && (st = copy_plane(f, v->m, F.m, 4 * n, v->device, false)) != CF_OK) return st;
+  if (v->strata_h && (st = copy_plane(f, v->strata_h, F.sh, 16 * n, v->device, false)) != CF_OK) return st;
+  if (v->strata_cure && (st = copy_plane(f, v->strata_cure, F.scu, 16 * n, v->device, false)) != CF_OK) return st;
+  if (v->sub_refl && (st = copy_plane(f, v->sub_refl, F.refl, 32 * n, v->device, false)) != CF_OK) return st;
+  if (v->lay && (st = copy_plane(f, v->lay, F.lay, 4 * n, v->device, false)) != CF_OK) return st;
+  size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2;
+  if (v->rheo || v->strata_pig) {
+    void* tmp = nullptr;
+    size_t need = std::max(v->strata_pig ? 64 * esz * n : 0, v->rheo ? 8 * n : 0);
+    CUDA_TRY(f, cudaMalloc(&tmp, need));
+    cudaError_t e = cudaSuccess;
+    if (v->strata_pig) {
+      cfk::launch_pig_export(F, f->prec, tmp, v->pig_format, 64 * n, 0);
+      e = cudaDeviceSynchronize();
+      if (e == cudaSuccess) e = cudaMemcpy(v->strata_pig, tmp, 64 * esz * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+    }
+    if (e == cudaSuccess && v->rheo) {
+      cfk::launch_rheo_export(F, f->prec, (float2*)tmp, n, 0);
+      e = cudaDeviceSynchronize();
+      if (e == cudaSuccess) e = cudaMemcpy(v->rheo, tmp, 8 * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+    }
+    cudaFree(tmp);
+    if (e != cudaSuccess) { f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
+  }
+  return CF_OK;
+}
+
+static cf_status post_frame_stats(cf_film* f, cudaStream_t st, bool sync_host) {
+  if (!sync_host) return CF_OK;
+  DevStats ds;
+  CUDA_TRY(f, cudaMemcpyAsync(&ds, f->d_stats, sizeof(ds), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(f, cudaStreamSynchronize(st));
+  float hm, mm;
+  std::memcpy(&hm, &ds.h_max_bits, 4);
+  std::memcpy(&mm, &ds.mu_min_bits, 4);
+  f->h_max_stat = hm;
+  f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
+  return CF_OK;
+}
+
+cf_status cf_update_params(cf_film* f, float frame_dt, uint32_t substeps) {
+  if (!f || !(frame_dt > 0.f) || substeps == 0) return fail(f, CF_ERR_INVALID_ARG, "cf_update_params");
+  pack_params(f, frame_dt, substeps);
+  return CF_OK;
+}
+
+cf_status cf_choose_substeps(cf_film* f, float frame_dt, uint32_t* out) {  // src/film/mod.rs:919-933
+  if (!f || !out || !(frame_dt > 0.f)) return fail(f, CF_ERR_INVALID_ARG, "cf_choose_substeps");
+  cf_status rs = post_frame_stats(f, 0, true);
+  if (rs != CF_OK) return rs;
+  const cf_settings& s = f->S;
+  float g[3];
+  gravity_vec(s, g);
+  float dx = s.width_m / (float)f->w;
+  float gxy = std::sqrt(g[0] * g[0] + g[1] * g[1]);
+  float h_max = std::fmax(std::fmax(f->h_max_stat, f->h_max_pending), 1e-5f);
+  float mu = std::fmax(f->mu_min_stat, 1e-3f);
+  float speed = std::fmin(s.rho * gxy * h_max * h_max / mu, s.v_cap);
+  float dt_cfl = speed > 1e-6f ? 0.5f * dx / speed : frame_dt;
+  float mob = h_max * h_max * h_max / (3.0f * mu);
+  uint32_t n_hyd = (uint32_t)std::fmax(std::ceil(frame_dt * s.rho * g[2] * std::fmin(mob, s.m_cap_hydro) / (0.2f * dx * dx)), 1.0f);
+  float dx2 = dx * dx, dx4 = dx2 * dx2;
+  uint32_t n_cap = (uint32_t)std::fmax(std::ceil(frame_dt * 32.0f * s.sigma * std::fmin(mob, s.m_cap) / dx4), 1.0f);
+  uint32_t n_cfl = (uint32_t)std::fmax(std::ceil(frame_dt / dt_cfl), 1.0f);
+  uint32_t n = std::max(std::max(n_cfl, n_hyd), n_cap);
+  *out = std::min(std::max(n, s.min_substeps), s.max_substeps);
+  return CF_OK;
+}
+
+cf_status cf_encode_frame(cf_film* f, uint32_t substeps, void* stream) {
+  if (!f || substeps == 0 || substeps > 4096) return fail(f, CF_ERR_INVALID_ARG, "cf_encode_frame");
+  if (f->S.implicit_hydro && f->implicit_steps > 0)
+    return fail(f, CF_ERR_UNSUPPORTED, "implicit hydrostatic CG solve is not implemented (set implicit_hydro = 0)");
+  if (f->S.slump) return fail(f, CF_ERR_UNSUPPORTED, "slump pass is not implemented (reference default is off)");
+  cudaStream_t st = (cudaStream_t)stream;
+  cf_status s = upload_params(f, st);
+  if (s != CF_OK) return s;
+  cfk::launch_frame(f->F, f->prec, substeps, f->S.all_active, st);
+  if ((s = check_launch(f)) != CF_OK) return s;
+  f->frames++;
+  return CF_OK;
+}
+
+cf_status cf_step_adaptive(cf_film* f, float dt_max, void* stream) {
+  if (!f || !(dt_max > 0.f)) return fail(f, CF_ERR_INVALID_ARG, "cf_step_adaptive");
+  if (f->S.slump) return fail(f, CF_ERR_UNSUPPORTED, "slump pass is not implemented");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (f->h_params->dt_max != dt_max) f->params_dirty = true;
+  cf_status s = upload_params(f, st, dt_max);
+  if (s != CF_OK) return s;
+  cfk::launch_adaptive_params(f->d_params, f->d_stats, st);
+  cfk::launch_frame(f->F, f->prec, 1, f->S.all_active, st);
+  if ((s = check_launch(f)) != CF_OK) return s;
+  f->frames++;
+  return CF_OK;
+}
+
+cf_status cf_dry_now(cf_film* f, void* stream) {  // src/film/mod.rs:1230-1244
+  if (!f) return CF_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  cf_params saved = f->P;
+  f->P.cure[0] = 4.0f / std::fmax(f->P.frame_dt, 1e-4f);
+  f->params_dirty = true;
+  cf_status s = upload_params(f, st);
+  if (s != CF_OK) return s;
+  cfk::launch_cure(f->F, f->prec, st);
+  if ((s = check_launch(f)) != CF_OK) return s;
+  CUDA_TRY(f, cudaStreamSynchronize(st));  // the pinned staging is reused below
+  f->P = saved;
+  f->params_dirty = true;
+  return upload_params(f, st);
+}
+
+cf_status cf_color_device_ptr(cf_film* f, void** ptr) {
+  if (!f || !ptr) return fail(f, CF_ERR_INVALID_ARG, "cf_color_device_ptr");
+  *ptr = f->F.color;
+  return CF_OK;
+}
+
+cf_status cf_read_color(cf_film* f, uint16_t* out) {
+  if (!f || !out) return fail(f, CF_ERR_INVALID_ARG, "cf_read_color");
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  CUDA_TRY(f, cudaMemcpy(out, f->F.color, 8 * f->n, cudaMemcpyDeviceToHost));
+  return CF_OK;
+}
+
+cf_status cf_get_stats(cf_film* f, cf_stats* out) {
+  if (!f || !out) return fail(f, CF_ERR_INVALID_ARG, "cf_get_stats");
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  cfk::launch_mass(f->F, f->sms, 0);
+  cf_status s = check_launch(f);
+  if (s != CF_OK) return s;
+  DevStats ds;
+  CUDA_TRY(f, cudaMemcpy(&ds, f->d_stats, sizeof(ds), cudaMemcpyDeviceToHost));
+  float hm, mm;
+  std::memcpy(&hm, &ds.h_max_bits, 4);
+  std::memcpy(&mm, &ds.mu_min_bits, 4);
+  f->h_max_stat = hm;
+  f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
+  double dx = (double)f->S.width_m / (double)f->w;
+  out->h_max = hm;
+  out->mu_min = f->mu_min_stat;
+  out->active_tiles = ds.active_tiles;
+  out->frames = f->frames;
+  out->wet_volume = ds.wet_sum * dx * dx;
+  out->relief_volume = ds.relief_sum * dx * dx;
+  out->last_dt = ds.last_dt > 0.f ? (double)ds.last_dt : (double)f->P.dt;
+  out->nan_cells = ds.nan_cells;
+  out->wet_cells = ds.wet_cells;
+  return CF_OK;
+}
+
+cf_status cf_get_params(cf_film* f, cf_params* out) {
+  if (!f || !out) return fail(f, CF_ERR_INVALID_ARG, "cf_get_params");
+  *out = f->P;
+  return CF_OK;
+}
+
+cf_status cf_sync(cf_film* f) {
+  if (!f) return CF_ERR_INVALID_ARG;
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  return post_frame_stats(f, 0, true);
+}
+
+}  // extern "C"
+
+// ---- inspection entry points (include/canvaz_film_debug.h) ----
+#include "../../include/canvaz_film_debug.h"
+
+namespace {
+struct PlaneRef {
+  void* ptr;
+  size_t bytes;
+  int32_t elem;
+};
+bool find_plane(cf_film* f, const std::string& n, PlaneRef& r) {
+  cfk::Film& F = f->F;
+  size_t N = f->n, nt = (size_t)f->tw * f->th;
+  int pe = f->prec == CF_PREC_FP32 ? CF_ELEM_F32 : (f->prec == CF_PREC_BF16 ? CF_ELEM_BF16 : CF_ELEM_F16);
+  size_t pb = f->prec == CF_PREC_FP32 ? 4 : 2;
+  int re = f->prec == CF_PREC_BF16 ? CF_ELEM_BF16 : CF_ELEM_F32;
+  size_t rb = f->prec == CF_PREC_BF16 ? 2 : 4;
+  struct E { const char* name; void* p; size_t b; int32_t e; } tab[] = {
+      {"h", F.hh, 4 * N, CF_ELEM_F32}, {"m", F.m, 4 * N, CF_ELEM_F32}, {"mu", F.mu, rb * N, re},
+      {"tau", F.tau, rb * N, re}, {"nn", F.nn, rb * N, re}, {"delta", F.delta, 4 * N, CF_ELEM_U32},
+      {"lay", F.lay, 4 * N, CF_ELEM_U32}, {"pres", F.pres, 8 * N, CF_ELEM_F32}, {"fnorm", F.fnorm, 8 * N, CF_ELEM_F32},
+      {"flux", F.flux, 16 * N, CF_ELEM_F32}, {"acc", F.acc, 16 * N, CF_ELEM_F32},
+      {"acc_s", F.acc_s, 64 * N, CF_ELEM_F32}, {"alpha_s", F.alpha_s, 16 * N, CF_ELEM_F32},
+      {"alpha", F.alpha, 4 * N, CF_ELEM_F32}, {"tmp", F.tmp, 4 * N, CF_ELEM_F32},
+      {"h_frame", F.h_frame, 4 * N, CF_ELEM_F32}, {"strata_h", F.sh, 16 * N, CF_ELEM_F32},
+      {"strata_cure", F.scu, 16 * N, CF_ELEM_F32}, {"strata_h2", F.sh2, 16 * N, CF_ELEM_F32},
+      {"strata_cure2", F.scu2, 16 * N, CF_ELEM_F32}, {"strata_pig", F.pig, 64 * pb * N, pe},
+      {"strata_pig2", F.pig2, 64 * pb * N, pe}, {"sub_refl", F.refl, 32 * N, CF_ELEM_F16},
+      {"color", F.color, 8 * N, CF_ELEM_F16}, {"tile_flags", F.tile_flags, 4 * nt, CF_ELEM_U32},
+      {"tile_moved", F.tile_moved, 4 * nt, CF_ELEM_U32}, {"fill_src", F.fill_src, 4 * N, CF_ELEM_I32},
+  };
+  for (auto& e : tab)
+    if (n == e.name) { r = {e.p, e.b, e.e}; return true; }
+  return false;
+}
+}  // namespace
+
+extern "C" {
+
+cf_status cf_debug_plane_info(cf_film* f, const char* name, size_t* bytes, int32_t* elem) {
+  if (!f || !name || !bytes || !elem) return fail(f, CF_ERR_INVALID_ARG, "cf_debug_plane_info");
+  PlaneRef r;
+  if (!find_plane(f, name, r)) return fail(f, CF_ERR_INVALID_ARG, "unknown plane");
+  *bytes = r.bytes;
+  *elem = r.elem;
+  return CF_OK;
+}
+
+cf_status cf_debug_read(cf_film* f, const char* name, void* host, size_t bytes) {
+  if (!f || !name || !host) return fail(f, CF_ERR_INVALID_ARG, "cf_debug_read");
+  PlaneRef r;
+  if (!find_plane(f, name, r) || r.bytes != bytes) return fail(f, CF_ERR_INVALID_ARG, "plane name or size");
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  CUDA_TRY(f, cudaMemcpy(host, r.ptr, bytes, cudaMemcpyDeviceToHost));
+  return CF_OK;
+}
+
+cf_status cf_debug_write(cf_film* f, const char* name, const void* host, size_t bytes) {
+  if (!f || !name || !host) return fail(f, CF_ERR_INVALID_ARG, "cf_debug_write");
+  PlaneRef r;
+  if (!find_plane(f, name, r) || r.bytes != bytes) return fail(f, CF_ERR_INVALID_ARG, "plane name or size");
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  CUDA_TRY(f, cudaMemcpy(r.ptr, host, bytes, cudaMemcpyHostToDevice));
+  return CF_OK;
+}
+
+cf_status cf_debug_run(cf_film* f, const char* kernel, void* stream) {
+  if (!f || !kernel) return fail(f, CF_ERR_INVALID_ARG, "cf_debug_run");
+  cudaStream_t st = (cudaStream_t)stream;
+  cf_status s = upload_params(f, st);
+  if (s != CF_OK) return s;
+  if (!cfk::launch_one(f->F, f->prec, kernel, f->S.all_active, st)) return fail(f, CF_ERR_INVALID_ARG, "unknown kernel");
+  if ((s = check_launch(f)) != CF_OK) return s;
+  CUDA_TRY(f, cudaStreamSynchronize(st));
+  return CF_OK;
+}
+
+cf_status cf_debug_set_params(cf_film* f, const cf_params* p) {
+  if (!f || !p) return fail(f, CF_ERR_INVALID_ARG, "cf_debug_set_params");
+  f->P = *p;
+  f->params_dirty = true;
+  return CF_OK;
+}
+
+}  // extern "C"

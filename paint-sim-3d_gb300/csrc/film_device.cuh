@@ -1,0 +1,661 @@
+// film_device.cuh — per-cell device functions of the thin-film step (sm_103a).
+//
+// Each function restates one WGSL helper of the reference; the comment names
+// the shader file and line range it follows.  Arithmetic is FP32 as in the
+// reference; CUDA's own expf/logf/powf/sqrtf/atanf are used throughout.
+//
+// Planes are addressed through `Film`, a POD of device pointers (one per
+// plane, reference layout) that every kernel receives by value.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/canvaz_film.h"
+
+namespace cfk {
+
+constexpr float W_AXIS = 0.6666667f;      // film.wgsl:105
+constexpr float W_DIAG_FLUX = 0.23570226f;  // film.wgsl:106
+constexpr float W_DIAG_LAP = 0.16666667f;   // film.wgsl:107
+constexpr float MOVE_EPS = 1e-6f;           // film.wgsl:108
+constexpr float FRAME_EPS = 2e-6f;          // film.wgsl:109
+constexpr float DRAINED_FILM = 1e-9f;       // film.wgsl:1
+constexpr uint32_t MOVED = 64u;
+constexpr uint32_t ACTIVE = 32u;
+
+// Device-resident parameters: the packed Params uniform plus the settings the
+// adaptive step re-derives dt-dependent fields from.
+struct DevParams {
+  cf_params p;
+  float gxy;            // |g.xy| (m/s^2)
+  float s_rho, s_sigma, s_vcap, s_mcap, s_mcap_hydro, s_cap_cond, s_gz;
+  int32_t s_capillary;  // capillary && !no_cap
+  int32_t s_cap_implicit;
+  int32_t s_implicit;
+  float dt_max;         // adaptive step upper bound
+  uint32_t implicit_steps;
+  uint32_t frames;
+};
+
+// Global reductions written by the stats kernels.
+struct DevStats {
+  uint32_t h_max_bits;   // max h over cells with h > 4 h_min (float bits, h >= 0)
+  uint32_t mu_min_bits;  // min mu over the same cells (float bits, mu > 0)
+  uint32_t active_tiles;
+  uint32_t nan_flag;
+  double wet_sum;        // sum(h)
+  double relief_sum;     // sum(m)
+  unsigned long long wet_cells;
+  unsigned long long nan_cells;
+  float last_dt;
+  float pad;
+};
+
+template <int MODE> struct Prec;
+template <> struct Prec<CF_PREC_REFERENCE> { using Pig = __half; using Rh = float; };
+template <> struct Prec<CF_PREC_FP32> { using Pig = float; using Rh = float; };
+template <> struct Prec<CF_PREC_BF16> { using Pig = __nv_bfloat16; using Rh = __nv_bfloat16; };
+
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <class T> __device__ __forceinline__ T from_f(float v);
+template <> __device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// All device planes of one film (reference layout; pig / rheo element types
+// depend on the precision mode and are reinterpreted by the kernels).
+struct Film {
+  uint32_t w, h, tw, th;  // grid and 16x16 tile counts
+  const DevParams* P;
+  DevStats* stats;
+  float* hh;       // h
+  float* m;
+  void* mu;        // rheo.x  (Rh)
+  void* tau;       // rheo.y  (Rh)
+  void* nn;        // power-law index (Rh)
+  uint32_t* delta;
+  uint32_t* delta_old;
+  uint32_t* lay;
+  float2* pres;
+  float2* fnorm;
+  float4* flux;
+  float4* acc;
+  float4* acc_s;   // 4 per cell
+  float4* alpha_s;
+  float* alpha;
+  float* tmp;
+  float* h_frame;
+  float4* sh;      // strata_h
+  float4* scu;     // strata_cure
+  float4* sh2;
+  float4* scu2;
+  void* pig;       // 64 Pig per cell
+  void* pig2;
+  uint16_t* refl;  // 16 half per cell
+  ushort4* color;  // rgba16f
+  uint32_t* tile_flags;
+  uint32_t* tile_moved;
+  float2* stats64; // per 64x64 tile (h_max, mu_min)
+  int32_t* fill_src;
+  const float* pigtab;  // 12 x 40
+  const float* cmf;     // 16 x 3
+};
+
+struct Cell {
+  int i, j;
+  uint32_t c;
+};
+
+__device__ __forceinline__ uint32_t idx(const Film& F, int i, int j) { return (uint32_t)j * F.w + (uint32_t)i; }
+__device__ __forceinline__ bool in_grid(const Film& F, int i, int j) {
+  return i >= 0 && j >= 0 && i < (int)F.w && j < (int)F.h;
+}
+__device__ __forceinline__ bool cell_active(const Film& F, int i, int j) {  // film.wgsl:128-131
+  return (F.tile_flags[(uint32_t)(i >> 4) + (uint32_t)(j >> 4) * F.tw] & ACTIVE) != 0u;
+}
+__device__ __forceinline__ int refl_i(const Film& F, int i) {  // common.wgsl:152-158
+  int w = (int)F.w, r = i;
+  if (r < 0) r = -r - 1;
+  if (r >= w) r = 2 * w - r - 1;
+  return min(max(r, 0), w - 1);
+}
+__device__ __forceinline__ int refl_j(const Film& F, int j) {
+  int hh = (int)F.h, r = j;
+  if (r < 0) r = -r - 1;
+  if (r >= hh) r = 2 * hh - r - 1;
+  return min(max(r, 0), hh - 1);
+}
+
+template <int MODE>
+__device__ __forceinline__ float rmu(const Film& F, uint32_t c) {
+  return to_f(((const typename Prec<MODE>::Rh*)F.mu)[c]);
+}
+template <int MODE>
+__device__ __forceinline__ float rtau(const Film& F, uint32_t c) {
+  return to_f(((const typename Prec<MODE>::Rh*)F.tau)[c]);
+}
+template <int MODE>
+__device__ __forceinline__ float rn(const Film& F, uint32_t c) {
+  return to_f(((const typename Prec<MODE>::Rh*)F.nn)[c]);
+}
+template <int MODE>
+__device__ __forceinline__ void set_rheo(const Film& F, uint32_t c, float mu, float tau, float n) {
+  using Rh = typename Prec<MODE>::Rh;
+  ((Rh*)F.mu)[c] = from_f<Rh>(mu);
+  ((Rh*)F.tau)[c] = from_f<Rh>(tau);
+  ((Rh*)F.nn)[c] = from_f<Rh>(n);
+}
+
+// IEEE half bits <-> float without type punning.
+__device__ __forceinline__ float h16_to_f(uint32_t bits) { return __half2float(__ushort_as_half((unsigned short)bits)); }
+__device__ __forceinline__ uint32_t f_to_h16(float v) { return (uint32_t)__half_as_ushort(__float2half_rn(v)); }
+
+// ---- pigment slots: 16 per stratum, 4 strata per cell ----
+template <class T>
+__device__ __forceinline__ void load_pig16(const T* base, float o[16]) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) o[q] = to_f(base[q]);
+}
+template <>
+__device__ __forceinline__ void load_pig16<__half>(const __half* base, float o[16]) {
+  const uint4* p = reinterpret_cast<const uint4*>(base);
+  uint4 a = p[0], b = p[1];
+  uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    o[2 * k] = h16_to_f(wv[k] & 0xffffu);
+    o[2 * k + 1] = h16_to_f(wv[k] >> 16);
+  }
+}
+template <>
+__device__ __forceinline__ void load_pig16<__nv_bfloat16>(const __nv_bfloat16* base, float o[16]) {
+  const uint4* p = reinterpret_cast<const uint4*>(base);
+  uint4 a = p[0], b = p[1];
+  uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    o[2 * k] = __uint_as_float(wv[k] << 16);
+    o[2 * k + 1] = __uint_as_float(wv[k] & 0xffff0000u);
+  }
+}
+template <>
+__device__ __forceinline__ void load_pig16<float>(const float* base, float o[16]) {
+  const float4* p = reinterpret_cast<const float4*>(base);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float4 v = p[k];
+    o[4 * k] = v.x; o[4 * k + 1] = v.y; o[4 * k + 2] = v.z; o[4 * k + 3] = v.w;
+  }
+}
+template <class T>
+__device__ __forceinline__ void store_pig16(T* base, const float v[16]) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) base[q] = from_f<T>(v[q]);
+}
+template <>
+__device__ __forceinline__ void store_pig16<float>(float* base, const float v[16]) {
+  float4* p = reinterpret_cast<float4*>(base);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) p[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+}
+template <>
+__device__ __forceinline__ void store_pig16<__half>(__half* base, const float v[16]) {
+  uint32_t wv[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) wv[k] = f_to_h16(v[2 * k]) | (f_to_h16(v[2 * k + 1]) << 16);
+  uint4* p = reinterpret_cast<uint4*>(base);
+  p[0] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+  p[1] = make_uint4(wv[4], wv[5], wv[6], wv[7]);
+}
+template <>
+__device__ __forceinline__ void store_pig16<__nv_bfloat16>(__nv_bfloat16* base, const float v[16]) {
+  uint32_t wv[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    wv[k] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * k])) |
+            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * k + 1])) << 16);
+  }
+  uint4* p = reinterpret_cast<uint4*>(base);
+  p[0] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+  p[1] = make_uint4(wv[4], wv[5], wv[6], wv[7]);
+}
+// Raw copy of one stratum's 16 slots (bit exact).
+template <class T>
+__device__ __forceinline__ void copy_pig16(T* dst, const T* src) {
+  constexpr int W = 16 * sizeof(T) / 16;
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+  for (int k = 0; k < W; ++k) d[k] = s[k];
+}
+template <class T>
+__device__ __forceinline__ void zero_pig16(T* dst) {
+  constexpr int W = 16 * sizeof(T) / 16;
+  uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+  for (int k = 0; k < W; ++k) d[k] = make_uint4(0, 0, 0, 0);
+}
+template <int MODE>
+__device__ __forceinline__ typename Prec<MODE>::Pig* pig_at(void* base, uint32_t c, int k) {
+  return reinterpret_cast<typename Prec<MODE>::Pig*>(base) + (size_t)c * 64 + 16 * k;
+}
+
+__device__ __forceinline__ float half_at(const uint16_t* p, int k) {
+  return __half2float(__ushort_as_half(p[k]));
+}
+
+// ---- film.wgsl helpers ----
+
+// film.wgsl:570-585
+__device__ __forceinline__ uint32_t pack_off(int dx, int dy) {
+  uint32_t ux = (uint32_t)min(max(dx + 128, 0), 255);
+  uint32_t uy = (uint32_t)min(max(dy + 128, 0), 255);
+  return (ux << 8) | uy | 0x10000u;
+}
+__device__ __forceinline__ void unpack_off(uint32_t bits, int& ox, int& oy) {
+  if ((bits & 0x10000u) == 0u) { ox = 64; oy = 64; return; }
+  ox = (int)((bits >> 8) & 0xffu) - 128;
+  oy = (int)(bits & 0xffu) - 128;
+}
+__device__ __forceinline__ float off_len(int ox, int oy) { return sqrtf((float)(ox * ox + oy * oy)); }
+__device__ __forceinline__ float nose_dist(const Film& F, uint32_t c) {
+  int ox, oy;
+  unpack_off(F.delta[c], ox, oy);
+  return off_len(ox, oy);
+}
+// film.wgsl:153-156
+__device__ __forceinline__ float hold_level(const cf_params& P, float d) {
+  return P.front[0] * (1.0f - expf(-(fmaxf(d, 1.0f) - 0.5f) * P.front[1]));
+}
+// common.wgsl:190-195
+__device__ __forceinline__ float disjoining(const cf_params& P, float hv) {
+  float x = fmaxf(1.0f - hv / P.cure[3], 0.0f);
+  return P.ein[2] * x * x;
+}
+__device__ __forceinline__ float sgnf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+
+// film.wgsl:94-107 with the evaluation's power-law index n
+__device__ __forceinline__ void hb_flux(float gmag, float hf, float mu, float ty, float n, float& q, float& y,
+                                        float& up) {
+  q = 0.f; y = 0.f; up = 0.f;
+  if (gmag < 1e-9f || hf <= 0.f) return;
+  float yy = fmaxf(hf - ty / gmag, 0.f);
+  if (yy <= 0.f) return;
+  float u;
+  if (fabsf(n - 1.0f) < 1e-4f) u = 0.5f * gmag / mu * yy * yy;
+  else u = n / (n + 1.0f) * powf(gmag / mu, 1.0f / n) * powf(yy, (n + 1.0f) / n);
+  q = u * (hf - n * yy / (2.0f * n + 1.0f));
+  y = yy;
+  up = u;
+}
+// film.wgsl:109-126
+__device__ __forceinline__ float band_flux(float up, float y, float za, float zb, float n) {
+  float ta = 0.f, tb = 0.f;
+  if (y > 0.f) {
+    float ra = fmaxf(y - za, 0.f) / y;
+    float rb = fmaxf(y - zb, 0.f) / y;
+    if (fabsf(n - 1.0f) < 1e-4f) {
+      ta = ra * ra * ra;
+      tb = rb * rb * rb;
+    } else {
+      float e = (2.0f * n + 1.0f) / n;
+      ta = powf(ra, e);
+      tb = powf(rb, e);
+    }
+  }
+  return up * ((zb - za) - n / (2.0f * n + 1.0f) * y * (ta - tb));
+}
+
+// film.wgsl:147-151
+__device__ __forceinline__ float usurf(const Film& F, const cf_params& P, int i, int j) {
+  uint32_t c = idx(F, refl_i(F, i), refl_j(F, j));
+  float hv = F.hh[c];
+  float hold = 0.f;
+  if (hv > 0.f) hold = hold_level(P, nose_dist(F, c));
+  return hv + F.m[c] - hold;
+}
+// film.wgsl:190-201
+__device__ __forceinline__ float line_pressure(const Film& F, const cf_params& P, int i, int j) {
+  if (i < 1 || j < 1 || i + 1 >= (int)F.w || j + 1 >= (int)F.h) return 0.f;
+  float2 nl = F.fnorm[idx(F, i - 1, j)], nr = F.fnorm[idx(F, i + 1, j)];
+  float2 nd = F.fnorm[idx(F, i, j - 1)], nu = F.fnorm[idx(F, i, j + 1)];
+  if (nl.x * nl.x + nl.y * nl.y < 0.5f || nr.x * nr.x + nr.y * nr.y < 0.5f || nd.x * nd.x + nd.y * nd.y < 0.5f ||
+      nu.x * nu.x + nu.y * nu.y < 0.5f)
+    return 0.f;
+  float curv = (nr.x - nl.x + nu.y - nd.y) * 0.5f * P.inv_dx;
+  return P.phys[1] * curv * P.front2[2];
+}
+
+// film.wgsl:134-145
+__device__ __forceinline__ uint32_t feeders(const Film& F, const cf_params& P, uint32_t c) {
+  int i = (int)(c % F.w), j = (int)(c / F.w);
+  float thr = 2.0f * F.hh[c] + P.ein[3];
+  uint32_t n = 0;
+  if (i > 0 && F.hh[idx(F, i - 1, j)] > thr) n++;
+  if (i + 1 < (int)F.w && F.hh[idx(F, i + 1, j)] > thr) n++;
+  if (j > 0 && F.hh[idx(F, i, j - 1)] > thr) n++;
+  if (j + 1 < (int)F.h && F.hh[idx(F, i, j + 1)] > thr) n++;
+  return n;
+}
+// film.wgsl:160-180
+__device__ inline float2 front_normal(const Film& F, const cf_params& P, uint32_t c) {
+  int i = (int)(c % F.w), j = (int)(c / F.w);
+  float dx = 0.f, dy = 0.f;
+#pragma unroll
+  for (int dj = -2; dj <= 2; ++dj)
+#pragma unroll
+    for (int di = -2; di <= 2; ++di) {
+      if (di == 0 && dj == 0) continue;
+      if (di * di + dj * dj > 5) continue;
+      int x = i + di, y = j + dj;
+      if (!in_grid(F, x, y)) continue;
+      if (F.hh[idx(F, x, y)] <= P.ein[3]) {
+        float dd = (float)(di * di + dj * dj);
+        dx += (float)di / dd;
+        dy += (float)dj / dd;
+      }
+    }
+  float l = sqrtf(dx * dx + dy * dy);
+  if (l < 1e-6f) return make_float2(0.f, 0.f);
+  return make_float2(dx / l, dy / l);
+}
+// film.wgsl:182-188
+__device__ __forceinline__ float wet_gain(float2 n) {
+  const float s2 = 0.70710678f;
+  float w = W_AXIS * (fmaxf(n.x, 0.f) + fmaxf(-n.x, 0.f) + fmaxf(n.y, 0.f) + fmaxf(-n.y, 0.f));
+  w += W_DIAG_FLUX * (fmaxf(s2 * (n.x + n.y), 0.f) + fmaxf(-s2 * (n.x + n.y), 0.f) + fmaxf(s2 * (n.x - n.y), 0.f) +
+                      fmaxf(-s2 * (n.x - n.y), 0.f));
+  float mm = fmaxf(fmaxf(fabsf(n.x), fabsf(n.y)), 1e-3f);
+  return 1.0f / (mm * fmaxf(w, 1e-3f));
+}
+// film.wgsl:203-222
+__device__ inline float front_shape(const Film& F, const cf_params& P, uint32_t c, float2 n) {
+  int i = (int)(c % F.w), j = (int)(c / F.w);
+  float w = 0.f, w0 = 0.f;
+  for (int dj = -3; dj <= 3; ++dj)
+    for (int di = -3; di <= 3; ++di) {
+      if (di == 0 && dj == 0) continue;
+      if (di * di + dj * dj > 9) continue;
+      if ((float)di * n.x + (float)dj * n.y < -0.5f) w0 += 1.f;
+      int x = i + di, y = j + dj;
+      if (!in_grid(F, x, y)) continue;
+      if (F.hh[idx(F, x, y)] > P.ein[3]) w += 1.f;
+    }
+  if (w0 < 1.f || ((uint32_t)P.front2[3] & 2u) != 0u) return 1.f;
+  return powf(fminf(fmaxf(w / w0, 0.f), 2.5f), P.front2[1]);
+}
+// film.wgsl:224-229
+template <int MODE>
+__device__ __forceinline__ float wet_threshold(const Film& F, const DevParams& D, uint32_t c) {
+  const cf_params& P = D.p;
+  float ty = rtau<MODE>(F, c);
+  float need = fmaxf(ty / (P.phys[0] * fmaxf(F.hh[c], 1e-4f)) - D.gxy, 0.f);
+  float ycap = need / fmaxf(P.g[2], 1e-3f) * P.dx;
+  return fmaxf(hold_level(P, 1.0f), ycap);
+}
+__device__ __forceinline__ float front_dist(const Film& F, uint32_t c) {  // film.wgsl:231-234
+  if (F.hh[c] <= 0.f) return 0.f;
+  return nose_dist(F, c);
+}
+// film.wgsl:236-244
+__device__ __forceinline__ float cox_speed(const cf_params& P, float excess, float mu) {
+  if (excess <= 0.f) return 0.f;
+  float theta = atanf(P.ein[0]);
+  float span = fmaxf(P.front[0] - hold_level(P, 1.0f), 1e-6f);
+  float th = theta + (3.14159265f - theta) * fminf(fmaxf(excess / span, 0.f), 1.f);
+  float adv = fminf(theta + P.front2[0], 3.1f);
+  if (th <= adv) return 0.f;
+  return P.phys[1] * (th * th * th - adv * adv * adv) / (132.0f * fmaxf(mu, 1e-4f));
+}
+// film.wgsl:246-265
+__device__ inline float cell_excess(const Film& F, const cf_params& P, uint32_t c) {
+  float e = F.hh[c] - hold_level(P, front_dist(F, c));
+  int ox, oy;
+  unpack_off(F.delta[c], ox, oy);
+  float ol = off_len(ox, oy);
+  if (ol > 0.5f && ol < 60.0f) {
+    float dirx = (float)ox * (-1.0f / ol), diry = (float)oy * (-1.0f / ol);
+    float bx = 0.5f * sgnf((float)(-ox)), by = 0.5f * sgnf((float)(-oy));
+    int ci = (int)(c % F.w), cj = (int)(c / F.w);
+    for (uint32_t k = 0; k < 3; ++k) {
+      float reach = (float)(4u << k);
+      int sx = (int)(dirx * reach + bx), sy = (int)(diry * reach + by);  // toward zero
+      int ri = ci + sx, rj = cj + sy;
+      if (!in_grid(F, ri, rj)) break;
+      uint32_t cr = idx(F, ri, rj);
+      if (F.hh[cr] <= 0.f) break;
+      e = fmaxf(e, F.hh[cr] - hold_level(P, front_dist(F, cr)));
+    }
+  }
+  return e;
+}
+// film.wgsl:267-295: (speed term, direction sign)
+template <int MODE>
+__device__ float2 rim_translation(const Film& F, const cf_params& P, uint32_t ca, uint32_t cb, float hf, float2 fd) {
+  if (((uint32_t)P.front2[3] & 1u) != 0u) return make_float2(0.f, 0.f);
+  float da = front_dist(F, ca), db = front_dist(F, cb);
+  if (fmaxf(da, db) > 3.0f / P.front[1]) return make_float2(0.f, 0.f);
+  float ha = F.hh[ca], hb = F.hh[cb];
+  float2 n = make_float2(0.f, 0.f);
+  if (da > db && ha > 0.f) n = F.fnorm[ca];
+  else if (db > da && hb > 0.f) n = F.fnorm[cb];
+  else {
+    if (ha > 0.f) { float2 a = F.fnorm[ca]; n.x += a.x; n.y += a.y; }
+    if (hb > 0.f) { float2 b = F.fnorm[cb]; n.x += b.x; n.y += b.y; }
+  }
+  float nl = sqrtf(n.x * n.x + n.y * n.y);
+  if (nl < 1e-6f) return make_float2(0.f, 0.f);
+  n.x = n.x / nl;
+  n.y = n.y / nl;
+  float s = n.x * fd.x + n.y * fd.y;
+  if (fabsf(s) < 1e-4f) return make_float2(0.f, 0.f);
+  uint32_t src = ca, dst = cb;
+  if (s < 0.f) { src = cb; dst = ca; }
+  if (F.hh[src] <= 0.f) return make_float2(0.f, 0.f);
+  float e = cell_excess(F, P, src);
+  if (e <= 0.f) return make_float2(0.f, 0.f);
+  float e_out = -hold_level(P, 1.0f);
+  if (F.hh[dst] > 0.f) e_out = cell_excess(F, P, dst);
+  float room = fminf(fmaxf(1.0f - fmaxf(e_out, 0.f) / e, 0.f), 1.f);
+  float u = cox_speed(P, e, rmu<MODE>(F, src));
+  float t = P.front2[0];
+  float mixv = 1.0f * (1.0f - t) + fabsf(s) * t;
+  return make_float2(u * hf * room * mixv, sgnf(s));
+}
+
+struct FaceOut {
+  float q, y, up, n;
+};
+
+// film.wgsl:297-372 (face between cell a and neighbour b)
+template <int MODE>
+__device__ FaceOut face(const Film& F, const DevParams& D, uint32_t ca, uint32_t cb, float2 gcap, float2 ghyd,
+                        float2 gtilt, bool diag, float2 fd) {
+  const cf_params& P = D.p;
+  FaceOut out = {0.f, 0.f, 0.f, 0.f};
+  float ha = F.hh[ca], hb = F.hh[cb];
+  float hf = 0.5f * (ha + hb);
+  if (hf <= 0.f) return out;
+  float shape = 1.f, proj = 1.f;
+  bool wetting = false;
+  if (fminf(ha, hb) <= 0.f) {
+    uint32_t wet = ha > 0.f ? ca : cb;
+    uint32_t dry = ha > 0.f ? cb : ca;
+    if (F.hh[wet] <= wet_threshold<MODE>(F, D, wet)) return out;
+    wetting = true;
+    float2 n = F.fnorm[wet];
+    if (n.x * n.x + n.y * n.y < 0.5f) n = front_normal(F, P, wet);
+    float toward = ha > 0.f ? 1.f : -1.f;
+    proj = fmaxf(n.x * (fd.x * toward) + n.y * (fd.y * toward), 0.f);
+    if (proj <= 0.f) return out;
+    shape = front_shape(F, P, dry, n) * wet_gain(n);
+    if (shape <= 0.f) return out;
+  }
+  float rax = rmu<MODE>(F, ca), ray = rtau<MODE>(F, ca);
+  float rbx = rmu<MODE>(F, cb), rby = rtau<MODE>(F, cb);
+  float wa = ha / (ha + hb);
+  float wb = 1.0f - wa;
+  float mu = expf(wa * logf(fmaxf(rax, 1e-4f)) + wb * logf(fmaxf(rbx, 1e-4f)));
+  float ty = wa * ray + wb * rby;
+  float na = rn<MODE>(F, ca), nb = rn<MODE>(F, cb);
+  float nf = na == nb ? na : wa * na + wb * nb;
+  float thin = fminf(ha, hb) / hf;
+  float fcap = thin * thin * thin;
+  // yield_cap (film.wgsl:44-49)
+  float2 yc = make_float2(gcap.x * fcap, gcap.y * fcap);
+  {
+    float gcl = sqrtf(yc.x * yc.x + yc.y * yc.y);
+    float gc_max = P.phys[1] / (1e-3f * 1e-3f);
+    if (!(ty <= 0.f || gcl <= gc_max)) {
+      float sc = gc_max / gcl;
+      yc.x = yc.x * sc;
+      yc.y = yc.y * sc;
+    }
+  }
+  float2 gg = make_float2(yc.x + ghyd.x + gtilt.x, yc.y + ghyd.y + gtilt.y);
+  float gmag = sqrtf(gg.x * gg.x + gg.y * gg.y);
+  float ydep = hf;  // yield_depth (film.wgsl:89-92)
+  if (ty > 0.f) ydep = gg.x >= 0.f ? ha : hb;
+  float qq, qy, qup;
+  hb_flux(gmag, ydep, mu, ty, nf, qq, qy, qup);
+  float meff = qq > 0.f ? qq / fmaxf(gmag, 1e-9f) : 0.f;
+  float mtilt = meff;
+  if (ty > 0.f) {  // plug_mobility (film.wgsl:51-56)
+    float gb = sqrtf(gtilt.x * gtilt.x + gtilt.y * gtilt.y);
+    if (gb < 1e-6f) mtilt = 0.f;
+    else {
+      uint32_t up = gtilt.x >= 0.f ? ca : cb;
+      mtilt = F.tmp[up] * F.hh[up] / gb;
+    }
+  }
+  if (meff <= 0.f && mtilt <= 0.f) return out;
+  float fcap2 = powf(thin, P.front3[3]);
+  float qn = mtilt * gtilt.x + fminf(meff, P.misc[3]) * ghyd.x + fminf(meff, P.phys[3]) * (gcap.x * fcap2);
+  float2 tr = rim_translation<MODE>(F, P, ca, cb, hf, fd);
+  const float vcap = 2.f;
+  if (wetting) {
+    uint32_t wet = ha > 0.f ? ca : cb;
+    float want = tr.x * 2.0f * F.hh[wet] / fmaxf(hf, 1e-9f);
+    qn = tr.y * fmaxf(qn * tr.y * proj, want) * shape;
+    if (fabsf(qn) > vcap * hf) qn = sgnf(qn) * vcap * hf;
+  } else {
+    if (tr.x > 0.f) qn = tr.y * fmaxf(qn * tr.y, tr.x);
+    if (fabsf(qn) > vcap * hf) qn = sgnf(qn) * vcap * hf;
+    float lo = fminf(ha, hb), hi = fmaxf(ha, hb);
+    if (lo < 0.5f * hi) {
+      if (diag) qn = 0.f;
+      else {
+        uint32_t tgt = cb;
+        if (hb > ha) tgt = ca;
+        uint32_t nfd = feeders(F, P, tgt);
+        qn = qn / powf((float)max(nfd, 1u), 0.7f);
+      }
+    }
+  }
+  out.q = qn;
+  out.y = qy;
+  out.up = qup;
+  out.n = nf;
+  return out;
+}
+
+__device__ __forceinline__ float2 pres_at(const Film& F, int i, int j) {
+  return F.pres[idx(F, refl_i(F, i), refl_j(F, j))];
+}
+__device__ __forceinline__ float2 pres_wet(const Film& F, int i, int j, float2 fb) {
+  uint32_t c = idx(F, refl_i(F, i), refl_j(F, j));
+  float2 p = F.pres[c];
+  if (F.hh[c] > 0.f) return p;
+  return make_float2(fb.x, p.y);
+}
+
+// film.wgsl:375-446, face k in {0: +x, 1: +y, 2: +x+y, 3: +x-y}
+template <int MODE>
+__device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k) {
+  const cf_params& P = D.p;
+  FaceOut z = {0.f, 0.f, 0.f, 0.f};
+  const float s2 = 0.70710678f;
+  uint32_t c = idx(F, i, j);
+  float2 p00 = pres_at(F, i, j);
+  float2 gxy = make_float2(P.phys[0] * P.g[0], P.phys[0] * P.g[1]);
+  if (k == 0) {
+    if (!(i + 1 < (int)F.w && cell_active(F, i + 1, j))) return z;
+    uint32_t cb = idx(F, i + 1, j);
+    float2 p10 = pres_at(F, i + 1, j);
+    float2 gm = make_float2(-(p10.x - p00.x) * P.inv_dx, -(p10.y - p00.y) * P.inv_dx);
+    float2 a = pres_wet(F, i, j + 1, p00), b = pres_wet(F, i + 1, j + 1, p10);
+    float2 cc = pres_wet(F, i, j - 1, p00), d = pres_wet(F, i + 1, j - 1, p10);
+    float2 pt = make_float2(a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y);
+    float2 gt = make_float2(-pt.x * 0.25f * P.inv_dx, -pt.y * 0.25f * P.inv_dx);
+    FaceOut f = face<MODE>(F, D, c, cb, make_float2(gm.x, gt.x), make_float2(gm.y, gt.y), gxy, false,
+                           make_float2(1.f, 0.f));
+    f.q *= W_AXIS;
+    return f;
+  }
+  if (k == 1) {
+    if (!(j + 1 < (int)F.h && cell_active(F, i, j + 1))) return z;
+    uint32_t cb = idx(F, i, j + 1);
+    float2 p01 = pres_at(F, i, j + 1);
+    float2 gm = make_float2(-(p01.x - p00.x) * P.inv_dx, -(p01.y - p00.y) * P.inv_dx);
+    float2 a = pres_wet(F, i + 1, j, p00), b = pres_wet(F, i + 1, j + 1, p01);
+    float2 cc = pres_wet(F, i - 1, j, p00), d = pres_wet(F, i - 1, j + 1, p01);
+    float2 pt = make_float2(a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y);
+    float2 gt = make_float2(-pt.x * 0.25f * P.inv_dx, -pt.y * 0.25f * P.inv_dx);
+    FaceOut f = face<MODE>(F, D, c, cb, make_float2(gm.x, gt.x), make_float2(gm.y, gt.y), make_float2(gxy.y, gxy.x),
+                           false, make_float2(0.f, 1.f));
+    f.q *= W_AXIS;
+    return f;
+  }
+  float hs = P.ein[3];
+  if (k == 2) {
+    if (!(i + 1 < (int)F.w && j + 1 < (int)F.h && cell_active(F, i + 1, j + 1))) return z;
+    uint32_t cb = idx(F, i + 1, j + 1);
+    float2 p11 = pres_at(F, i + 1, j + 1);
+    float2 ga = make_float2(-(p11.x - p00.x) * P.inv_dx * s2, -(p11.y - p00.y) * P.inv_dx * s2);
+    float2 pa = pres_wet(F, i + 1, j, p00), pb = pres_wet(F, i, j + 1, p11);
+    float2 gp = make_float2(-(pa.x - pb.x) * P.inv_dx * s2, -(pa.y - pb.y) * P.inv_dx * s2);
+    float2 gt = make_float2((gxy.x + gxy.y) * s2, (gxy.x - gxy.y) * s2);
+    bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j + 1)] > hs;
+    if (!open) return z;
+    FaceOut f = face<MODE>(F, D, c, cb, make_float2(ga.x, gp.x), make_float2(ga.y, gp.y), gt, true,
+                           make_float2(s2, s2));
+    f.q *= W_DIAG_FLUX;
+    return f;
+  }
+  if (!(i + 1 < (int)F.w && j > 0 && cell_active(F, i + 1, j - 1))) return z;
+  uint32_t cb = idx(F, i + 1, j - 1);
+  float2 p1m = pres_at(F, i + 1, j - 1);
+  float2 ga = make_float2(-(p1m.x - p00.x) * P.inv_dx * s2, -(p1m.y - p00.y) * P.inv_dx * s2);
+  float2 pa = pres_wet(F, i + 1, j, p00), pb = pres_wet(F, i, j - 1, p1m);
+  float2 gp = make_float2(-(pa.x - pb.x) * P.inv_dx * s2, -(pa.y - pb.y) * P.inv_dx * s2);
+  float2 gt = make_float2((gxy.x - gxy.y) * s2, (gxy.x + gxy.y) * s2);
+  bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j - 1)] > hs;
+  if (!open) return z;
+  FaceOut f = face<MODE>(F, D, c, cb, make_float2(ga.x, gp.x), make_float2(ga.y, gp.y), gt, true,
+                         make_float2(s2, -s2));
+  f.q *= W_DIAG_FLUX;
+  return f;
+}
+
+// ---- Kubelka-Munk (km.wgsl) ----
+__device__ __forceinline__ void km_layer(float k, float s, float t, float& r, float& tr) {  // km.wgsl:1-11
+  if (k + s < 1e-6f || t <= 0.f) { r = 0.f; tr = 1.f; return; }
+  float bs = sqrtf(fmaxf(k * (k + 2.0f * s), 0.f));
+  float arg = fminf(bs * t, 20.0f);
+  float e = expf(arg);
+  float sh = 0.5f * (e - 1.0f / e);
+  float ch = 0.5f * (e + 1.0f / e);
+  float den = (k + s) * sh + bs * ch;
+  if (den < 1e-12f) { r = 0.f; tr = 1.f; return; }
+  r = s * sh / den;
+  tr = bs / den;
+}
+__device__ __forceinline__ float composite(float r, float t, float rb) {  // km.wgsl:13-15
+  return r + t * t * rb / fmaxf(1.0f - r * rb, 1e-4f);
+}
+
+}  // namespace cfk

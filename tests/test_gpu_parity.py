@@ -1,0 +1,307 @@
+"""CUDA kernels against the oracle (GPU).
+
+Per-dispatch parity: the oracle runs a few frames to reach a state with
+fronts, multi-strata stacks and sleeping tiles; that whole internal state
+(rounded to f32, the storage precision) is copied into the CUDA film, one
+dispatch runs on both sides, and every plane it writes is compared.
+
+Frame parity: the CUDA film replays the golden fixtures (inputs, schedule,
+params) and is compared with the reference's FP64 outputs through the
+branch-robust metrics of tests/parity.py.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import parity
+import pyoracle as po
+from canvaz_film import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted((Path(__file__).resolve().parent / "golden").glob("*.npz"))
+
+# oracle plane -> (CUDA plane(s), per-cell count)
+TRANSFER = ["h", "m", "strata_h", "strata_cure", "strata_pig", "sub_refl", "lay", "pres", "flux", "acc", "alpha",
+            "tmp", "acc_s", "alpha_s", "strata_h2", "strata_cure2", "strata_pig2", "h_frame", "fnorm", "delta"]
+WRITES = {
+    "mark_tiles": ["tile_flags", "tile_moved"],
+    "compact_tiles": ["tile_flags"],
+    "cure_step": ["strata_cure", "rheo", "h", "m", "sub_refl", "strata_h", "strata_pig"],
+    "clear_acc": ["acc", "h_frame"],
+    "laplacian": ["pres"],
+    "plug": ["tmp"],
+    "fluxes": ["flux"],
+    "limiter": ["alpha"],
+    "apply": ["h", "acc", "rheo", "strata_h", "strata_pig", "strata_cure", "tile_moved"],
+    "nose": ["delta", "fnorm"],
+    "strata_split": ["acc_s"],
+    "strata_limit": ["alpha_s"],
+    "strata_update": ["strata_h2", "strata_cure2", "strata_pig2"],
+    "strata_copy_back": ["strata_h", "strata_cure", "strata_pig"],
+    "strata_fill": ["strata_h", "strata_cure", "strata_pig"],
+    "shade_full": ["color"],
+}
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as g
+    g.build()
+    from canvaz_film.film import Film  # noqa: F401
+    return True
+
+
+def make_case(name):
+    if name == "drip":
+        cv = synth.drip_canvas(96, 80, 5, n_lines=8, per_cell_n=True)
+        sched = (2e-4, 1, 4)
+    elif name == "blob":
+        cv = synth.blob_canvas(80, 64, 13, n_blobs=6, sigma=(3, 9), per_cell_n=True, tau=(0, 0.5), mu=(0.05, 0.3),
+                               peak_mm=(1.0, 3.0))
+        cv.settings.update(rho=1000.0)
+        sched = (1 / 60, 16, 2)
+    else:  # mixed stacks, relief, thinner, line pressure
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("mg", Path(__file__).parent / "golden" / "make_golden.py")
+        mg = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mg)
+        cv = mg.mixed_canvas(21)
+        sched = (1 / 60, 8, 2)
+    return cv, sched
+
+
+def oracle_state(cv, sched):
+    st = po.make_settings(cv.settings)
+    o = po.Oracle(cv.w, cv.h, st, 0, 64)
+    o.set_tables(cv.pigtab, cv.cmf)
+    o.write_state(cv.planes)
+    fdt, n, frames = sched
+    for _ in range(frames):
+        o.update_params(fdt, n)
+        o.encode_frame(n)
+    o.run("mark_tiles")
+    o.run("compact_tiles")
+    return o
+
+
+def transfer(o, f):
+    """Round the oracle's state to f32 and copy it into the CUDA film."""
+    for k in TRANSFER:
+        v = o.buf(k)
+        if k not in ("delta", "lay"):
+            v = v.astype(np.float32).astype(np.float64)
+            o.set_buf(k, v)
+        f.set_plane(k, v)
+    r = o.buf("rheo").astype(np.float32).astype(np.float64)
+    o.set_buf("rheo", r)
+    r = r.reshape(-1, 3)
+    f.set_plane("mu", r[:, 0])
+    f.set_plane("tau", r[:, 1])
+    f.set_plane("nn", r[:, 2])
+    f.set_plane("tile_flags", _u32(o, "tile_flags"))
+    f.set_plane("tile_moved", _u32(o, "tile_moved"))
+    f.set_params(o.params())
+
+
+def _u32(o, name):
+    return o.buf(name).astype(np.uint32)
+
+
+def cuda_plane(f, name):
+    if name == "rheo":
+        return np.stack([f.plane("mu"), f.plane("tau"), f.plane("nn")], 1).reshape(-1)
+    return f.plane(name)
+
+
+def compare(name, got, want, rtol=1e-4, frac=2e-3):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    assert got.shape == want.shape, (name, got.shape, want.shape)
+    if name in ("delta", "tile_flags", "tile_moved"):
+        bad = got.astype(np.uint64) != want.astype(np.uint64)
+        assert bad.mean() <= frac, (name, int(bad.sum()))
+        return
+    scale = max(float(np.abs(want).max()), 1e-30)
+    err = np.abs(got - want) / scale
+    bad = err > rtol
+    assert bad.mean() <= frac, (name, int(bad.sum()), got.size, float(err.max()))
+
+
+@pytest.mark.parametrize("case", ["drip", "blob", "mixed"])
+@pytest.mark.parametrize("kernel", list(WRITES))
+def test_dispatch_parity(built, case, kernel):
+    from canvaz_film.film import Film
+    cv, sched = make_case(case)
+    o = oracle_state(cv, sched)
+    f = Film(po.make_settings(cv.settings), cv.w, cv.h, capi.CF_PREC_REFERENCE)
+    f.set_tables(cv.pigtab, cv.cmf)
+    transfer(o, f)
+    if kernel == "shade_full":
+        pass
+    o.run(kernel)
+    f.run(kernel)
+    for plane in WRITES[kernel]:
+        want = o.buf(plane)
+        got = cuda_plane(f, plane)
+        if plane == "color":
+            compare(plane, got, want, rtol=2e-3, frac=1e-3)
+        elif plane in ("strata_pig", "strata_pig2"):
+            compare(plane, got, want, rtol=2e-3, frac=2e-3)
+        else:
+            compare(plane, got, want)
+
+
+def replay_cuda(d, precision=capi.CF_PREC_REFERENCE):
+    from canvaz_film.film import Film
+    w, h = int(d["w"]), int(d["h"])
+    st = po.make_settings(json.loads(str(d["settings"])))
+    f = Film(st, w, h, precision)
+    f.set_tables(d["pigtab"], d["cmf"])
+    f.write_state({k[3:]: d[k] for k in d.files if k.startswith("in_")})
+    for (fdt, n), praw in zip(d["schedule"], d["params"]):
+        f.update_params(float(fdt), int(n))
+        got, want = bytes(f.params()), praw.tobytes()
+        # front.zw and front3.xyz feed only the implicit CG solve and depend on
+        # the stats each side measured; every other field is bit exact.
+        cg = set(range(136, 144)) | set(range(160, 172))
+        assert all(got[b] == want[b] for b in range(176) if b not in cg)
+        f.encode_frame(int(n))
+        f.sync()
+    return f
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[p.stem for p in GOLDEN])
+def test_frames_vs_reference_fixture(built, path):
+    d = np.load(path)
+    f = replay_cuda(d)
+    s = f.read_state()
+    got = {"h": s["h"], "m": s["m"], "strata_h": s["strata_h"], "strata_pig": s["strata_pig"], "color": f.color()}
+    want = {k: d["out_" + k] for k in got}
+    m = parity.metrics(got, want)
+    print(path.stem, m)
+    parity.check(m)
+    tf = f.plane("tile_flags").astype(np.uint64)
+    assert (tf == d["out_tile_flags"].astype(np.uint64)).mean() >= 0.95
+
+
+def test_state_roundtrip(built):
+    from canvaz_film.film import Film
+    cv = synth.blob_canvas(48, 40, 3, n_blobs=4, sigma=(3, 8))
+    for prec, tol in ((capi.CF_PREC_REFERENCE, 1e-3), (capi.CF_PREC_FP32, 0.0), (capi.CF_PREC_BF16, 8e-3)):
+        f = Film(po.make_settings(cv.settings), cv.w, cv.h, prec)
+        f.write_state(cv.planes, pig_format=capi.CF_PIG_F32)
+        s = f.read_state()
+        for k in ("h", "m", "strata_h", "strata_cure", "lay"):
+            assert np.array_equal(np.asarray(s[k]).reshape(-1), np.asarray(cv.planes[k]).reshape(-1)), k
+        p, q = s["strata_pig"].reshape(-1), cv.planes["strata_pig"].reshape(-1)
+        assert np.all(np.abs(p - q) <= tol * np.maximum(np.abs(q), 1e-3)), prec
+
+
+def test_smoke_entry(built):
+    import __graft_entry__ as g
+    g.smoke()
+
+
+@pytest.mark.parametrize("prec", [capi.CF_PREC_FP32, capi.CF_PREC_BF16])
+def test_precision_modes_vs_oracle(built, prec):
+    """FP32 and BF16 storage against the oracle storing pigments the same way."""
+    from canvaz_film.film import Film
+    cv = synth.drip_canvas(80, 80, 11, n_lines=6, per_cell_n=True)
+    st = po.make_settings(cv.settings)
+    pig_mode = {capi.CF_PREC_FP32: capi.CF_PIG_F32, capi.CF_PREC_BF16: capi.CF_PIG_BF16}[prec]
+    o = po.Oracle(cv.w, cv.h, st, pig_mode, 64)
+    o.set_tables(cv.pigtab, cv.cmf)
+    o.write_state(cv.planes)
+    f = Film(st, cv.w, cv.h, prec)
+    f.set_tables(cv.pigtab, cv.cmf)
+    f.write_state(cv.planes, pig_format=capi.CF_PIG_F32)
+    for _ in range(4):
+        o.update_params(2e-4, 1)
+        f.update_params(2e-4, 1)
+        o.encode_frame(1)
+        f.encode_frame(1)
+    s = f.read_state()
+    got = {"h": s["h"], "m": s["m"], "strata_h": s["strata_h"], "strata_pig": s["strata_pig"], "color": f.color()}
+    want = {k: o.buf(k) for k in got}
+    m = parity.metrics(got, want)
+    print(prec, m)
+    if prec == capi.CF_PREC_BF16:
+        # rheology is stored in bf16 on the GPU only: bound the height loosely
+        assert m["h_rel_l2"] < 5e-3, m
+    else:
+        parity.check(m)
+
+
+def test_adaptive_step_matches_oracle(built):
+    """dt derived on the device from the last frame's stats equals the host rule."""
+    from canvaz_film.film import Film
+    cv = synth.drip_canvas(96, 96, 21, n_lines=8, per_cell_n=True)
+    st = po.make_settings(cv.settings)
+    o = po.Oracle(cv.w, cv.h, st, 0, 64)
+    o.set_tables(cv.pigtab, cv.cmf)
+    o.write_state(cv.planes)
+    f = Film(st, cv.w, cv.h, capi.CF_PREC_REFERENCE)
+    f.set_tables(cv.pigtab, cv.cmf)
+    f.write_state(cv.planes)
+    for k in range(6):
+        dto = o.step_adaptive(1.0 / 60.0)
+        f.step_adaptive(1.0 / 60.0)
+        dtf = f.stats()["last_dt"]
+        assert abs(dtf - dto) <= 1e-5 * dto, (k, dtf, dto)
+    s = f.read_state()
+    assert parity.rel_l2(s["h"], o.buf("h")) < 1e-4
+
+
+def test_all_active_mode(built):
+    from canvaz_film.film import Film
+    cv = synth.blob_canvas(64, 64, 2, n_blobs=5, sigma=(3, 10), per_cell_n=True)
+    cv.settings.update(all_active=1)
+    st = po.make_settings(cv.settings)
+    o = po.Oracle(cv.w, cv.h, st, 0, 64)
+    o.set_tables(cv.pigtab, cv.cmf)
+    o.write_state(cv.planes)
+    f = Film(st, cv.w, cv.h, capi.CF_PREC_REFERENCE)
+    f.set_tables(cv.pigtab, cv.cmf)
+    f.write_state(cv.planes)
+    for _ in range(5):
+        o.update_params(1e-3, 1)
+        f.update_params(1e-3, 1)
+        o.encode_frame(1)
+        f.encode_frame(1)
+    assert f.stats()["active_tiles"] == (64 // 16) ** 2
+    s = f.read_state()
+    got = {"h": s["h"], "m": s["m"], "strata_h": s["strata_h"], "strata_pig": s["strata_pig"], "color": f.color()}
+    m = parity.metrics(got, {k: o.buf(k) for k in got})
+    parity.check(m)
+
+
+def test_mass_is_conserved_without_sinks(built):
+    """No cure commit (cure_rate 0) and no drained film: sum(h) is conserved to
+    FP32 rounding over many frames (FP64 accumulation on the device)."""
+    from canvaz_film.film import Film
+    cv = synth.drip_canvas(128, 128, 4, n_lines=10, per_cell_n=True)
+    cv.settings.update(cure_rate=0.0)
+    f = Film(po.make_settings(cv.settings), cv.w, cv.h, capi.CF_PREC_REFERENCE)
+    f.set_tables(cv.pigtab, cv.cmf)
+    f.write_state(cv.planes)
+    m0 = f.stats()["wet_volume"]
+    for _ in range(50):
+        f.update_params(2e-4, 1)
+        f.encode_frame(1)
+    m1 = f.stats()["wet_volume"]
+    assert abs(m1 - m0) / m0 < 1e-5, (m0, m1)
+
+
+def test_errors_are_status_codes(built):
+    from canvaz_film.capi import FilmError
+    from canvaz_film.film import Film
+    with pytest.raises(FilmError):
+        Film(capi.Settings.default(), 0, 10)
+    f = Film(capi.Settings.default(width_m=0.064, height_m=0.064), 64, 64)
+    with pytest.raises(FilmError):
+        f.encode_frame(0)
+    with pytest.raises(FilmError):
+        f.run("no_such_kernel")
