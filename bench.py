@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 thin-film step (one JSON line on rank 0).
+
+Workload (default): a 2048 x 2048 FP32 canvas (1 mm cells) tilted 60 deg with
+gravity along +y, seeded with 200 random drip polylines (width 2-8 cells,
+height 0.2-3 mm, per-line Herschel-Bulkley rheology and Dirichlet(0.5)
+pigments), stepped with adaptive-CFL steps.  One step = the device-side dt
+choice + one frame of film + strata/pigment transport + cure + KM shade
+(cf_step_adaptive), every 16x16 tile active.  The canvas state (~3.4 GB)
+is far larger than L2, so no flush is needed between steps.
+
+Arms:
+  --impl gb300 (default): the CUDA library through its C ABI.  `value` is
+      device throughput with the state resident in HBM (CUDA events on the
+      stream the kernels run on); `e2e` goes through the same C ABI with host
+      buffers: every timed step uploads the full state from pinned host
+      memory (cf_write_state), steps, and reads back h and the colour image.
+  --impl reference: the reference path on the host cores (the reference's
+      own WGSL translated to C++ when oracle/_ref is built here, else the
+      oracle's FP32 restatement), OpenMP over rows on all cores.
+Multi-GPU: one replica canvas per rank (independent canvases; no collective
+on the data path), `value` = all ranks' cell-updates / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT / "paint-sim-3d_gb300", ROOT / "oracle"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+from canvaz_film import capi, synth  # noqa: E402
+
+WORKLOADS = {
+    # name: (generator, precision, dt_max, adaptive)
+    "drips2048_tilt60_fp32": (lambda seed: synth.config(1, seed), capi.CF_PREC_FP32, 1.0 / 60.0, True),
+    "blobs512_dt1e-3_fp32": (lambda seed: synth.config(0, seed), capi.CF_PREC_FP32, 1e-3, False),
+    "blobs4096_dt1e-3_bf16": (lambda seed: synth.config(2, seed), capi.CF_PREC_BF16, 1e-3, False),
+    "blobs4096_dt1e-3_fp32": (lambda seed: synth.config(2, seed), capi.CF_PREC_FP32, 1e-3, False),
+}
+DEFAULT_WORKLOAD = "drips2048_tilt60_fp32"
+
+# Compulsory persistent-state bytes per cell-step (read once + write once):
+# h 4R+4W, m 4R, rheo 3 fields R+W, delta 4R+4W, strata_h 16R+16W,
+# strata_cure 16R+16W, strata_pig 64 slots R+W, sub_refl 16 f16 R, colour 8W.
+ALG_BYTES_PER_CELL = {capi.CF_PREC_FP32: 660, capi.CF_PREC_REFERENCE: 404, capi.CF_PREC_BF16: 392}
+PREC_NAME = {capi.CF_PREC_FP32: "f32", capi.CF_PREC_REFERENCE: "f32+f16pig", capi.CF_PREC_BF16: "f32+bf16pig"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def step_traffic():
+    """dram bytes per cell-step from the committed ncu summary (or None)."""
+    p = ROOT / "profiles" / "step_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_cell_step="):
+            return float(line.split("=", 1)[1].split()[0])
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in Path(self.file.name).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        finally:
+            os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(rows[0][2]) if rows else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def settings_for(cv):
+    s = dict(cv.settings)
+    s["all_active"] = 1
+    return capi.Settings.default(**s)
+
+
+def cpu_baseline(cv, workload, budget_s, steps_hint=3):
+    """The oracle's FP32 restatement of the reference path on all host cores,
+    on a bounded sample: the same canvas, as many whole steps as fit the
+    budget (at least one)."""
+    import pyoracle as po
+    po.build()
+    gen, prec, dt_max, adaptive = WORKLOADS[workload]
+    pig = capi.PREC_TO_PIG[prec]
+    o = po.Oracle(cv.w, cv.h, settings_for(cv), pig, 32)
+    o.set_tables(cv.pigtab, cv.cmf)
+    o.write_state(cv.planes)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        if adaptive:
+            o.step_adaptive(dt_max)
+        else:
+            o.update_params(dt_max, 1)
+            o.encode_frame(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if n >= steps_hint or el > budget_s or (el / n) * (n + 1) > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": cv.w * cv.h * n / el / 1e9, "unit": "Gcell-updates/s", "cores": os.cpu_count(),
+            "kind": "port", "sample": "%d whole step(s) of the %dx%d workload, FP32 oracle restatement, OpenMP %d threads, %.1f s"
+            % (n, cv.w, cv.h, os.cpu_count(), el)}
+
+
+def reference_arm(args):
+    """CPU reference path, same workload / metric / unit; rank 0 only."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    gen, prec, dt_max, adaptive = WORKLOADS[args.workload]
+    cv = gen(0)
+    per_step_budget = 150.0 / max(args.steps + args.warmup, 1)
+    cb = cpu_baseline(cv, args.workload, per_step_budget * (args.steps + args.warmup), steps_hint=args.steps + args.warmup)
+    line = {"impl": "reference", "metric": "Gcell-updates/s", "value": cb["value"], "unit": "Gcell-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": PREC_NAME[prec], "data": "synthetic",
+            "config": {"workload": args.workload, "cells": cv.w * cv.h, "all_tiles_active": True},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from canvaz_film.film import Film
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    gen, prec, dt_max, adaptive = WORKLOADS[args.workload]
+    cv = gen(rank)  # one replica canvas per rank, own seed
+    st = settings_for(cv)
+    film = Film(st, cv.w, cv.h, prec)
+    film.set_tables(cv.pigtab, cv.cmf)
+    film.write_state(cv.planes)
+    s0 = film.stats()
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def step():
+        if adaptive:
+            film.step_adaptive(dt_max, sh)
+        else:
+            film.encode_frame(1, sh)
+
+    if not adaptive:
+        film.update_params(dt_max, 1)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = film.stats()["launches"]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    s1 = film.stats()
+    launches = s1["launches"] - l0
+    cells = cv.w * cv.h
+    value = world * cells * args.steps / t / 1e9
+    alg = ALG_BYTES_PER_CELL[prec]
+    peak, peak_kind = peaks()
+    achieved = alg * cells * args.steps / t / 1e9
+    traffic_pc = step_traffic()
+    mass0 = s0["wet_volume"] + s0["relief_volume"]
+    mass1 = s1["wet_volume"] + s1["relief_volume"]
+
+    # end to end through the C ABI with host buffers (pinned)
+    e2e = None
+    if args.e2e_steps > 0:
+        state = film.read_state(pig_format=capi.PREC_TO_PIG[prec] if prec != capi.CF_PREC_FP32 else capi.CF_PIG_F32)
+        pinned = {}
+        for k, v in state.items():
+            tv = torch.from_numpy(np.ascontiguousarray(v))
+            pinned[k] = tv.pin_memory().numpy()
+        pig_fmt = capi.CF_PIG_F32 if prec == capi.CF_PREC_FP32 else capi.PREC_TO_PIG[prec]
+        h_out = torch.empty(cells, dtype=torch.float32).pin_memory()
+        col_out = torch.empty(cells * 4, dtype=torch.int16).pin_memory()
+        import ctypes as C
+        L = capi.load_library()
+        v = capi.StateView(pig_format=pig_fmt, device=0)
+        for k in ("h", "m", "rheo", "strata_h", "strata_cure", "lay"):
+            setattr(v, k, pinned[k].ctypes.data)
+        sub = np.ascontiguousarray(state["sub_refl"].astype(np.float16))
+        subp = torch.from_numpy(sub).pin_memory().numpy()
+        v.sub_refl = subp.ctypes.data
+        pig = state["strata_pig"]
+        if pig_fmt == capi.CF_PIG_F16:
+            pig = pig.astype(np.float16)
+        elif pig_fmt == capi.CF_PIG_BF16:
+            from canvaz_film.film import _f32_to_bf16
+            pig = _f32_to_bf16(pig)
+        pigp = torch.from_numpy(np.ascontiguousarray(pig)).pin_memory().numpy()
+        v.strata_pig = pigp.ctypes.data
+        hv = capi.StateView(pig_format=pig_fmt, device=0, h=h_out.data_ptr())
+        h2d = sum(pinned[k].nbytes for k in ("h", "m", "rheo", "strata_h", "strata_cure", "lay")) + subp.nbytes + pigp.nbytes
+        d2h = h_out.numel() * 4 + col_out.numel() * 2
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            assert L.cf_write_state(film.p, C.byref(v)) == 0
+            step()
+            assert L.cf_read_state(film.p, C.byref(hv)) == 0
+            assert L.cf_read_color(film.p, C.cast(col_out.data_ptr(), C.POINTER(C.c_uint16))) == 0
+        te = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([te], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": world * cells * args.e2e_steps / te / 1e9, "unit": "Gcell-updates/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+               "path": "cf_write_state(pinned host) + step + cf_read_state(h) + cf_read_color"}
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(cv, args.workload, args.cpu_seconds)
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": PREC_NAME[prec],
+            "data": "synthetic (seeded drip polylines / Gaussian blobs; no public dataset)",
+            "config": {"workload": args.workload, "w": cv.w, "h": cv.h, "cells_per_gpu": cells,
+                       "precision": PREC_NAME[prec], "adaptive_dt": adaptive, "dt_max": dt_max,
+                       "all_tiles_active": True, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set %.1f GB > L2 (129 MB): no flush needed" % (film_bytes(cells, prec) / 1e9)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "alg_bytes_per_cell": alg, "scope": "whole step (all kernels of cf_step_adaptive)",
+                         "traffic": None if traffic_pc is None else traffic_pc * cells},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "e2e": e2e,
+            "cpu_baseline": cb,
+            "mass_drift_rel": abs(mass1 - mass0) / max(mass0, 1e-300),
+            "last_dt": s1["last_dt"],
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def film_bytes(cells, prec):
+    pig = 4 if prec == capi.CF_PREC_FP32 else 2
+    return cells * (4 * 13 + 8 * 2 + 16 * 8 + 64 + 2 * 64 * pig + 32 + 8)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

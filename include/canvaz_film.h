@@ -153,6 +153,7 @@ typedef struct cf_stats {
     double last_dt;        /* substep dt of the last frame                    */
     uint64_t nan_cells;    /* non-finite h                                    */
     uint64_t wet_cells;
+    uint64_t launches;     /* kernels this film has enqueued since create     */
 } cf_stats;
 
 typedef struct cf_film cf_film;

@@ -99,6 +99,7 @@ class Stats(C.Structure):
         ("h_max", C.c_float), ("mu_min", C.c_float), ("active_tiles", C.c_uint32),
         ("frames", C.c_uint32), ("wet_volume", C.c_double), ("relief_volume", C.c_double),
         ("last_dt", C.c_double), ("nan_cells", C.c_uint64), ("wet_cells", C.c_uint64),
+        ("launches", C.c_uint64),
     ]
 
 

@@ -38,6 +38,7 @@ struct cf_film {
   bool params_dirty = true;
   float h_max_stat = 0.f, mu_min_stat = 1.f, h_max_pending = 0.f;
   uint32_t frames = 0;
+  uint64_t launches = 0;  // kernels enqueued by this film
   int device = 0, sms = 0;
   std::string err;
 };
@@ -231,10 +232,10 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
   add((void**)&F.flux, 16 * n); add((void**)&F.acc, 16 * n); add((void**)&F.acc_s, 64 * n);
   add((void**)&F.alpha_s, 16 * n); add((void**)&F.alpha, 4 * n); add((void**)&F.tmp, 4 * n);
   add((void**)&F.h_frame, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
-  add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add(&F.pig, 64 * pig_b * n);
-  add(&F.pig2, 64 * pig_b * n); add((void**)&F.refl, 32 * n); add((void**)&F.color, 8 * n);
+  add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
+  add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n); add((void**)&F.color, 8 * n);
   add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt); add((void**)&F.stats64, 8 * n64);
-  add((void**)&F.fill_src, 4 * n);
+  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, n);
   size_t total = 0;
   for (auto& sl : slots) total += (sl.bytes + 255) & ~(size_t)255;
   cudaError_t e = cudaMalloc(&f->arena, total);
@@ -258,7 +259,7 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
     cudaGetLastError();
     return bail(CF_ERR_OUT_OF_MEMORY);
   }
-  F.w = w; F.h = h; F.tw = f->tw; F.th = f->th;
+  F.w = w; F.h = h; F.tw = f->tw; F.th = f->th; F.n = (uint32_t)n;
   F.P = f->d_params; F.stats = f->d_stats;
   F.pigtab = f->d_tables; F.cmf = f->d_tables + 480;
   // Film::new: zeroed buffers, substrate refl, weave relief, rheo = (1, 0)
@@ -374,7 +375,7 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
     CUDA_TRY(f, cudaMalloc(&tmp, need));
     if (v->strata_pig) {
       cudaError_t e = cudaMemcpy(tmp, v->strata_pig, 64 * esz * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) cfk::launch_pig_import(F, f->prec, tmp, v->pig_format, 64 * n, 0);
+      if (e == cudaSuccess) cfk::launch_pig_import(F, f->prec, F.pig, tmp, v->pig_format, 0);
       if (e == cudaSuccess) e = cudaDeviceSynchronize();
       if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
     }
@@ -399,6 +400,8 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   CUDA_TRY(f, cudaMemset(F.pig2, 0, 64 * pig_b * n));
   CUDA_TRY(f, cudaMemset(F.alpha_s, 0, 16 * n));
   cfk::launch_fill_u32(F.tile_moved, 1u, (size_t)f->tw * f->th, 0);
+  // aggregates of the uploaded strata for the first cure, and its colour
+  cfk::launch_compose(F, f->prec, 1, 0);
   // current stats so that the first adaptive step sees this state
   cfk::launch_reduce(F, f->prec, 0);
   CUDA_TRY(f, cudaGetLastError());
@@ -433,7 +436,7 @@ cf_status cf_read_state(cf_film* f, const cf_state_view* v) {
     CUDA_TRY(f, cudaMalloc(&tmp, need));
     cudaError_t e = cudaSuccess;
     if (v->strata_pig) {
-      cfk::launch_pig_export(F, f->prec, tmp, v->pig_format, 64 * n, 0);
+      cfk::launch_pig_export(F, f->prec, F.pig, tmp, v->pig_format, 0);
       e = cudaDeviceSynchronize();
       if (e == cudaSuccess) e = cudaMemcpy(v->strata_pig, tmp, 64 * esz * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
     }
@@ -498,7 +501,7 @@ cf_status cf_encode_frame(cf_film* f, uint32_t substeps, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
-  cfk::launch_frame(f->F, f->prec, substeps, f->S.all_active, st);
+  f->launches += cfk::launch_frame(f->F, f->prec, substeps, f->S.all_active, st);
   if ((s = check_launch(f)) != CF_OK) return s;
   f->frames++;
   return CF_OK;
@@ -512,7 +515,7 @@ cf_status cf_step_adaptive(cf_film* f, float dt_max, void* stream) {
   cf_status s = upload_params(f, st, dt_max);
   if (s != CF_OK) return s;
   cfk::launch_adaptive_params(f->d_params, f->d_stats, st);
-  cfk::launch_frame(f->F, f->prec, 1, f->S.all_active, st);
+  f->launches += 1 + cfk::launch_frame(f->F, f->prec, 1, f->S.all_active, st);
   if ((s = check_launch(f)) != CF_OK) return s;
   f->frames++;
   return CF_OK;
@@ -570,6 +573,7 @@ cf_status cf_get_stats(cf_film* f, cf_stats* out) {
   out->last_dt = ds.last_dt > 0.f ? (double)ds.last_dt : (double)f->P.dt;
   out->nan_cells = ds.nan_cells;
   out->wet_cells = ds.wet_cells;
+  out->launches = f->launches;
   return CF_OK;
 }
 
@@ -591,6 +595,9 @@ cf_status cf_sync(cf_film* f) {
 #include "../../include/canvaz_film_debug.h"
 
 namespace {
+int internal_pig_format(const cf_film* f) {
+  return f->prec == CF_PREC_FP32 ? CF_PIG_F32 : (f->prec == CF_PREC_BF16 ? CF_PIG_BF16 : CF_PIG_F16);
+}
 struct PlaneRef {
   void* ptr;
   size_t bytes;
@@ -616,6 +623,7 @@ bool find_plane(cf_film* f, const std::string& n, PlaneRef& r) {
       {"strata_pig2", F.pig2, 64 * pb * N, pe}, {"sub_refl", F.refl, 32 * N, CF_ELEM_F16},
       {"color", F.color, 8 * N, CF_ELEM_F16}, {"tile_flags", F.tile_flags, 4 * nt, CF_ELEM_U32},
       {"tile_moved", F.tile_moved, 4 * nt, CF_ELEM_U32}, {"fill_src", F.fill_src, 4 * N, CF_ELEM_I32},
+      {"agg", F.agg, 16 * N, CF_ELEM_F32},
   };
   for (auto& e : tab)
     if (n == e.name) { r = {e.p, e.b, e.e}; return true; }
@@ -639,6 +647,25 @@ cf_status cf_debug_read(cf_film* f, const char* name, void* host, size_t bytes) 
   PlaneRef r;
   if (!find_plane(f, name, r) || r.bytes != bytes) return fail(f, CF_ERR_INVALID_ARG, "plane name or size");
   CUDA_TRY(f, cudaDeviceSynchronize());
+  std::string n(name);
+  if (n == "strata_pig" || n == "strata_pig2") {  // chunk planes -> [cell][stratum][slot]
+    void* tmp = nullptr;
+    CUDA_TRY(f, cudaMalloc(&tmp, bytes));
+    cfk::launch_pig_export(f->F, f->prec, (const uint4*)r.ptr, tmp, internal_pig_format(f), 0);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(host, tmp, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(tmp);
+    if (e != cudaSuccess) { f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
+    return CF_OK;
+  }
+  if (n == "acc_s") {  // face-major -> [cell][face]
+    std::vector<float4> v(4 * (size_t)f->n);
+    CUDA_TRY(f, cudaMemcpy(v.data(), r.ptr, bytes, cudaMemcpyDeviceToHost));
+    float4* o = (float4*)host;
+    for (size_t c = 0; c < f->n; ++c)
+      for (int k = 0; k < 4; ++k) o[4 * c + k] = v[(size_t)k * f->n + c];
+    return CF_OK;
+  }
   CUDA_TRY(f, cudaMemcpy(host, r.ptr, bytes, cudaMemcpyDeviceToHost));
   return CF_OK;
 }
@@ -648,6 +675,27 @@ cf_status cf_debug_write(cf_film* f, const char* name, const void* host, size_t 
   PlaneRef r;
   if (!find_plane(f, name, r) || r.bytes != bytes) return fail(f, CF_ERR_INVALID_ARG, "plane name or size");
   CUDA_TRY(f, cudaDeviceSynchronize());
+  std::string n(name);
+  if (n == "strata_pig" || n == "strata_pig2") {
+    void* tmp = nullptr;
+    CUDA_TRY(f, cudaMalloc(&tmp, bytes));
+    cudaError_t e = cudaMemcpy(tmp, host, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      cfk::launch_pig_import(f->F, f->prec, (uint4*)r.ptr, tmp, internal_pig_format(f), 0);
+      e = cudaDeviceSynchronize();
+    }
+    cudaFree(tmp);
+    if (e != cudaSuccess) { f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
+    return CF_OK;
+  }
+  if (n == "acc_s") {
+    std::vector<float4> v(4 * (size_t)f->n);
+    const float4* in = (const float4*)host;
+    for (size_t c = 0; c < f->n; ++c)
+      for (int k = 0; k < 4; ++k) v[(size_t)k * f->n + c] = in[4 * c + k];
+    CUDA_TRY(f, cudaMemcpy(r.ptr, v.data(), bytes, cudaMemcpyHostToDevice));
+    return CF_OK;
+  }
   CUDA_TRY(f, cudaMemcpy(r.ptr, host, bytes, cudaMemcpyHostToDevice));
   return CF_OK;
 }

@@ -44,7 +44,7 @@ struct DevStats {
   uint32_t h_max_bits;   // max h over cells with h > 4 h_min (float bits, h >= 0)
   uint32_t mu_min_bits;  // min mu over the same cells (float bits, mu > 0)
   uint32_t active_tiles;
-  uint32_t nan_flag;
+  uint32_t fill_needed;  // wet cells left without strata by the strata pass (fill is skipped at 0)
   double wet_sum;        // sum(h)
   double relief_sum;     // sum(m)
   unsigned long long wet_cells;
@@ -66,10 +66,15 @@ template <> __device__ __forceinline__ float from_f<float>(float v) { return v; 
 template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
-// All device planes of one film (reference layout; pig / rheo element types
-// depend on the precision mode and are reinterpreted by the kernels).
+// All device planes of one film.  The strata come in two generations (cur /
+// nxt) that swap every frame, so the strata pass never copies back.  Pigment
+// slots are stored chunk-major: 16-byte chunk q of stratum k of cell c lives at
+// chunk index (k * QN + q) * n + c (QN = chunks per stratum), so a warp reads
+// 512 contiguous bytes per load.  acc_s is face-major: face f of cell c at
+// f * n + c.
 struct Film {
   uint32_t w, h, tw, th;  // grid and 16x16 tile counts
+  uint32_t n;             // cells
   const DevParams* P;
   DevStats* stats;
   float* hh;       // h
@@ -84,30 +89,27 @@ struct Film {
   float2* fnorm;
   float4* flux;
   float4* acc;
-  float4* acc_s;   // 4 per cell
+  float4* acc_s;   // 4 faces x n, face-major
   float4* alpha_s;
   float* alpha;
   float* tmp;
   float* h_frame;
-  float4* sh;      // strata_h
+  float4* sh;      // strata_h, current generation
   float4* scu;     // strata_cure
-  float4* sh2;
+  uint4* pig;      // pigment chunks
+  float4* sh2;     // next generation
   float4* scu2;
-  void* pig;       // 64 Pig per cell
-  void* pig2;
+  uint4* pig2;
+  float4* agg;     // composition aggregates for the next cure (see composition_parts)
   uint16_t* refl;  // 16 half per cell
   ushort4* color;  // rgba16f
   uint32_t* tile_flags;
   uint32_t* tile_moved;
   float2* stats64; // per 64x64 tile (h_max, mu_min)
   int32_t* fill_src;
+  uint8_t* fflags;  // bit f: strata_split wrote a nonzero acc_s face f this frame
   const float* pigtab;  // 12 x 40
   const float* cmf;     // 16 x 3
-};
-
-struct Cell {
-  int i, j;
-  uint32_t c;
 };
 
 __device__ __forceinline__ uint32_t idx(const Film& F, int i, int j) { return (uint32_t)j * F.w + (uint32_t)i; }
@@ -129,6 +131,7 @@ __device__ __forceinline__ int refl_j(const Film& F, int j) {
   if (r >= hh) r = 2 * hh - r - 1;
   return min(max(r, 0), hh - 1);
 }
+__device__ __forceinline__ float4 acc_face(const Film& F, uint32_t c, int f) { return F.acc_s[(size_t)f * F.n + c]; }
 
 template <int MODE>
 __device__ __forceinline__ float rmu(const Film& F, uint32_t c) {
@@ -150,99 +153,71 @@ __device__ __forceinline__ void set_rheo(const Film& F, uint32_t c, float mu, fl
   ((Rh*)F.nn)[c] = from_f<Rh>(n);
 }
 
-// IEEE half bits <-> float without type punning.
+// IEEE half / bfloat16 bits <-> float without type punning.
 __device__ __forceinline__ float h16_to_f(uint32_t bits) { return __half2float(__ushort_as_half((unsigned short)bits)); }
 __device__ __forceinline__ uint32_t f_to_h16(float v) { return (uint32_t)__half_as_ushort(__float2half_rn(v)); }
+__device__ __forceinline__ float b16_to_f(uint32_t bits) { return __uint_as_float(bits << 16); }
+__device__ __forceinline__ uint32_t f_to_b16(float v) { return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v)); }
 
-// ---- pigment slots: 16 per stratum, 4 strata per cell ----
-template <class T>
-__device__ __forceinline__ void load_pig16(const T* base, float o[16]) {
-#pragma unroll
-  for (int q = 0; q < 16; ++q) o[q] = to_f(base[q]);
-}
-template <>
-__device__ __forceinline__ void load_pig16<__half>(const __half* base, float o[16]) {
-  const uint4* p = reinterpret_cast<const uint4*>(base);
-  uint4 a = p[0], b = p[1];
-  uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    o[2 * k] = h16_to_f(wv[k] & 0xffffu);
-    o[2 * k + 1] = h16_to_f(wv[k] >> 16);
-  }
-}
-template <>
-__device__ __forceinline__ void load_pig16<__nv_bfloat16>(const __nv_bfloat16* base, float o[16]) {
-  const uint4* p = reinterpret_cast<const uint4*>(base);
-  uint4 a = p[0], b = p[1];
-  uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    o[2 * k] = __uint_as_float(wv[k] << 16);
-    o[2 * k + 1] = __uint_as_float(wv[k] & 0xffff0000u);
-  }
-}
-template <>
-__device__ __forceinline__ void load_pig16<float>(const float* base, float o[16]) {
-  const float4* p = reinterpret_cast<const float4*>(base);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    float4 v = p[k];
-    o[4 * k] = v.x; o[4 * k + 1] = v.y; o[4 * k + 2] = v.z; o[4 * k + 3] = v.w;
-  }
-}
-template <class T>
-__device__ __forceinline__ void store_pig16(T* base, const float v[16]) {
-#pragma unroll
-  for (int q = 0; q < 16; ++q) base[q] = from_f<T>(v[q]);
-}
-template <>
-__device__ __forceinline__ void store_pig16<float>(float* base, const float v[16]) {
-  float4* p = reinterpret_cast<float4*>(base);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) p[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-}
-template <>
-__device__ __forceinline__ void store_pig16<__half>(__half* base, const float v[16]) {
-  uint32_t wv[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) wv[k] = f_to_h16(v[2 * k]) | (f_to_h16(v[2 * k + 1]) << 16);
-  uint4* p = reinterpret_cast<uint4*>(base);
-  p[0] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-  p[1] = make_uint4(wv[4], wv[5], wv[6], wv[7]);
-}
-template <>
-__device__ __forceinline__ void store_pig16<__nv_bfloat16>(__nv_bfloat16* base, const float v[16]) {
-  uint32_t wv[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    wv[k] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * k])) |
-            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * k + 1])) << 16);
-  }
-  uint4* p = reinterpret_cast<uint4*>(base);
-  p[0] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-  p[1] = make_uint4(wv[4], wv[5], wv[6], wv[7]);
-}
-// Raw copy of one stratum's 16 slots (bit exact).
-template <class T>
-__device__ __forceinline__ void copy_pig16(T* dst, const T* src) {
-  constexpr int W = 16 * sizeof(T) / 16;
-  const uint4* s = reinterpret_cast<const uint4*>(src);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-  for (int k = 0; k < W; ++k) d[k] = s[k];
-}
-template <class T>
-__device__ __forceinline__ void zero_pig16(T* dst) {
-  constexpr int W = 16 * sizeof(T) / 16;
-  uint4* d = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-  for (int k = 0; k < W; ++k) d[k] = make_uint4(0, 0, 0, 0);
-}
+// ---- pigment slots: 16 per stratum, 4 strata per cell, chunk-major ----
 template <int MODE>
-__device__ __forceinline__ typename Prec<MODE>::Pig* pig_at(void* base, uint32_t c, int k) {
-  return reinterpret_cast<typename Prec<MODE>::Pig*>(base) + (size_t)c * 64 + 16 * k;
-}
+struct PigIO {
+  using Pig = typename Prec<MODE>::Pig;
+  static constexpr int QN = 16 * (int)sizeof(Pig) / 16;  // 16-byte chunks per stratum
+  __device__ static __forceinline__ size_t at(const Film& F, uint32_t c, int k, int q) {
+    return (size_t)(k * QN + q) * F.n + c;
+  }
+  // 16 slot values of stratum k of cell c from `base` (cur or nxt generation)
+  __device__ static __forceinline__ void load(const Film& F, const uint4* base, uint32_t c, int k, float o[16]) {
+#pragma unroll
+    for (int q = 0; q < QN; ++q) {
+      uint4 v = base[at(F, c, k, q)];
+      uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+      if constexpr (MODE == CF_PREC_FP32) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) o[4 * q + e] = __uint_as_float(wv[e]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if constexpr (MODE == CF_PREC_REFERENCE) {
+            o[8 * q + 2 * e] = h16_to_f(wv[e] & 0xffffu);
+            o[8 * q + 2 * e + 1] = h16_to_f(wv[e] >> 16);
+          } else {
+            o[8 * q + 2 * e] = b16_to_f(wv[e] & 0xffffu);
+            o[8 * q + 2 * e + 1] = b16_to_f(wv[e] >> 16);
+          }
+        }
+      }
+    }
+  }
+  __device__ static __forceinline__ void store(const Film& F, uint4* base, uint32_t c, int k, const float v[16]) {
+#pragma unroll
+    for (int q = 0; q < QN; ++q) {
+      uint32_t wv[4];
+      if constexpr (MODE == CF_PREC_FP32) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) wv[e] = __float_as_uint(v[4 * q + e]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if constexpr (MODE == CF_PREC_REFERENCE) wv[e] = f_to_h16(v[8 * q + 2 * e]) | (f_to_h16(v[8 * q + 2 * e + 1]) << 16);
+          else wv[e] = f_to_b16(v[8 * q + 2 * e]) | (f_to_b16(v[8 * q + 2 * e + 1]) << 16);
+        }
+      }
+      base[at(F, c, k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+    }
+  }
+  // bit-exact copy of stratum ks of cell cs (in src) to stratum kd of cell cd (in dst)
+  __device__ static __forceinline__ void copy(const Film& F, uint4* dst, uint32_t cd, int kd, const uint4* src,
+                                              uint32_t cs, int ks) {
+#pragma unroll
+    for (int q = 0; q < QN; ++q) dst[at(F, cd, kd, q)] = src[at(F, cs, ks, q)];
+  }
+  __device__ static __forceinline__ void zero(const Film& F, uint4* dst, uint32_t c, int k) {
+#pragma unroll
+    for (int q = 0; q < QN; ++q) dst[at(F, c, k, q)] = make_uint4(0u, 0u, 0u, 0u);
+  }
+};
 
 __device__ __forceinline__ float half_at(const uint16_t* p, int k) {
   return __half2float(__ushort_as_half(p[k]));
@@ -585,6 +560,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
   if (k == 0) {
     if (!(i + 1 < (int)F.w && cell_active(F, i + 1, j))) return z;
     uint32_t cb = idx(F, i + 1, j);
+    if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;  // face() is zero on a dry pair
     float2 p10 = pres_at(F, i + 1, j);
     float2 gm = make_float2(-(p10.x - p00.x) * P.inv_dx, -(p10.y - p00.y) * P.inv_dx);
     float2 a = pres_wet(F, i, j + 1, p00), b = pres_wet(F, i + 1, j + 1, p10);
@@ -599,6 +575,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
   if (k == 1) {
     if (!(j + 1 < (int)F.h && cell_active(F, i, j + 1))) return z;
     uint32_t cb = idx(F, i, j + 1);
+    if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;
     float2 p01 = pres_at(F, i, j + 1);
     float2 gm = make_float2(-(p01.x - p00.x) * P.inv_dx, -(p01.y - p00.y) * P.inv_dx);
     float2 a = pres_wet(F, i + 1, j, p00), b = pres_wet(F, i + 1, j + 1, p01);
@@ -614,6 +591,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
   if (k == 2) {
     if (!(i + 1 < (int)F.w && j + 1 < (int)F.h && cell_active(F, i + 1, j + 1))) return z;
     uint32_t cb = idx(F, i + 1, j + 1);
+    if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;
     float2 p11 = pres_at(F, i + 1, j + 1);
     float2 ga = make_float2(-(p11.x - p00.x) * P.inv_dx * s2, -(p11.y - p00.y) * P.inv_dx * s2);
     float2 pa = pres_wet(F, i + 1, j, p00), pb = pres_wet(F, i, j + 1, p11);
@@ -628,6 +606,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
   }
   if (!(i + 1 < (int)F.w && j > 0 && cell_active(F, i + 1, j - 1))) return z;
   uint32_t cb = idx(F, i + 1, j - 1);
+  if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;  // face() is zero on a dry pair
   float2 p1m = pres_at(F, i + 1, j - 1);
   float2 ga = make_float2(-(p1m.x - p00.x) * P.inv_dx * s2, -(p1m.y - p00.y) * P.inv_dx * s2);
   float2 pa = pres_wet(F, i + 1, j, p00), pb = pres_wet(F, i, j - 1, p1m);

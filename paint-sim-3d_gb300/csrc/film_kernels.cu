@@ -1,12 +1,23 @@
-// film_kernels.cu — sm_103a kernels of the thin-film step, one per dispatch of
-// Film::encode_frame (src/film/mod.rs:1322-1462), plus stats and state I/O.
+// film_kernels.cu — sm_103a kernels of the thin-film step and their host
+// launchers.  The frame follows Film::encode_frame (src/film/mod.rs:1322-1462):
+//
+//   mark_tiles, compact_tiles          16x16 tile activity (film.wgsl:1365-1425)
+//   cure                               cure.wgsl:119-159, from per-frame aggregates
+//   [clear_acc + laplacian], plug, fluxes, limiter, apply, nose   per substep
+//   laplacian, strata_split, reduce_tiles
+//   strata pass: strata_limit + strata_update + shade_full + the next frame's
+//                rheology aggregates, in one kernel, into the other strata
+//                generation (no copy back)
+//   strata_fill x 6                    skipped on the device when no wet cell
+//                                      was left without strata
 //
 // Launch geometry: one 16x16 block per 16x16 activity tile.  A tile-list
-// dispatch of the reference (dispatch_workgroups_indirect over the active
-// tiles) becomes a full-grid launch whose blocks on inactive tiles return at
-// once, so the active set stays on the device and the frame has no host
+// dispatch of the reference becomes a full-grid launch whose blocks on
+// inactive tiles return at once (or, for the strata pass, carry their strata
+// over), so the active set stays on the device and the frame needs no host
 // round trip.  Dispatches whose invocations read what the same dispatch
-// writes in the reference (nose, strata_fill) read a snapshot here.
+// writes in the reference (nose, strata_fill) read a snapshot or run in two
+// passes (Jacobi semantics).
 #include <cuda_runtime.h>
 
 #include <string_view>
@@ -27,25 +38,33 @@ namespace cfk {
   const cf_params& P = D.p;                                        \
   (void)P;
 
+__device__ __forceinline__ float sel4(float4 v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ float4 neg4(float4 v) { return make_float4(-v.x, -v.y, -v.z, -v.w); }
+__device__ __forceinline__ bool nb_ok(const Film& F, int i, int j) { return in_grid(F, i, j) && cell_active(F, i, j); }
+
 // film.wgsl:1365-1391
 __global__ void __launch_bounds__(256) k_mark_tiles(Film F) {
   __shared__ uint32_t any;
   if (threadIdx.x == 0 && threadIdx.y == 0) any = 0u;
   __syncthreads();
   const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+  uint32_t bits = 0u;
   if (i < (int)F.w && j < (int)F.h) {
     uint32_t c = idx(F, i, j);
     float hv = F.hh[c];
     if (hv > 0.f) {
-      uint32_t bits = 1u;
+      bits = 1u;
       if (threadIdx.x < 8) bits |= 2u;
       if (threadIdx.x >= 8) bits |= 4u;
       if (threadIdx.y < 8) bits |= 8u;
       if (threadIdx.y >= 8) bits |= 16u;
       if (fabsf(hv - F.h_frame[c]) > FRAME_EPS) bits |= MOVED;
-      atomicOr(&any, bits);
     }
   }
+  bits = __reduce_or_sync(0xffffffffu, bits);
+  if ((threadIdx.x & 31) == 0 && bits) atomicOr(&any, bits);
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     uint32_t t = blockIdx.x + blockIdx.y * F.tw;
@@ -87,7 +106,14 @@ __global__ void __launch_bounds__(256) k_compact_tiles(Film F, int all_active) {
   }
 }
 
-// cure.wgsl:119-159 (full grid)
+__device__ __forceinline__ void lnmu_table(const float* pigtab, float out[12]) {
+#pragma unroll
+  for (int q = 0; q < 12; ++q) out[q] = logf(fmaxf(pigtab[q * 40 + 32], 1e-3f));
+}
+
+// cure.wgsl:119-159 (full grid).  The pigment part of the composition comes
+// from agg (written by the last strata pass); the stack is only read when
+// the bottom stratum commits.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_cure(Film F) {
   const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
@@ -101,17 +127,17 @@ __global__ void __launch_bounds__(256) k_cure(Film F) {
   float t[4] = {t4.x, t4.y, t4.z, t4.w}, u[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
   for (int k = 0; k < 4; ++k) u[k] = t[k] > 0.f ? fminf(u[k] + rate, 1.f) : u[k];
-  Stack s;
-  stack_load<MODE>(F, F.pig, c, s);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) s.cu[k] = u[k];
   if (!(t[0] > 0.f && u[0] >= 1.f)) {
     F.scu[c] = make_float4(u[0], u[1], u[2], u[3]);
     float mu, ty, n;
-    composition_rheo(P, F.pigtab, s, mu, ty, n);
+    rheo_from_parts(P, F.agg[c], t, u, mu, ty, n);
     set_rheo<MODE>(F, c, mu, ty, n);
     return;
   }
+  Stack s;
+  stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) s.cu[k] = u[k];
   float committed = 0.f;
   uint32_t guard = 0;
   uint16_t* rf = F.refl + (size_t)c * 16;
@@ -133,10 +159,16 @@ __global__ void __launch_bounds__(256) k_cure(Film F) {
     stack_compact(s, P.misc[0]);
   }
   if (committed > 0.f) F.hh[c] = fmaxf(F.hh[c] - committed, 0.f);
+  float lt[12];
+  lnmu_table(F.pigtab, lt);
+  float4 agg;
+  ushort4 col_unused;
+  finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, F.hh[c], F.m[c], s, agg, col_unused);
   float mu, ty, n;
-  composition_rheo(P, F.pigtab, s, mu, ty, n);
+  rheo_from_parts(P, agg, s.th, s.cu, mu, ty, n);
   set_rheo<MODE>(F, c, mu, ty, n);
-  stack_store<MODE>(F.sh, F.scu, F.pig, c, s);
+  stack_store<MODE>(F, F.sh, F.scu, F.pig, c, s);
+  F.agg[c] = agg;
 }
 
 // film.wgsl:1427-1434
@@ -146,10 +178,16 @@ __global__ void __launch_bounds__(256) k_clear_acc(Film F) {
   F.h_frame[c] = F.hh[c];
 }
 
-// film.wgsl:16-42
+// film.wgsl:16-42; with CLEAR the kernel also does clear_acc (film.wgsl:1427-1434)
+// for its cell, which the reference dispatches just before the first laplacian.
+template <bool CLEAR>
 __global__ void __launch_bounds__(256) k_laplacian(Film F) {
   TILE_PROLOGUE
   float hv = F.hh[c];
+  if (CLEAR) {
+    F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    F.h_frame[c] = hv;
+  }
   float s0 = hv + F.m[c];
   float hold = 0.f, pl = 0.f;
   if (hv > 0.f) hold = hold_level(P, nose_dist(F, c));
@@ -168,29 +206,57 @@ __global__ void __launch_bounds__(256) k_laplacian(Film F) {
   F.pres[c] = make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * (s0 - hold) + pl);
 }
 
-// film.wgsl:58-87
+// film.wgsl:58-87.  The HB flux of every cell of the tile and its 3-cell
+// halo is evaluated once into shared memory; each cell then sums its 7x7
+// window in the reference's row-major order, so the result is identical to
+// evaluating the flux 49 times per cell.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_plug(Film F) {
-  TILE_PROLOGUE
+  constexpr int R = 3, S = 16 + 2 * R;
+  __shared__ float sq[S * S], sm[S * S];  // flux q and mass h of each window cell
+  __shared__ uint8_t sy[S * S];           // bit 0: wet cell in the grid, bit 1: tau_y > 0
+  if ((F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) == 0u) return;
+  const DevParams& D = *F.P;
+  const cf_params& P = D.p;
+  const float gb = P.phys[0] * D.gxy;
+  const int x0 = (int)blockIdx.x * 16 - R, y0 = (int)blockIdx.y * 16 - R;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  for (int q = tid; q < S * S; q += 256) {
+    int x = x0 + q % S, y = y0 + q / S;
+    float qq = 0.f, mass = 0.f;
+    uint8_t yl = 0;
+    if (in_grid(F, x, y)) {
+      uint32_t n = idx(F, x, y);
+      float hn = F.hh[n];
+      if (hn > 0.f) {
+        float rx = rmu<MODE>(F, n), ry = rtau<MODE>(F, n);
+        yl = (uint8_t)(1u | (ry > 0.f ? 2u : 0u));
+        float yy, up;
+        hb_flux(gb, hn, fmaxf(rx, 1e-4f), ry, rn<MODE>(F, n), qq, yy, up);
+        mass = hn;
+      }
+    }
+    sq[q] = qq;
+    sm[q] = mass;
+    sy[q] = yl;
+  }
+  __syncthreads();
+  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const uint32_t c = idx(F, i, j);
   F.tmp[c] = 0.f;
   if (F.hh[c] <= 0.f) return;
-  float gb = P.phys[0] * D.gxy;
   if (gb < 1e-6f) return;
   float sum = 0.f, mass = 0.f;
   bool yielding = false;
-  for (int dy = -3; dy <= 3; ++dy)
-    for (int dx = -3; dx <= 3; ++dx) {
-      int x = i + dx, y = j + dy;
-      if (!in_grid(F, x, y)) continue;
-      uint32_t n = idx(F, x, y);
-      float hn = F.hh[n];
-      if (hn <= 0.f) continue;
-      float rx = rmu<MODE>(F, n), ry = rtau<MODE>(F, n);
-      if (ry > 0.f) yielding = true;
-      float q, yy, up;
-      hb_flux(gb, hn, fmaxf(rx, 1e-4f), ry, rn<MODE>(F, n), q, yy, up);
-      sum += q;
-      mass += hn;
+  for (int dy = 0; dy < 7; ++dy)
+    for (int dx = 0; dx < 7; ++dx) {
+      int q = (threadIdx.y + dy) * S + threadIdx.x + dx;
+      uint8_t fl = sy[q];
+      if (!(fl & 1u)) continue;  // outside the grid or dry
+      if (fl & 2u) yielding = true;
+      sum += sq[q];
+      mass += sm[q];
     }
   if (!yielding || mass <= 0.f) return;
   F.tmp[c] = sum / mass;
@@ -207,7 +273,6 @@ __global__ void __launch_bounds__(256) k_fluxes(Film F) {
 }
 
 // film.wgsl:516-537
-__device__ __forceinline__ bool nb_ok(const Film& F, int i, int j) { return in_grid(F, i, j) && cell_active(F, i, j); }
 __global__ void __launch_bounds__(256) k_limiter(Film F) {
   TILE_PROLOGUE
   float4 f = F.flux[c];
@@ -221,7 +286,8 @@ __global__ void __launch_bounds__(256) k_limiter(Film F) {
   F.alpha[c] = a;
 }
 
-// wetting back-fill: film.wgsl:847-860 / strata.wgsl:314-322
+// wetting back-fill (film.wgsl:847-860 / strata.wgsl:314-322) on the current
+// strata generation: cell c takes the top stratum of src
 template <int MODE>
 __device__ __forceinline__ void backfill(const Film& F, uint32_t c, uint32_t src, float hn) {
   float4 ts = F.sh[src];
@@ -231,10 +297,9 @@ __device__ __forceinline__ void backfill(const Film& F, uint32_t c, uint32_t src
   if (ts.z > 0.f) ks = 2;
   if (ts.w > 0.f) ks = 3;
   F.sh[c] = make_float4(hn, 0.f, 0.f, 0.f);
-  using Pig = typename Prec<MODE>::Pig;
-  copy_pig16<Pig>(pig_at<MODE>(F.pig, c, 0), pig_at<MODE>(F.pig, src, ks));
+  PigIO<MODE>::copy(F, F.pig, c, 0, F.pig, src, ks);
 #pragma unroll
-  for (int k = 1; k < 4; ++k) zero_pig16<Pig>(pig_at<MODE>(F.pig, c, k));
+  for (int k = 1; k < 4; ++k) PigIO<MODE>::zero(F, F.pig, c, k);
   float4 cs = F.scu[src];
   float cv = ks == 0 ? cs.x : (ks == 1 ? cs.y : (ks == 2 ? cs.z : cs.w));
   F.scu[c] = make_float4(cv, 0.f, 0.f, 0.f);
@@ -359,7 +424,7 @@ __device__ __forceinline__ float4 band_split(const Film& F, uint32_t cu, float h
   return make_float4(fr[0] * total, fr[1] * total, fr[2] * total, fr[3] * total);
 }
 
-// film.wgsl:475-514
+// film.wgsl:475-514 (acc_s face-major)
 template <int MODE>
 __global__ void __launch_bounds__(256) k_strata_split(Film F) {
   TILE_PROLOGUE
@@ -367,17 +432,20 @@ __global__ void __launch_bounds__(256) k_strata_split(Film F) {
   float a[4] = {a4.x, a4.y, a4.z, a4.w};
   const int ni[4] = {1, 0, 1, 1}, nj[4] = {0, 1, 1, -1};
   bool ok[4] = {i + 1 < (int)F.w, j + 1 < (int)F.h, i + 1 < (int)F.w && j + 1 < (int)F.h, i + 1 < (int)F.w && j > 0};
+  uint32_t flags = 0u;
 #pragma unroll 1
   for (int k = 0; k < 4; ++k) {
-    FaceOut ff = face_k<MODE>(F, D, i, j, k);
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a[k] != 0.f && ok[k]) {
+    if (a[k] != 0.f && ok[k]) {  // a face with no frame flux needs no recompute
+      FaceOut ff = face_k<MODE>(F, D, i, j, k);
       uint32_t cb = idx(F, i + ni[k], j + nj[k]);
       uint32_t cu = a[k] < 0.f ? cb : c;
       o = band_split(F, cu, 0.5f * (F.hh[c] + F.hh[cb]), ff.y, ff.up, a[k], ff.n);
+      if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f) flags |= 1u << k;
     }
-    F.acc_s[4 * (size_t)c + k] = o;
+    F.acc_s[(size_t)k * F.n + c] = o;
   }
+  F.fflags[c] = (uint8_t)flags;
 }
 
 // film.wgsl:1330-1361, plus the device-wide max/min the adaptive step reads
@@ -417,18 +485,17 @@ __global__ void __launch_bounds__(256) k_reduce_tiles(Film F) {
   }
 }
 
-// strata.wgsl:157-173
-__global__ void __launch_bounds__(256) k_strata_limit(Film F) {
-  TILE_PROLOGUE
+// strata.wgsl:157-173 for one active cell
+__device__ __forceinline__ float4 strata_limit_at(const Film& F, const cf_params& P, int i, int j) {
+  uint32_t c = idx(F, i, j);
+  float4 a0 = acc_face(F, c, 0), a1 = acc_face(F, c, 1), a2 = acc_face(F, c, 2), a3 = acc_face(F, c, 3);
   float out[4];
-  const float4* as = F.acc_s + 4 * (size_t)c;
-  float4 a0 = as[0], a1 = as[1], a2 = as[2], a3 = as[3];
   out[0] = fmaxf(a0.x, 0.f) + fmaxf(a1.x, 0.f) + fmaxf(a2.x, 0.f) + fmaxf(a3.x, 0.f);
   out[1] = fmaxf(a0.y, 0.f) + fmaxf(a1.y, 0.f) + fmaxf(a2.y, 0.f) + fmaxf(a3.y, 0.f);
   out[2] = fmaxf(a0.z, 0.f) + fmaxf(a1.z, 0.f) + fmaxf(a2.z, 0.f) + fmaxf(a3.z, 0.f);
   out[3] = fmaxf(a0.w, 0.f) + fmaxf(a1.w, 0.f) + fmaxf(a2.w, 0.f) + fmaxf(a3.w, 0.f);
   auto addn = [&](uint32_t n, int f) {
-    float4 v = F.acc_s[4 * (size_t)n + f];
+    float4 v = acc_face(F, n, f);
     out[0] += fmaxf(-v.x, 0.f);
     out[1] += fmaxf(-v.y, 0.f);
     out[2] += fmaxf(-v.z, 0.f);
@@ -442,20 +509,23 @@ __global__ void __launch_bounds__(256) k_strata_limit(Film F) {
   float t[4] = {th.x, th.y, th.z, th.w}, a[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) a[k] = out[k] > 0.f ? fminf(1.f, t[k] * P.dx / out[k]) : 1.f;
-  F.alpha_s[c] = make_float4(a[0], a[1], a[2], a[3]);
+  return make_float4(a[0], a[1], a[2], a[3]);
 }
 
-__device__ __forceinline__ float sel4(float4 v, int k) {
-  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+// strata_limit as a dispatch of its own (inspection only; the strata pass
+// computes the same values in shared memory)
+__global__ void __launch_bounds__(256) k_strata_limit(Film F) {
+  TILE_PROLOGUE
+  F.alpha_s[c] = strata_limit_at(F, P, i, j);
 }
-__device__ __forceinline__ float4 neg4(float4 v) { return make_float4(-v.x, -v.y, -v.z, -v.w); }
 
-// strata.wgsl:175-188; the face volumes arrive by value (one per stratum).
+// strata.wgsl:175-188; the face volumes arrive by value (one per stratum) and
+// the source's alpha_s comes from the caller
 template <int MODE>
-__device__ __forceinline__ void inflow_from(const Film& F, const cf_params& P, Stack& s, uint32_t cn, float4 f) {
-  const float4 an4 = F.alpha_s[cn], th4 = F.sh[cn], cu4 = F.scu[cn];
+__device__ __forceinline__ void inflow_from(const Film& F, const cf_params& P, Stack& s, uint32_t cn, float4 an4,
+                                            float4 f) {
+  const float4 th4 = F.sh[cn], cu4 = F.scu[cn];
   float z0 = 0.f;
-  using Pig = typename Prec<MODE>::Pig;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const float thn = sel4(th4, k);
@@ -463,36 +533,88 @@ __device__ __forceinline__ void inflow_from(const Film& F, const cf_params& P, S
     const float v = sel4(f, k) * sel4(an4, k) * P.inv_dx;
     if (v > 0.f && thn > 0.f) {
       float pg[16];
-      load_pig16<Pig>(pig_at<MODE>(F.pig, cn, k), pg);
+      PigIO<MODE>::load(F, F.pig, cn, k, pg);
       stack_add_band(s, z0, z1, v, pg, sel4(cu4, k), P.misc[0], P.misc[1]);
     }
     z0 = z1;
   }
 }
 
-// strata.wgsl:190-274
-template <int MODE>
-__global__ void __launch_bounds__(256) k_strata_update(Film F) {
+// Face flags from acc_s as strata_split writes them (for an inspection
+// dispatch of the strata pass that does not follow a strata_split).
+__global__ void __launch_bounds__(256) k_face_flags(Film F) {
   TILE_PROLOGUE
-  using Pig = typename Prec<MODE>::Pig;
-  const float4* as = F.acc_s + 4 * (size_t)c;
-  float4 fr4 = as[0], fu4 = as[1], fd4 = as[2], fe4 = as[3];
-  float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 fl4 = z4, fdn4 = z4, fll4 = z4, flu4 = z4;
-  uint32_t cl = c, cd = c, cll = c, clu = c;
-  if (i > 0 && cell_active(F, i - 1, j)) { cl = c - 1; fl4 = F.acc_s[4 * (size_t)cl]; }
-  if (j > 0 && cell_active(F, i, j - 1)) { cd = c - F.w; fdn4 = F.acc_s[4 * (size_t)cd + 1]; }
-  if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1)) { cll = c - F.w - 1; fll4 = F.acc_s[4 * (size_t)cll + 2]; }
-  if (i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1)) { clu = c + F.w - 1; flu4 = F.acc_s[4 * (size_t)clu + 3]; }
-  auto nz = [](float4 v) { return v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f; };
-  if (!(nz(fr4) || nz(fu4) || nz(fd4) || nz(fe4) || nz(fl4) || nz(fdn4) || nz(fll4) || nz(flu4))) {
-    float hc = F.hh[c];
-    float4 t4 = F.sh[c];
+  uint32_t flags = 0u;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float4 o = acc_face(F, c, k);
+    if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f) flags |= 1u << k;
+  }
+  F.fflags[c] = (uint8_t)flags;
+}
+
+// Whether strata_update (strata.wgsl:190-274) takes its full path for this
+// active cell: any of its 8 faces carries a strata flux (the face flags of
+// strata_split), or its renormalised stack is not compact (:222-228).
+__device__ __forceinline__ bool needs_full(const Film& F, const cf_params& P, int i, int j, uint32_t c, float hc) {
+  if (F.fflags[c] != 0u) return true;
+  if (i > 0 && cell_active(F, i - 1, j) && (F.fflags[c - 1] & 1u)) return true;
+  if (j > 0 && cell_active(F, i, j - 1) && (F.fflags[c - F.w] & 2u)) return true;
+  if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1) && (F.fflags[c - F.w - 1] & 4u)) return true;
+  if (i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1) && (F.fflags[c + F.w - 1] & 8u)) return true;
+  if (hc <= 0.f) return false;
+  float4 t4 = F.sh[c];
+  float th[4] = {fmaxf(t4.x, 0.f), fmaxf(t4.y, 0.f), fmaxf(t4.z, 0.f), fmaxf(t4.w, 0.f)};
+  float nt[4] = {th[0], th[1], th[2], th[3]};
+  float sum = th[0] + th[1] + th[2] + th[3];
+  if (sum > 0.f) {
+    float sc = hc / sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) nt[k] = th[k] * sc;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (nt[k] <= 0.f && nt[k + 1] > 0.f) return true;
+    if (nt[k] > 0.f && nt[k] < P.misc[0] && nt[k + 1] > 0.f) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm, float* ltab, int tid, int nthreads) {
+  for (int q = tid; q < 480; q += nthreads) tab[q] = F.pigtab[q];
+  if (tid < 48) cm[tid] = F.cmf[tid];
+  if (tid < 12) ltab[tid] = logf(fmaxf(F.pigtab[tid * 40 + 32], 1e-3f));
+}
+
+// Strata pass, part 1 (every cell not taken by part 2): the fast path of
+// strata_update (strata.wgsl:212-237: renormalise the stack to h and carry
+// the pigments over) into the next generation, streamed stratum by stratum
+// through the shade (shade.wgsl:28-84) and the composition aggregates.
+// Inactive tiles carry their strata over unchanged and are shaded, as the
+// reference's full-grid shade does.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_strata_fast(Film F) {
+  __shared__ float tab[480];
+  __shared__ float cm[48];
+  __shared__ float ltab[12];
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  load_tables(F, tab, cm, ltab, tid, 256);
+  __syncthreads();
+  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const uint32_t c = idx(F, i, j);
+  const cf_params& P = F.P->p;
+  const bool act = (F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) != 0u;
+  const float hc = F.hh[c];
+  if (act && needs_full(F, P, i, j, c, hc)) return;
+  float4 t4 = F.sh[c], cu = F.scu[c];
+  float nt[4] = {t4.x, t4.y, t4.z, t4.w};
+  if (act) {
     float th[4] = {fmaxf(t4.x, 0.f), fmaxf(t4.y, 0.f), fmaxf(t4.z, 0.f), fmaxf(t4.w, 0.f)};
-    float nt[4] = {0.f, 0.f, 0.f, 0.f};
-    float4 cu = F.scu[c];
     if (hc <= 0.f) {
-      cu = z4;
+      cu = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) nt[k] = 0.f;
     } else {
       float sum = th[0] + th[1] + th[2] + th[3];
 #pragma unroll
@@ -503,23 +625,68 @@ __global__ void __launch_bounds__(256) k_strata_update(Film F) {
         for (int k = 0; k < 4; ++k) nt[k] = th[k] * sc;
       }
     }
-    bool plain = true;
+  }
+  F.sh2[c] = make_float4(nt[0], nt[1], nt[2], nt[3]);
+  F.scu2[c] = cu;
+  CellAcc acc;
+  acc.begin(F.refl + (size_t)c * 16);
+  const bool dbg = P.flags[0] == 1u;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      if (nt[k] <= 0.f && nt[k + 1] > 0.f) plain = false;
-      if (nt[k] > 0.f && nt[k] < P.misc[0] && nt[k + 1] > 0.f) plain = false;
-    }
-    if (plain) {
-      F.sh2[c] = make_float4(nt[0], nt[1], nt[2], nt[3]);
-      F.scu2[c] = cu;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) copy_pig16<Pig>(pig_at<MODE>(F.pig2, c, k), pig_at<MODE>(F.pig, c, k));
-      return;
+  for (int k = 0; k < 4; ++k) {
+    PigIO<MODE>::copy(F, F.pig2, c, k, F.pig, c, k);
+    if (nt[k] > 0.f) {
+      float pg[16];
+      PigIO<MODE>::load(F, F.pig, c, k, pg);
+      acc.add(k, nt[k], sel4(cu, k), pg, hc, ltab, tab, dbg);
+    } else {
+      acc.ssum += nt[k];
     }
   }
+  F.agg[c] = acc.agg(P);
+  F.color[c] = acc.color(P, cm, hc, F.m[c]);
+}
+
+// Strata pass, part 2: the cells of active tiles that needs_full selects.
+// strata_limit (strata.wgsl:157-173) of the tile and its 1-cell halo goes to
+// shared memory (only in blocks that have such a cell), then the full
+// strata_update (:238-273) builds the new stack, which is stored into the
+// next generation, shaded and composed.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_strata_full(Film F) {
+  __shared__ float tab[480];
+  __shared__ float cm[48];
+  __shared__ float ltab[12];
+  __shared__ float4 s_alpha[18 * 18];
+  if ((F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) == 0u) return;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const cf_params& P = F.P->p;
+  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+  const bool inside = i < (int)F.w && j < (int)F.h;
+  const uint32_t c = inside ? idx(F, i, j) : 0u;
+  const float hc = inside ? F.hh[c] : 0.f;
+  const bool mine = inside && needs_full(F, P, i, j, c, hc);
+  if (!__syncthreads_or(mine)) return;
+  load_tables(F, tab, cm, ltab, tid, 256);
+  for (int q = tid; q < 18 * 18; q += 256) {
+    int x = (int)blockIdx.x * 16 - 1 + q % 18, y = (int)blockIdx.y * 16 - 1 + q / 18;
+    float4 a = make_float4(1.f, 1.f, 1.f, 1.f);
+    if (in_grid(F, x, y) && cell_active(F, x, y)) a = strata_limit_at(F, P, x, y);
+    s_alpha[q] = a;
+  }
+  __syncthreads();
+  if (!mine) return;
+  auto sa = [&](int di, int dj) { return s_alpha[(threadIdx.y + 1 + dj) * 18 + threadIdx.x + 1 + di]; };
+  const float4 fr4 = acc_face(F, c, 0), fu4 = acc_face(F, c, 1), fd4 = acc_face(F, c, 2), fe4 = acc_face(F, c, 3);
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 fl4 = z4, fdn4 = z4, fll4 = z4, flu4 = z4;
+  bool hl = false, hd = false, hll = false, hlu = false;
+  if (i > 0 && cell_active(F, i - 1, j)) { hl = true; fl4 = acc_face(F, c - 1, 0); }
+  if (j > 0 && cell_active(F, i, j - 1)) { hd = true; fdn4 = acc_face(F, c - F.w, 1); }
+  if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1)) { hll = true; fll4 = acc_face(F, c - F.w - 1, 2); }
+  if (i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1)) { hlu = true; flu4 = acc_face(F, c + F.w - 1, 3); }
   Stack s;
-  stack_load<MODE>(F, F.pig, c, s);
-  const float4 a4 = F.alpha_s[c];
+  stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
+  const float4 a4 = sa(0, 0);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     float out = fmaxf(sel4(fr4, k), 0.f) + fmaxf(sel4(fu4, k), 0.f) + fmaxf(sel4(fd4, k), 0.f) +
@@ -527,15 +694,14 @@ __global__ void __launch_bounds__(256) k_strata_update(Film F) {
                 fmaxf(-sel4(fll4, k), 0.f) + fmaxf(-sel4(flu4, k), 0.f);
     s.th[k] = fmaxf(s.th[k] - out * sel4(a4, k) * P.inv_dx, 0.f);
   }
-  if (i + 1 < (int)F.w) inflow_from<MODE>(F, P, s, c + 1, neg4(fr4));
-  if (j + 1 < (int)F.h) inflow_from<MODE>(F, P, s, c + F.w, neg4(fu4));
-  if (i + 1 < (int)F.w && j + 1 < (int)F.h) inflow_from<MODE>(F, P, s, c + F.w + 1, neg4(fd4));
-  if (i + 1 < (int)F.w && j > 0) inflow_from<MODE>(F, P, s, c - F.w + 1, neg4(fe4));
-  if (cl != c) inflow_from<MODE>(F, P, s, cl, fl4);
-  if (cd != c) inflow_from<MODE>(F, P, s, cd, fdn4);
-  if (cll != c) inflow_from<MODE>(F, P, s, cll, fll4);
-  if (clu != c) inflow_from<MODE>(F, P, s, clu, flu4);
-  float hc = F.hh[c];
+  if (i + 1 < (int)F.w) inflow_from<MODE>(F, P, s, c + 1, sa(1, 0), neg4(fr4));
+  if (j + 1 < (int)F.h) inflow_from<MODE>(F, P, s, c + F.w, sa(0, 1), neg4(fu4));
+  if (i + 1 < (int)F.w && j + 1 < (int)F.h) inflow_from<MODE>(F, P, s, c + F.w + 1, sa(1, 1), neg4(fd4));
+  if (i + 1 < (int)F.w && j > 0) inflow_from<MODE>(F, P, s, c - F.w + 1, sa(1, -1), neg4(fe4));
+  if (hl) inflow_from<MODE>(F, P, s, c - 1, sa(-1, 0), fl4);
+  if (hd) inflow_from<MODE>(F, P, s, c - F.w, sa(0, -1), fdn4);
+  if (hll) inflow_from<MODE>(F, P, s, c - F.w - 1, sa(-1, -1), fll4);
+  if (hlu) inflow_from<MODE>(F, P, s, c + F.w - 1, sa(-1, 1), flu4);
   float sum = s.th[0] + s.th[1] + s.th[2] + s.th[3];
   if (hc <= 0.f) {
 #pragma unroll
@@ -546,24 +712,23 @@ __global__ void __launch_bounds__(256) k_strata_update(Film F) {
     for (int q = 0; q < 4; ++q) s.th[q] *= kk;
   }
   stack_compact(s, P.misc[0]);
-  stack_store<MODE>(F.sh2, F.scu2, F.pig2, c, s);
-}
-
-// strata.wgsl:276-286
-template <int MODE>
-__global__ void __launch_bounds__(256) k_copy_back(Film F) {
-  TILE_PROLOGUE
-  using Pig = typename Prec<MODE>::Pig;
-  F.sh[c] = F.sh2[c];
-  F.scu[c] = F.scu2[c];
+  stack_store<MODE>(F, F.sh2, F.scu2, F.pig2, c, s);
+  // the stored (rounded) slots are what the shade and later frames see
 #pragma unroll
-  for (int k = 0; k < 4; ++k) copy_pig16<Pig>(pig_at<MODE>(F.pig, c, k), pig_at<MODE>(F.pig2, c, k));
+  for (int k = 0; k < 4; ++k) PigIO<MODE>::load(F, F.pig2, c, k, s.pg[k]);
+  if (hc > 0.f && !(s.th[0] + s.th[1] + s.th[2] + s.th[3] > 0.f)) atomicAdd(&F.stats->fill_needed, 1u);
+  float4 agg;
+  ushort4 col;
+  finish_stack(P, ltab, tab, cm, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
+  F.agg[c] = agg;
+  F.color[c] = col;
 }
 
-// strata.wgsl:288-323, Jacobi in two passes: select reads only the sums of
-// the current strata; apply writes only cells that had no strata, and its
-// sources always have strata, so no pass reads what it writes.
+// strata.wgsl:288-323, Jacobi in two passes over the current generation:
+// select reads only the sums of the strata; apply writes only cells that had
+// none, whose sources always have some, so no pass reads what it writes.
 __global__ void __launch_bounds__(256) k_fill_select(Film F) {
+  if (F.stats->fill_needed == 0u) return;
   TILE_PROLOGUE
   int32_t src = -1;
   float hc = F.hh[c];
@@ -586,107 +751,43 @@ __global__ void __launch_bounds__(256) k_fill_select(Film F) {
   }
   F.fill_src[c] = src;
 }
+// ...and re-shades the filled cell and refreshes its aggregates.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_fill_apply(Film F) {
+  if (F.stats->fill_needed == 0u) return;
   TILE_PROLOGUE
   int32_t src = F.fill_src[c];
   if (src < 0) return;
-  backfill<MODE>(F, c, (uint32_t)src, F.hh[c]);
+  float hc = F.hh[c];
+  backfill<MODE>(F, c, (uint32_t)src, hc);
+  Stack s;
+  stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
+  float lt[12];
+  lnmu_table(F.pigtab, lt);
+  float4 agg;
+  ushort4 col;
+  finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
+  F.agg[c] = agg;
+  F.color[c] = col;
 }
 
-// shade.wgsl:28-84 (colour and roughness; full grid)
+// Aggregates and colour of the current state (after a state upload, or for
+// an inspection dispatch of cure or shade).
 template <int MODE>
-__global__ void __launch_bounds__(256) k_shade(Film F) {
-  __shared__ float tab[12 * 40];
-  __shared__ float cm[48];
-  int tid = threadIdx.y * 16 + threadIdx.x;
-  for (int q = tid; q < 480; q += 256) tab[q] = F.pigtab[q];
-  if (tid < 48) cm[tid] = F.cmf[tid];
-  __syncthreads();
+__global__ void __launch_bounds__(256) k_compose(Film F, int shade) {
   const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   const cf_params& P = F.P->p;
-  using Pig = typename Prec<MODE>::Pig;
-  float r[16];
-  const uint16_t* rf = F.refl + (size_t)c * 16;
-  {
-    const uint4* p = reinterpret_cast<const uint4*>(rf);
-    uint4 a = p[0], b = p[1];
-    uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      r[2 * k] = h16_to_f(wv[k] & 0xffffu);
-      r[2 * k + 1] = h16_to_f(wv[k] >> 16);
-    }
-  }
-  float hv = F.hh[c];
-  float wet = 0.f, cure_top = 0.f;
-  float4 th4 = F.sh[c], cu4 = F.scu[c];
-  float th[4] = {th4.x, th4.y, th4.z, th4.w}, cu[4] = {cu4.x, cu4.y, cu4.z, cu4.w};
-  if (hv > 0.f) {
-    for (int k = 0; k < 4; ++k) {
-      float t = th[k];
-      if (t <= 0.f) continue;
-      float pg[16];
-      load_pig16<Pig>(pig_at<MODE>(F.pig, c, k), pg);
-      float w[12], sc;
-      layer_weights(pg, tab, w, sc);
-#pragma unroll 4
-      for (int b = 0; b < 16; ++b) {
-        float kk, ss, rr, tt;
-        layer_ks_band(pg, w, sc, tab, b, kk, ss);
-        km_layer(kk, ss, t, rr, tt);
-        r[b] = composite(rr, tt, r[b]);
-      }
-      wet = 1.0f - cu[k];
-      cure_top = cu[k];
-    }
-  }
-  const float k1 = 0.04f;
-  float k2 = 0.4f * (1.0f - wet) + 0.6f * wet;
-  float X = 0.f, Y = 0.f, Z = 0.f;
-#pragma unroll
-  for (int b = 0; b < 16; ++b) {
-    float rb = (1.0f - k1) * (1.0f - k2) * r[b] / fmaxf(1.0f - k2 * r[b], 1e-3f);
-    X += rb * cm[3 * b];
-    Y += rb * cm[3 * b + 1];
-    Z += rb * cm[3 * b + 2];
-  }
-  float rgb[3] = {3.2406f * X - 1.5372f * Y - 0.4986f * Z, -0.9689f * X + 1.8758f * Y + 0.0415f * Z,
-                  0.0557f * X - 0.2040f * Y + 1.0570f * Z};
-#pragma unroll
-  for (int q = 0; q < 3; ++q) rgb[q] = fmaxf(rgb[q], 0.f);
-  auto smooth = [](float e0, float e1, float x) {
-    float t = fminf(fmaxf((x - e0) / (e1 - e0), 0.f), 1.f);
-    return t * t * (3.0f - 2.0f * t);
-  };
-  float mv = F.m[c];
-  float painted = smooth(60e-6f, 150e-6f, mv);
-  cure_top = fmaxf(cure_top, painted * (1.0f - smooth(0.f, 50e-6f, hv)));
-  float sq = sqrtf(cure_top);
-  float rough = 0.06f * (1.0f - sq) + 0.35f * sq;
-  if (hv <= 0.f) rough = 0.85f * (1.0f - painted) + 0.35f * painted;
-  if (P.flags[0] == 1u && hv > 0.f) {  // shade.wgsl:65-82 invariant view
-    float ssum = th[0] + th[1] + th[2] + th[3];
-    bool bad = false;
-    uint32_t cnt = 0;
-    for (int k = 0; k < 4; ++k) {
-      if (th[k] > 0.f) cnt = k + 1;
-      if (th[k] <= 0.f) continue;
-      float pg[16];
-      load_pig16<Pig>(pig_at<MODE>(F.pig, c, k), pg);
-      float cs = 0.f;
-      for (int q = 0; q < 13; ++q) cs += pg[q];
-      if (!(cs > 0.f)) bad = true;
-    }
-    if (ssum <= 0.f) { rgb[0] = 0.f; rgb[1] = 0.f; rgb[2] = 1.f; }
-    else if (bad) { rgb[0] = 1.f; rgb[1] = 0.f; rgb[2] = 0.f; }
-    else if (fabsf(ssum - hv) > 0.01f * hv) { rgb[0] = 0.f; rgb[1] = 1.f; rgb[2] = 0.f; }
-    else { float v = 0.3f + 0.15f * (float)cnt; rgb[0] = v; rgb[1] = v; rgb[2] = v; }
-  }
-  F.color[c] = make_ushort4(__half_as_ushort(__float2half_rn(rgb[0])), __half_as_ushort(__float2half_rn(rgb[1])),
-                            __half_as_ushort(__float2half_rn(rgb[2])), __half_as_ushort(__float2half_rn(rough)));
+  Stack s;
+  stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
+  float lt[12];
+  lnmu_table(F.pigtab, lt);
+  float4 agg;
+  ushort4 col;
+  finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, F.hh[c], F.m[c], s, agg, col);
+  F.agg[c] = agg;
+  if (shade) F.color[c] = col;
 }
 
 // FP64 mass / NaN census (compute_stats, src/main.rs:1679-1773)
@@ -719,6 +820,7 @@ __global__ void k_stats_reset(Film F) {
   F.stats->h_max_bits = 0u;
   F.stats->mu_min_bits = __float_as_uint(1e9f);
   F.stats->active_tiles = 0u;
+  F.stats->fill_needed = 0u;
 }
 __global__ void k_mass_reset(Film F) {
   F.stats->wet_sum = 0.0;
@@ -726,6 +828,7 @@ __global__ void k_mass_reset(Film F) {
   F.stats->wet_cells = 0ull;
   F.stats->nan_cells = 0ull;
 }
+__global__ void k_set_fill_needed(Film F) { F.stats->fill_needed = 1u; }
 
 // Device-side adaptive dt (choose_substeps formulas, src/film/mod.rs:919-933,
 // one substep per frame) and the dt-dependent fields of update_params
@@ -738,7 +841,6 @@ __global__ void k_adaptive_params(DevParams* Dp, DevStats* S) {
   float mu_raw = __uint_as_float(S->mu_min_bits);
   float mu_stat = mu_raw > 1e8f ? 1.0f : mu_raw;
   float dx = P.dx;
-  // adaptive dt
   float h_max = fmaxf(h_stat, 1e-5f);
   float mu = fmaxf(mu_stat, 1e-3f);
   float speed = fminf(__fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(D.s_rho, D.gxy), h_max), h_max), mu), D.s_vcap);
@@ -750,7 +852,6 @@ __global__ void k_adaptive_params(DevParams* Dp, DevStats* S) {
   float dx2 = __fmul_rn(dx, dx), dx4 = __fmul_rn(dx2, dx2);
   float cap = __fmul_rn(__fmul_rn(32.0f, D.s_sigma), fminf(mob, D.s_mcap));
   if (cap > 0.f) dt = fminf(dt, __fdiv_rn(dx4, cap));
-  // update_params(frame_dt = dt, substeps = 1)
   float frame_dt = dt;
   float m_cap_exp = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(0.5f, dx), dx), dx), dx),
                               __fmul_rn(__fmul_rn(32.0f, D.s_sigma), dt));
@@ -786,25 +887,54 @@ __global__ void k_adaptive_params(DevParams* Dp, DevStats* S) {
   S->last_dt = dt;
 }
 
-// ---- state I/O conversions ----
-template <class T>
-__global__ void k_pig_import(Film F, const void* src, int fmt, size_t nslots) {
-  size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (q >= nslots) return;
-  float v;
-  if (fmt == CF_PIG_F32) v = ((const float*)src)[q];
-  else if (fmt == CF_PIG_F16) v = __half2float(((const __half*)src)[q]);
-  else v = __bfloat162float(((const __nv_bfloat16*)src)[q]);
-  ((T*)F.pig)[q] = from_f<T>(v);
+// ---- state I/O: reference pigment layout [cell][stratum][slot] <-> chunks ----
+// one thread per (cell, stratum, chunk)
+template <int MODE>
+__global__ void k_pig_import(Film F, uint4* dst, const void* src, int fmt) {
+  constexpr int QN = PigIO<MODE>::QN, PER = 16 / QN;  // slots per chunk
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)F.n * 4 * QN) return;
+  uint32_t c = (uint32_t)(t / (4 * QN));
+  int k = (int)((t / QN) % 4), q = (int)(t % QN);
+  float v[16] = {};
+  for (int e = 0; e < PER; ++e) {
+    size_t s = (size_t)c * 64 + 16 * k + q * PER + e;
+    float x;
+    if (fmt == CF_PIG_F32) x = ((const float*)src)[s];
+    else if (fmt == CF_PIG_F16) x = h16_to_f(((const uint16_t*)src)[s]);
+    else x = b16_to_f(((const uint16_t*)src)[s]);
+    v[q * PER + e] = x;
+  }
+  // pack this chunk only
+  uint32_t wv[4];
+  for (int e = 0; e < 4; ++e) {
+    if (MODE == CF_PREC_FP32) wv[e] = __float_as_uint(v[q * PER + e]);
+    else if (MODE == CF_PREC_REFERENCE) wv[e] = f_to_h16(v[q * PER + 2 * e]) | (f_to_h16(v[q * PER + 2 * e + 1]) << 16);
+    else wv[e] = f_to_b16(v[q * PER + 2 * e]) | (f_to_b16(v[q * PER + 2 * e + 1]) << 16);
+  }
+  dst[PigIO<MODE>::at(F, c, k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
 }
-template <class T>
-__global__ void k_pig_export(Film F, void* dst, int fmt, size_t nslots) {
-  size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (q >= nslots) return;
-  float v = to_f(((const T*)F.pig)[q]);
-  if (fmt == CF_PIG_F32) ((float*)dst)[q] = v;
-  else if (fmt == CF_PIG_F16) ((__half*)dst)[q] = __float2half_rn(v);
-  else ((__nv_bfloat16*)dst)[q] = __float2bfloat16_rn(v);
+template <int MODE>
+__global__ void k_pig_export(Film F, const uint4* srcp, void* dst, int fmt) {
+  constexpr int QN = PigIO<MODE>::QN, PER = 16 / QN;
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)F.n * 4 * QN) return;
+  uint32_t c = (uint32_t)(t / (4 * QN));
+  int k = (int)((t / QN) % 4), q = (int)(t % QN);
+  uint4 u = srcp[PigIO<MODE>::at(F, c, k, q)];
+  uint32_t wv[4] = {u.x, u.y, u.z, u.w};
+  for (int e = 0; e < PER; ++e) {
+    float x;
+    if (MODE == CF_PREC_FP32) x = __uint_as_float(wv[e]);
+    else {
+      uint32_t bits = (e & 1) ? (wv[e / 2] >> 16) : (wv[e / 2] & 0xffffu);
+      x = MODE == CF_PREC_REFERENCE ? h16_to_f(bits) : b16_to_f(bits);
+    }
+    size_t s = (size_t)c * 64 + 16 * k + q * PER + e;
+    if (fmt == CF_PIG_F32) ((float*)dst)[s] = x;
+    else if (fmt == CF_PIG_F16) ((uint16_t*)dst)[s] = (uint16_t)f_to_h16(x);
+    else ((uint16_t*)dst)[s] = (uint16_t)f_to_b16(x);
+  }
 }
 template <class Rh>
 __global__ void k_rheo_import(Film F, const float2* src, float n_global, size_t n) {
@@ -830,64 +960,76 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
 
 static inline dim3 tiles_grid(const Film& F) { return dim3(F.tw, F.th); }
 
+static void swap_generations(Film& F) {
+  float4* t = F.sh; F.sh = F.sh2; F.sh2 = t;
+  t = F.scu; F.scu = F.scu2; F.scu2 = t;
+  uint4* p = F.pig; F.pig = F.pig2; F.pig2 = p;
+}
+
+// Enqueues one frame; returns the number of kernel launches.  F's strata
+// generations are swapped in place.
 template <int MODE>
-static void frame_t(const Film& F, uint32_t substeps, int all_active, cudaStream_t st) {
+static uint32_t frame_t(Film& F, uint32_t substeps, int all_active, cudaStream_t st) {
   dim3 g = tiles_grid(F), b(16, 16);
-  uint32_t nt = F.tw * F.th;
-  k_stats_reset<<<1, 1, 0, st>>>(F);
-  k_mark_tiles<<<g, b, 0, st>>>(F);
-  k_compact_tiles<<<(nt + 255) / 256, 256, 0, st>>>(F, all_active);
-  k_cure<MODE><<<g, b, 0, st>>>(F);
-  k_clear_acc<<<g, b, 0, st>>>(F);
+  uint32_t nt = F.tw * F.th, n = 0;
+  k_stats_reset<<<1, 1, 0, st>>>(F); ++n;
+  k_mark_tiles<<<g, b, 0, st>>>(F); ++n;
+  k_compact_tiles<<<(nt + 255) / 256, 256, 0, st>>>(F, all_active); ++n;
+  k_cure<MODE><<<g, b, 0, st>>>(F); ++n;
+  if (substeps == 0) { k_clear_acc<<<g, b, 0, st>>>(F); ++n; }
   for (uint32_t s = 0; s < substeps; ++s) {
-    k_laplacian<<<g, b, 0, st>>>(F);
+    if (s == 0) k_laplacian<true><<<g, b, 0, st>>>(F);
+    else k_laplacian<false><<<g, b, 0, st>>>(F);
     k_plug<MODE><<<g, b, 0, st>>>(F);
     k_fluxes<MODE><<<g, b, 0, st>>>(F);
     k_limiter<<<g, b, 0, st>>>(F);
     k_apply<MODE><<<g, b, 0, st>>>(F);
     cudaMemcpyAsync(F.delta_old, F.delta, sizeof(uint32_t) * (size_t)F.w * F.h, cudaMemcpyDeviceToDevice, st);
     k_nose<<<g, b, 0, st>>>(F);
+    n += 6;
   }
-  k_laplacian<<<g, b, 0, st>>>(F);
+  k_laplacian<false><<<g, b, 0, st>>>(F);
   k_strata_split<MODE><<<g, b, 0, st>>>(F);
   k_reduce_tiles<MODE><<<dim3((F.w + 63) / 64, (F.h + 63) / 64), b, 0, st>>>(F);
-  k_strata_limit<<<g, b, 0, st>>>(F);
-  k_strata_update<MODE><<<g, b, 0, st>>>(F);
-  k_copy_back<MODE><<<g, b, 0, st>>>(F);
+  k_strata_fast<MODE><<<g, b, 0, st>>>(F);
+  k_strata_full<MODE><<<g, b, 0, st>>>(F);
+  n += 5;
+  swap_generations(F);
   for (int r = 0; r < 6; ++r) {
     k_fill_select<<<g, b, 0, st>>>(F);
     k_fill_apply<MODE><<<g, b, 0, st>>>(F);
+    n += 2;
   }
-  k_shade<MODE><<<g, b, 0, st>>>(F);
+  return n;
 }
 
-void launch_frame(const Film& F, int mode, uint32_t substeps, int all_active, cudaStream_t st) {
-  if (mode == CF_PREC_REFERENCE) frame_t<CF_PREC_REFERENCE>(F, substeps, all_active, st);
-  else if (mode == CF_PREC_FP32) frame_t<CF_PREC_FP32>(F, substeps, all_active, st);
-  else frame_t<CF_PREC_BF16>(F, substeps, all_active, st);
+uint32_t launch_frame(Film& F, int mode, uint32_t substeps, int all_active, cudaStream_t st) {
+  if (mode == CF_PREC_REFERENCE) return frame_t<CF_PREC_REFERENCE>(F, substeps, all_active, st);
+  if (mode == CF_PREC_FP32) return frame_t<CF_PREC_FP32>(F, substeps, all_active, st);
+  return frame_t<CF_PREC_BF16>(F, substeps, all_active, st);
 }
 
 void launch_adaptive_params(DevParams* Dp, DevStats* S, cudaStream_t st) { k_adaptive_params<<<1, 1, 0, st>>>(Dp, S); }
 
-template <int MODE>
-static void cure_only_t(const Film& F, cudaStream_t st) {
-  k_cure<MODE><<<tiles_grid(F), dim3(16, 16), 0, st>>>(F);
-}
 void launch_cure(const Film& F, int mode, cudaStream_t st) {
-  if (mode == CF_PREC_REFERENCE) cure_only_t<CF_PREC_REFERENCE>(F, st);
-  else if (mode == CF_PREC_FP32) cure_only_t<CF_PREC_FP32>(F, st);
-  else cure_only_t<CF_PREC_BF16>(F, st);
+  dim3 g = tiles_grid(F), b(16, 16);
+  if (mode == CF_PREC_REFERENCE) k_cure<CF_PREC_REFERENCE><<<g, b, 0, st>>>(F);
+  else if (mode == CF_PREC_FP32) k_cure<CF_PREC_FP32><<<g, b, 0, st>>>(F);
+  else k_cure<CF_PREC_BF16><<<g, b, 0, st>>>(F);
 }
 
-template <int MODE>
-static void reduce_only_t(const Film& F, cudaStream_t st) {
-  k_stats_reset<<<1, 1, 0, st>>>(F);
-  k_reduce_tiles<MODE><<<dim3((F.w + 63) / 64, (F.h + 63) / 64), dim3(16, 16), 0, st>>>(F);
+void launch_compose(const Film& F, int mode, int shade, cudaStream_t st) {
+  dim3 g = tiles_grid(F), b(16, 16);
+  if (mode == CF_PREC_REFERENCE) k_compose<CF_PREC_REFERENCE><<<g, b, 0, st>>>(F, shade);
+  else if (mode == CF_PREC_FP32) k_compose<CF_PREC_FP32><<<g, b, 0, st>>>(F, shade);
+  else k_compose<CF_PREC_BF16><<<g, b, 0, st>>>(F, shade);
 }
+
 void launch_reduce(const Film& F, int mode, cudaStream_t st) {
-  if (mode == CF_PREC_REFERENCE) reduce_only_t<CF_PREC_REFERENCE>(F, st);
-  else if (mode == CF_PREC_FP32) reduce_only_t<CF_PREC_FP32>(F, st);
-  else reduce_only_t<CF_PREC_BF16>(F, st);
+  dim3 g((F.w + 63) / 64, (F.h + 63) / 64), b(16, 16);
+  k_stats_reset<<<1, 1, 0, st>>>(F);
+  if (mode == CF_PREC_BF16) k_reduce_tiles<CF_PREC_BF16><<<g, b, 0, st>>>(F);
+  else k_reduce_tiles<CF_PREC_FP32><<<g, b, 0, st>>>(F);
 }
 
 void launch_mass(const Film& F, int sms, cudaStream_t st) {
@@ -899,17 +1041,19 @@ void launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st) {
   if (n) k_fill_u32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, v, n);
 }
 
-void launch_pig_import(const Film& F, int mode, const void* src, int fmt, size_t nslots, cudaStream_t st) {
-  unsigned g = (unsigned)((nslots + 255) / 256);
-  if (mode == CF_PREC_REFERENCE) k_pig_import<__half><<<g, 256, 0, st>>>(F, src, fmt, nslots);
-  else if (mode == CF_PREC_FP32) k_pig_import<float><<<g, 256, 0, st>>>(F, src, fmt, nslots);
-  else k_pig_import<__nv_bfloat16><<<g, 256, 0, st>>>(F, src, fmt, nslots);
+void launch_pig_import(const Film& F, int mode, uint4* dst, const void* src, int fmt, cudaStream_t st) {
+  size_t qn = mode == CF_PREC_FP32 ? 4 : 2;
+  unsigned g = (unsigned)(((size_t)F.n * 4 * qn + 255) / 256);
+  if (mode == CF_PREC_REFERENCE) k_pig_import<CF_PREC_REFERENCE><<<g, 256, 0, st>>>(F, dst, src, fmt);
+  else if (mode == CF_PREC_FP32) k_pig_import<CF_PREC_FP32><<<g, 256, 0, st>>>(F, dst, src, fmt);
+  else k_pig_import<CF_PREC_BF16><<<g, 256, 0, st>>>(F, dst, src, fmt);
 }
-void launch_pig_export(const Film& F, int mode, void* dst, int fmt, size_t nslots, cudaStream_t st) {
-  unsigned g = (unsigned)((nslots + 255) / 256);
-  if (mode == CF_PREC_REFERENCE) k_pig_export<__half><<<g, 256, 0, st>>>(F, dst, fmt, nslots);
-  else if (mode == CF_PREC_FP32) k_pig_export<float><<<g, 256, 0, st>>>(F, dst, fmt, nslots);
-  else k_pig_export<__nv_bfloat16><<<g, 256, 0, st>>>(F, dst, fmt, nslots);
+void launch_pig_export(const Film& F, int mode, const uint4* srcp, void* dst, int fmt, cudaStream_t st) {
+  size_t qn = mode == CF_PREC_FP32 ? 4 : 2;
+  unsigned g = (unsigned)(((size_t)F.n * 4 * qn + 255) / 256);
+  if (mode == CF_PREC_REFERENCE) k_pig_export<CF_PREC_REFERENCE><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
+  else if (mode == CF_PREC_FP32) k_pig_export<CF_PREC_FP32><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
+  else k_pig_export<CF_PREC_BF16><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
 }
 void launch_rheo_import(const Film& F, int mode, const float2* src, float n_global, size_t n, cudaStream_t st) {
   unsigned g = (unsigned)((n + 255) / 256);
@@ -922,8 +1066,10 @@ void launch_rheo_export(const Film& F, int mode, float2* dst, size_t n, cudaStre
   else k_rheo_export<float><<<g, 256, 0, st>>>(F, dst, n);
 }
 
-// Single dispatches for parity tests (kernel ids follow the WGSL names).
-int launch_one(const Film& F, int mode, const char* name, int all_active, cudaStream_t st) {
+// Single dispatches for parity checks, named after the WGSL entry points.
+// "strata_pass" runs strata_limit + strata_update + shade (swapping the
+// generations) and "strata_fill" one select/apply pair.
+int launch_one(Film& F, int mode, const char* name, int all_active, cudaStream_t st) {
   dim3 g = tiles_grid(F), b(16, 16);
   uint32_t nt = F.tw * F.th;
   std::string_view n(name);
@@ -931,9 +1077,9 @@ int launch_one(const Film& F, int mode, const char* name, int all_active, cudaSt
   (mode == CF_PREC_REFERENCE ? (void)K<CF_PREC_REFERENCE><<<g, b, 0, st>>>(F) : mode == CF_PREC_FP32 ? (void)K<CF_PREC_FP32><<<g, b, 0, st>>>(F) : (void)K<CF_PREC_BF16><<<g, b, 0, st>>>(F))
   if (n == "mark_tiles") k_mark_tiles<<<g, b, 0, st>>>(F);
   else if (n == "compact_tiles") { k_stats_reset<<<1, 1, 0, st>>>(F); k_compact_tiles<<<(nt + 255) / 256, 256, 0, st>>>(F, all_active); }
-  else if (n == "cure_step") CFK_T(k_cure);
+  else if (n == "cure_step") { launch_compose(F, mode, 0, st); CFK_T(k_cure); }
   else if (n == "clear_acc") k_clear_acc<<<g, b, 0, st>>>(F);
-  else if (n == "laplacian") k_laplacian<<<g, b, 0, st>>>(F);
+  else if (n == "laplacian") k_laplacian<false><<<g, b, 0, st>>>(F);
   else if (n == "plug") CFK_T(k_plug);
   else if (n == "fluxes") CFK_T(k_fluxes);
   else if (n == "limiter") k_limiter<<<g, b, 0, st>>>(F);
@@ -945,10 +1091,15 @@ int launch_one(const Film& F, int mode, const char* name, int all_active, cudaSt
   else if (n == "strata_split") CFK_T(k_strata_split);
   else if (n == "reduce_tiles") launch_reduce(F, mode, st);
   else if (n == "strata_limit") k_strata_limit<<<g, b, 0, st>>>(F);
-  else if (n == "strata_update") CFK_T(k_strata_update);
-  else if (n == "strata_copy_back") CFK_T(k_copy_back);
-  else if (n == "strata_fill") { k_fill_select<<<g, b, 0, st>>>(F); CFK_T(k_fill_apply); }
-  else if (n == "shade_full") CFK_T(k_shade);
+  else if (n == "strata_pass") {
+    k_stats_reset<<<1, 1, 0, st>>>(F);
+    k_face_flags<<<g, b, 0, st>>>(F);
+    CFK_T(k_strata_fast);
+    CFK_T(k_strata_full);
+    swap_generations(F);
+  }
+  else if (n == "strata_fill") { k_set_fill_needed<<<1, 1, 0, st>>>(F); k_fill_select<<<g, b, 0, st>>>(F); CFK_T(k_fill_apply); }
+  else if (n == "shade_full") launch_compose(F, mode, 1, st);
   else return 0;
 #undef CFK_T
   return 1;

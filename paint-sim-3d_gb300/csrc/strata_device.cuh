@@ -1,9 +1,10 @@
-// strata_device.cuh — the 4-layer material stack of strata.wgsl:1-155 and the
-// rheology/cure composition of cure.wgsl:3-117, as device functions.
+// strata_device.cuh — the 4-layer material stack of strata.wgsl:1-155, the
+// rheology composition of cure.wgsl:3-117 and the KM shade of
+// shade.wgsl:28-84, as device functions over an in-register stack.
 //
-// A Stack lives in the thread's registers/local memory: 4 thicknesses, 4 cure
-// fractions and 4 x 16 pigment slots, exactly the WGSL `Stack`.  Slot 15 (the
-// per-cell power-law index, 0 = global) is mixed like slot 14.
+// A Stack is the WGSL `Stack`: 4 thicknesses, 4 cure fractions and 4 x 16
+// pigment slots.  Slot 15 (the per-cell power-law index, 0 = global) is mixed
+// like slot 14.
 #pragma once
 
 #include "film_device.cuh"
@@ -17,21 +18,21 @@ struct Stack {
 };
 
 template <int MODE>
-__device__ __forceinline__ void stack_load(const Film& F, const void* pig, uint32_t c, Stack& s) {
-  float4 t = F.sh[c], u = F.scu[c];
+__device__ __forceinline__ void stack_load(const Film& F, const float4* sh, const float4* scu, const uint4* pig,
+                                           uint32_t c, Stack& s) {
+  float4 t = sh[c], u = scu[c];
   s.th[0] = t.x; s.th[1] = t.y; s.th[2] = t.z; s.th[3] = t.w;
   s.cu[0] = u.x; s.cu[1] = u.y; s.cu[2] = u.z; s.cu[3] = u.w;
-  using Pig = typename Prec<MODE>::Pig;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) load_pig16<Pig>((const Pig*)pig + (size_t)c * 64 + 16 * k, s.pg[k]);
+  for (int k = 0; k < 4; ++k) PigIO<MODE>::load(F, pig, c, k, s.pg[k]);
 }
 template <int MODE>
-__device__ __forceinline__ void stack_store(float4* th, float4* cu, void* pig, uint32_t c, const Stack& s) {
-  th[c] = make_float4(s.th[0], s.th[1], s.th[2], s.th[3]);
-  cu[c] = make_float4(s.cu[0], s.cu[1], s.cu[2], s.cu[3]);
-  using Pig = typename Prec<MODE>::Pig;
+__device__ __forceinline__ void stack_store(const Film& F, float4* sh, float4* scu, uint4* pig, uint32_t c,
+                                            const Stack& s) {
+  sh[c] = make_float4(s.th[0], s.th[1], s.th[2], s.th[3]);
+  scu[c] = make_float4(s.cu[0], s.cu[1], s.cu[2], s.cu[3]);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) store_pig16<Pig>((Pig*)pig + (size_t)c * 64 + 16 * k, s.pg[k]);
+  for (int k = 0; k < 4; ++k) PigIO<MODE>::store(F, pig, c, k, s.pg[k]);
 }
 
 __device__ __forceinline__ float pig_dist(const float* a, const float* b) {  // strata.wgsl:37-43
@@ -123,7 +124,7 @@ __device__ inline void stack_push_top(Stack& s, float vol, const float* pg, floa
 }
 // strata.wgsl:133-155
 __device__ inline void stack_add_band(Stack& s, float zlo, float zhi, float vol, const float* pg, float cv, float tiny,
-                               float close_d) {
+                                      float close_d) {
   if (vol <= 0.f) return;
   float span = fmaxf(zhi - zlo, 1e-12f);
   float z0 = 0.f, above = vol;
@@ -142,46 +143,6 @@ __device__ inline void stack_add_band(Stack& s, float zlo, float zhi, float vol,
     z0 = z1;
   }
   if (above > 1e-14f) stack_push_top(s, above, pg, cv, tiny, close_d);
-}
-
-// cure.wgsl:3-48 (equivalently packed_rheo :62-117): (mu, tau_y, n)
-__device__ inline void composition_rheo(const cf_params& P, const float* pigtab, const Stack& s, float& mu_o, float& ty_o,
-                                 float& n_o) {
-  float total = 0.f, lnmu = 0.f, tau = 0.f, thin = 0.f, wsum = 0.f, cur = 0.f, nsum = 0.f, nw = 0.f;
-  for (int k = 0; k < 4; ++k) {
-    float t = s.th[k];
-    if (t <= 0.f) continue;
-    total += t;
-    cur += t * s.cu[k];
-    float csum = 0.f, lm = 0.f, ty = 0.f;
-    for (int q = 0; q < 12; ++q) {
-      float cc = s.pg[k][q];
-      if (cc > 0.f) {
-        csum += cc;
-        lm += cc * logf(fmaxf(__ldg(pigtab + q * 40 + 32), 1e-3f));
-        ty += cc * s.pg[k][13];
-      }
-    }
-    if (s.pg[k][14] > 0.f) lm = csum * (s.pg[k][14] - 10.0f);
-    if (csum > 0.f) {
-      lnmu += t * lm / csum;
-      tau += t * ty / csum;
-      wsum += t;
-      if (s.pg[k][15] > 0.f) { nsum += t * s.pg[k][15]; nw += t; }
-    }
-    thin += t * s.pg[k][12];
-  }
-  if (total <= 0.f) { mu_o = 1.f; ty_o = 0.f; n_o = P.phys[2]; return; }
-  float mu = logf(P.misc[2]);
-  float ty = 0.f;
-  if (wsum > 0.f) { mu = lnmu / wsum; ty = tau / wsum; }
-  float tf = fminf(fmaxf(thin / total, 0.f), 0.95f);
-  float cb = cur / total;
-  mu += 3.0f * logf(1.0f - tf) + P.cure[2] * cb * cb;
-  ty = ty * powf(1.0f - tf, 4.0f) + P.cure[1] * cb * cb;
-  mu_o = expf(mu);
-  ty_o = ty;
-  n_o = nw > 0.f ? nsum / nw : P.phys[2];
 }
 
 // km.wgsl:17-33 for all bands at once: K,S of one stratum's pigment mix.
@@ -209,6 +170,158 @@ __device__ __forceinline__ void layer_ks_band(const float* pg, const float w[12]
   }
   k = k * scale;
   s = s * scale;
+}
+
+// Per-cell accumulation over the final strata, bottom to top, of
+//  - the pigment part of the rheology composition (cure.wgsl:3-48), kept as
+//    agg = (mu_base, 3 ln(1 - tf), tau_base (1 - tf)^4, n) for the next cure
+//    (rheo_from_parts adds the cure-dependent part), and
+//  - the KM shade (shade.wgsl:28-84): each stratum composited over the
+//    substrate, then the surface correction and XYZ -> linear sRGB.
+// Every path (strata pass, fill, cure commit, state upload) goes through this
+// one accumulator, so their colour and aggregates are bitwise alike.
+struct CellAcc {
+  // composition
+  float total, lnmu, tau, thin, wsum, nsum, nw;
+  // shade
+  float r[16];
+  float wet, cure_top, ssum;
+  uint32_t cnt;
+  bool bad;
+
+  __device__ __forceinline__ void begin(const uint16_t* rf) {
+    total = lnmu = tau = thin = wsum = nsum = nw = 0.f;
+    wet = cure_top = ssum = 0.f;
+    cnt = 0;
+    bad = false;
+    const uint4* p = reinterpret_cast<const uint4*>(rf);
+    uint4 a = p[0], b = p[1];
+    uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      r[2 * k] = h16_to_f(wv[k] & 0xffffu);
+      r[2 * k + 1] = h16_to_f(wv[k] >> 16);
+    }
+  }
+  // stratum k (in order 0..3) of thickness t, cure u and slots pg
+  __device__ __forceinline__ void add(int k, float t, float u, const float* pg, float hv, const float* lnmu_tab,
+                                      const float* tab, bool debug) {
+    ssum += t;
+    if (t > 0.f) {
+      total += t;
+      float csum = 0.f, lm = 0.f, ty = 0.f;
+#pragma unroll
+      for (int q = 0; q < 12; ++q) {
+        float cc = pg[q];
+        if (cc > 0.f) {
+          csum += cc;
+          lm += cc * lnmu_tab[q];
+          ty += cc * pg[13];
+        }
+      }
+      if (pg[14] > 0.f) lm = csum * (pg[14] - 10.0f);
+      if (csum > 0.f) {
+        lnmu += t * lm / csum;
+        tau += t * ty / csum;
+        wsum += t;
+        if (pg[15] > 0.f) { nsum += t * pg[15]; nw += t; }
+      }
+      thin += t * pg[12];
+      if (hv > 0.f) {
+        float w[12], sc;
+        layer_weights(pg, tab, w, sc);
+#pragma unroll 4
+        for (int b = 0; b < 16; ++b) {
+          float kk, ss, rr, tt;
+          layer_ks_band(pg, w, sc, tab, b, kk, ss);
+          km_layer(kk, ss, t, rr, tt);
+          r[b] = composite(rr, tt, r[b]);
+        }
+        wet = 1.0f - u;
+        cure_top = u;
+      }
+      cnt = k + 1;
+      if (debug) {
+        float cs = 0.f;
+#pragma unroll
+        for (int q = 0; q < 13; ++q) cs += pg[q];
+        if (!(cs > 0.f)) bad = true;
+      }
+    }
+  }
+  __device__ __forceinline__ float4 agg(const cf_params& P) const {
+    if (total <= 0.f) return make_float4(0.f, 0.f, 0.f, P.phys[2]);
+    float mu = logf(P.misc[2]);
+    float ty = 0.f;
+    if (wsum > 0.f) { mu = lnmu / wsum; ty = tau / wsum; }
+    float tf = fminf(fmaxf(thin / total, 0.f), 0.95f);
+    return make_float4(mu, 3.0f * logf(1.0f - tf), ty * powf(1.0f - tf, 4.0f), nw > 0.f ? nsum / nw : P.phys[2]);
+  }
+  __device__ __forceinline__ ushort4 color(const cf_params& P, const float* cm, float hv, float mv) const {
+    const float k1 = 0.04f;
+    float wt = hv > 0.f ? wet : 0.f;
+    float k2 = 0.4f * (1.0f - wt) + 0.6f * wt;
+    float X = 0.f, Y = 0.f, Z = 0.f;
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      float rb = (1.0f - k1) * (1.0f - k2) * r[b] / fmaxf(1.0f - k2 * r[b], 1e-3f);
+      X += rb * cm[3 * b];
+      Y += rb * cm[3 * b + 1];
+      Z += rb * cm[3 * b + 2];
+    }
+    float rgb[3] = {3.2406f * X - 1.5372f * Y - 0.4986f * Z, -0.9689f * X + 1.8758f * Y + 0.0415f * Z,
+                    0.0557f * X - 0.2040f * Y + 1.0570f * Z};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) rgb[q] = fmaxf(rgb[q], 0.f);
+    auto smooth = [](float e0, float e1, float x) {
+      float t = fminf(fmaxf((x - e0) / (e1 - e0), 0.f), 1.f);
+      return t * t * (3.0f - 2.0f * t);
+    };
+    float painted = smooth(60e-6f, 150e-6f, mv);
+    float ct = fmaxf(hv > 0.f ? cure_top : 0.f, painted * (1.0f - smooth(0.f, 50e-6f, hv)));
+    float sq = sqrtf(ct);
+    float rough = 0.06f * (1.0f - sq) + 0.35f * sq;
+    if (hv <= 0.f) rough = 0.85f * (1.0f - painted) + 0.35f * painted;
+    if (P.flags[0] == 1u && hv > 0.f) {  // shade.wgsl:65-82 invariant view
+      if (ssum <= 0.f) { rgb[0] = 0.f; rgb[1] = 0.f; rgb[2] = 1.f; }
+      else if (bad) { rgb[0] = 1.f; rgb[1] = 0.f; rgb[2] = 0.f; }
+      else if (fabsf(ssum - hv) > 0.01f * hv) { rgb[0] = 0.f; rgb[1] = 1.f; rgb[2] = 0.f; }
+      else { float v = 0.3f + 0.15f * (float)cnt; rgb[0] = v; rgb[1] = v; rgb[2] = v; }
+    }
+    return make_ushort4((unsigned short)f_to_h16(rgb[0]), (unsigned short)f_to_h16(rgb[1]),
+                        (unsigned short)f_to_h16(rgb[2]), (unsigned short)f_to_h16(rough));
+  }
+};
+
+// Completes cure.wgsl:40-47 with the cure fractions u of strata of thickness t.
+__device__ __forceinline__ void rheo_from_parts(const cf_params& P, float4 agg, const float t[4], const float u[4],
+                                                float& mu_o, float& ty_o, float& n_o) {
+  float total = 0.f, cur = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (t[k] <= 0.f) continue;
+    total += t[k];
+    cur += t[k] * u[k];
+  }
+  if (total <= 0.f) { mu_o = 1.f; ty_o = 0.f; n_o = P.phys[2]; return; }
+  float cb = cur / total;
+  float mu = agg.x + (agg.y + P.cure[2] * cb * cb);
+  ty_o = agg.z + P.cure[1] * cb * cb;
+  mu_o = expf(mu);
+  n_o = agg.w;
+}
+
+// Aggregates and colour of a whole in-register stack.
+__device__ inline void finish_stack(const cf_params& P, const float* lnmu_tab, const float* tab, const float* cm,
+                                    const uint16_t* rf, float hv, float mv, const Stack& s, float4& agg,
+                                    ushort4& col) {
+  CellAcc a;
+  a.begin(rf);
+  const bool dbg = P.flags[0] == 1u;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) a.add(k, s.th[k], s.cu[k], s.pg[k], hv, lnmu_tab, tab, dbg);
+  agg = a.agg(P);
+  col = a.color(P, cm, hv, mv);
 }
 
 }  // namespace cfk
