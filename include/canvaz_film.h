@@ -240,6 +240,32 @@ cf_status cf_sync(cf_film* film);
  * cf_create when film is NULL). */
 const char* cf_last_error(const cf_film* film);
 
+/* --- allocation-free CFL statistics -------------------------------------- */
+
+/* Largest grid cf_cfl_stats_noalloc accepts, in 64 x 64 tiles (65,536 tiles:
+ * 268M cells, e.g. 16384 x 16384).  Its scratch is one (h_max, mu_min) pair
+ * per tile, 512 KB, held by every GPU that loads the library until exit. */
+#define CF_NOALLOC_MAX_TILES 65536
+
+/* No counterpart in the reference: it is an addition for callers that must
+ * not allocate device memory when they ask for these numbers (a frame loop
+ * that did all its allocation at start-up, where a cudaMalloc could stall
+ * the device, or a host that owns a fixed memory budget).
+ *
+ * Computes, from caller-owned device planes h and mu (w x h FP32, row-major),
+ * the same h_max and mu_min as the film's tile reduction (over cells with
+ * h > 4 h_min; mu_min = 1 when no cell qualifies) and writes them to
+ * d_out[0], d_out[1] (device memory) on `stream` (NULL = legacy default).
+ * It allocates nothing: its scratch is a fixed array in the library's device
+ * image.  The first call on each device looks up that array's address with
+ * the device current; make that first call before any stream capture.
+ * Every call on a device shares the one array, so calls that overlap on the
+ * GPU (different streams or host threads, without ordering) race.
+ * Grids of more than CF_NOALLOC_MAX_TILES tiles return CF_ERR_INVALID_ARG
+ * before anything is launched. */
+cf_status cf_cfl_stats_noalloc(const float* d_h, const float* d_mu, uint32_t w, uint32_t h,
+                               float h_min, float* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -143,6 +143,7 @@ def load_library(path=None):
         "cf_get_params": ([vp, C.POINTER(Params)], i32),
         "cf_sync": ([vp], i32),
         "cf_last_error": ([vp], C.c_char_p),
+        "cf_cfl_stats_noalloc": ([vp, vp, u32, u32, f32, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
