@@ -44,6 +44,8 @@ from canvaz_film import capi, synth  # noqa: E402
 WORKLOADS = {
     # name: (generator, precision, dt_max, adaptive)
     "drips2048_tilt60_fp32": (lambda seed: synth.config(1, seed), capi.CF_PREC_FP32, 1.0 / 60.0, True),
+    # the same field at half the side (50 lines): small case for kernel captures
+    "drips1024_tilt60_fp32": (lambda seed: synth.config(1, seed, scale=2), capi.CF_PREC_FP32, 1.0 / 60.0, True),
     "blobs512_dt1e-3_fp32": (lambda seed: synth.config(0, seed), capi.CF_PREC_FP32, 1e-3, False),
     "blobs4096_dt1e-3_bf16": (lambda seed: synth.config(2, seed), capi.CF_PREC_BF16, 1e-3, False),
     "blobs4096_dt1e-3_fp32": (lambda seed: synth.config(2, seed), capi.CF_PREC_FP32, 1e-3, False),
