@@ -236,6 +236,7 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
   add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n); add((void**)&F.color, 8 * n);
   add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt); add((void**)&F.stats64, 8 * n64);
   add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, n);
+  add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
   size_t total = 0;
   for (auto& sl : slots) total += (sl.bytes + 255) & ~(size_t)255;
   cudaError_t e = cudaMalloc(&f->arena, total);
@@ -260,6 +261,7 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
     return bail(CF_ERR_OUT_OF_MEMORY);
   }
   F.w = w; F.h = h; F.tw = f->tw; F.th = f->th; F.n = (uint32_t)n;
+  F.persist_blocks = (uint32_t)std::max(f->sms, 1) * 8u;
   F.P = f->d_params; F.stats = f->d_stats;
   F.pigtab = f->d_tables; F.cmf = f->d_tables + 480;
   // Film::new: zeroed buffers, substrate refl, weave relief, rheo = (1, 0)

@@ -44,13 +44,13 @@ struct DevStats {
   uint32_t h_max_bits;   // max h over cells with h > 4 h_min (float bits, h >= 0)
   uint32_t mu_min_bits;  // min mu over the same cells (float bits, mu > 0)
   uint32_t active_tiles;
-  uint32_t fill_needed;  // wet cells left without strata by the strata pass (fill is skipped at 0)
+  uint32_t fill_count;   // entries of Film::fill_list (wet active cells the strata pass left without strata)
   double wet_sum;        // sum(h)
   double relief_sum;     // sum(m)
   unsigned long long wet_cells;
   unsigned long long nan_cells;
   float last_dt;
-  float pad;
+  uint32_t full_count;   // entries of Film::full_list (cells of the strata full path)
 };
 
 template <int MODE> struct Prec;
@@ -66,12 +66,15 @@ template <> __device__ __forceinline__ float from_f<float>(float v) { return v; 
 template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
-// All device planes of one film.  The strata come in two generations (cur /
-// nxt) that swap every frame, so the strata pass never copies back.  Pigment
-// slots are stored chunk-major: 16-byte chunk q of stratum k of cell c lives at
-// chunk index (k * QN + q) * n + c (QN = chunks per stratum), so a warp reads
-// 512 contiguous bytes per load.  acc_s is face-major: face f of cell c at
-// f * n + c.
+// All device planes of one film.  Strata thicknesses and cure fractions come
+// in two generations (cur / nxt) that swap every frame, so the strata pass
+// never copies them back.  The pigments have one plane: only the cells of the
+// strata full path change them, and those write their new slots to the side
+// plane pig2 first, copied back after the pass (other cells read their
+// neighbours' pigments during it).  Pigment slots are stored chunk-major:
+// 16-byte chunk q of stratum k of cell c lives at chunk index (k * QN + q) * n
+// + c (QN = chunks per stratum), so a warp reads 512 contiguous bytes per
+// load.  acc_s is face-major: face f of cell c at f * n + c.
 struct Film {
   uint32_t w, h, tw, th;  // grid and 16x16 tile counts
   uint32_t n;             // cells
@@ -99,7 +102,7 @@ struct Film {
   uint4* pig;      // pigment chunks
   float4* sh2;     // next generation
   float4* scu2;
-  uint4* pig2;
+  uint4* pig2;     // new pigments of the strata full path's cells (side plane)
   float4* agg;     // composition aggregates for the next cure (see composition_parts)
   uint16_t* refl;  // 16 half per cell
   ushort4* color;  // rgba16f
@@ -108,6 +111,9 @@ struct Film {
   float2* stats64; // per 64x64 tile (h_max, mu_min)
   int32_t* fill_src;
   uint8_t* fflags;  // bit f: strata_split wrote a nonzero acc_s face f this frame
+  uint32_t* full_list;  // cells of the strata full path (DevStats::full_count)
+  uint32_t* fill_list;  // strata fill candidates (DevStats::fill_count)
+  uint32_t persist_blocks;  // grid of the list kernels: a few blocks per SM
   const float* pigtab;  // 12 x 40
   const float* cmf;     // 16 x 3
 };

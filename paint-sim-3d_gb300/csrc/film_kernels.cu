@@ -6,10 +6,11 @@
 //   [clear_acc + laplacian], plug, fluxes, limiter, apply, nose   per substep
 //   laplacian, strata_split, reduce_tiles
 //   strata pass: strata_limit + strata_update + shade_full + the next frame's
-//                rheology aggregates, in one kernel, into the other strata
-//                generation (no copy back)
-//   strata_fill x 6                    skipped on the device when no wet cell
-//                                      was left without strata
+//                rheology aggregates: a grid kernel takes the fast path and
+//                lists the other cells, a list kernel (one cell per
+//                half-warp) takes the full path, then the listed cells'
+//                pigments are copied back
+//   strata_fill x 6                    one block over the fill candidates
 //
 // Launch geometry: one 16x16 block per 16x16 activity tile.  A tile-list
 // dispatch of the reference becomes a full-grid launch whose blocks on
@@ -25,6 +26,7 @@
 #include "film_device.cuh"
 #include "film_kernels.h"
 #include "strata_device.cuh"
+#include "strata_lane.cuh"
 
 namespace cfk {
 
@@ -519,27 +521,6 @@ __global__ void __launch_bounds__(256) k_strata_limit(Film F) {
   F.alpha_s[c] = strata_limit_at(F, P, i, j);
 }
 
-// strata.wgsl:175-188; the face volumes arrive by value (one per stratum) and
-// the source's alpha_s comes from the caller
-template <int MODE>
-__device__ __forceinline__ void inflow_from(const Film& F, const cf_params& P, Stack& s, uint32_t cn, float4 an4,
-                                            float4 f) {
-  const float4 th4 = F.sh[cn], cu4 = F.scu[cn];
-  float z0 = 0.f;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const float thn = sel4(th4, k);
-    const float z1 = z0 + thn;
-    const float v = sel4(f, k) * sel4(an4, k) * P.inv_dx;
-    if (v > 0.f && thn > 0.f) {
-      float pg[16];
-      PigIO<MODE>::load(F, F.pig, cn, k, pg);
-      stack_add_band(s, z0, z1, v, pg, sel4(cu4, k), P.misc[0], P.misc[1]);
-    }
-    z0 = z1;
-  }
-}
-
 // Face flags from acc_s as strata_split writes them (for an inspection
 // dispatch of the strata pass that does not follow a strata_split).
 __global__ void __launch_bounds__(256) k_face_flags(Film F) {
@@ -553,17 +534,21 @@ __global__ void __launch_bounds__(256) k_face_flags(Film F) {
   F.fflags[c] = (uint8_t)flags;
 }
 
-// Whether strata_update (strata.wgsl:190-274) takes its full path for this
-// active cell: any of its 8 faces carries a strata flux (the face flags of
-// strata_split), or its renormalised stack is not compact (:222-228).
-__device__ __forceinline__ bool needs_full(const Film& F, const cf_params& P, int i, int j, uint32_t c, float hc) {
+// Whether any of the 8 faces of active cell (i, j) carries a strata flux (the
+// face flags of strata_split): only then is its strata_limit alpha below 1
+// and only then does strata_update move material into or out of it.
+__device__ __forceinline__ bool flux_touched(const Film& F, int i, int j, uint32_t c) {
   if (F.fflags[c] != 0u) return true;
   if (i > 0 && cell_active(F, i - 1, j) && (F.fflags[c - 1] & 1u)) return true;
   if (j > 0 && cell_active(F, i, j - 1) && (F.fflags[c - F.w] & 2u)) return true;
   if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1) && (F.fflags[c - F.w - 1] & 4u)) return true;
   if (i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1) && (F.fflags[c + F.w - 1] & 8u)) return true;
+  return false;
+}
+// Whether the stack renormalised to h is not compact (strata.wgsl:222-228),
+// which sends a cell without strata fluxes down the full path as well.
+__device__ __forceinline__ bool not_compact(const cf_params& P, float hc, float4 t4) {
   if (hc <= 0.f) return false;
-  float4 t4 = F.sh[c];
   float th[4] = {fmaxf(t4.x, 0.f), fmaxf(t4.y, 0.f), fmaxf(t4.z, 0.f), fmaxf(t4.w, 0.f)};
   float nt[4] = {th[0], th[1], th[2], th[3]};
   float sum = th[0] + th[1] + th[2] + th[3];
@@ -580,18 +565,33 @@ __device__ __forceinline__ bool needs_full(const Film& F, const cf_params& P, in
   return false;
 }
 
+// Appends v to a device list; one atomic per warp (the threads of the warp
+// that append at this point).
+__device__ __forceinline__ void list_append(uint32_t* list, uint32_t* count, uint32_t v) {
+  const unsigned m = __activemask();
+  const int lane = (int)((threadIdx.y * blockDim.x + threadIdx.x) & 31u);
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  list[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
 __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm, float* ltab, int tid, int nthreads) {
   for (int q = tid; q < 480; q += nthreads) tab[q] = F.pigtab[q];
   if (tid < 48) cm[tid] = F.cmf[tid];
   if (tid < 12) ltab[tid] = logf(fmaxf(F.pigtab[tid * 40 + 32], 1e-3f));
 }
 
-// Strata pass, part 1 (every cell not taken by part 2): the fast path of
-// strata_update (strata.wgsl:212-237: renormalise the stack to h and carry
-// the pigments over) into the next generation, streamed stratum by stratum
-// through the shade (shade.wgsl:28-84) and the composition aggregates.
-// Inactive tiles carry their strata over unchanged and are shaded, as the
-// reference's full-grid shade does.
+// Strata pass, part 1, over every cell.  Active cells with a strata flux on a
+// face or a stack that is not compact are listed for part 2, with their
+// strata_limit alpha (strata.wgsl:157-173; 1 without fluxes).  Every other
+// cell takes the fast path of strata_update (strata.wgsl:212-237): the stack
+// renormalised to h into the next generation of thicknesses, its pigments left
+// in place (this path never changes them), then the shade (shade.wgsl:28-84)
+// and the composition aggregates.  Inactive tiles carry their strata over and
+// are shaded, as the reference's full-grid shade does.  Active wet cells left
+// without strata become strata_fill candidates.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_strata_fast(Film F) {
   __shared__ float tab[480];
@@ -606,8 +606,15 @@ __global__ void __launch_bounds__(256) k_strata_fast(Film F) {
   const cf_params& P = F.P->p;
   const bool act = (F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) != 0u;
   const float hc = F.hh[c];
-  if (act && needs_full(F, P, i, j, c, hc)) return;
   float4 t4 = F.sh[c], cu = F.scu[c];
+  if (act) {
+    const bool ft = flux_touched(F, i, j, c);
+    if (ft || not_compact(P, hc, t4)) {
+      F.alpha_s[c] = ft ? strata_limit_at(F, P, i, j) : make_float4(1.f, 1.f, 1.f, 1.f);
+      list_append(F.full_list, &F.stats->full_count, c);
+      return;
+    }
+  }
   float nt[4] = {t4.x, t4.y, t4.z, t4.w};
   if (act) {
     float th[4] = {fmaxf(t4.x, 0.f), fmaxf(t4.y, 0.f), fmaxf(t4.z, 0.f), fmaxf(t4.w, 0.f)};
@@ -625,6 +632,7 @@ __global__ void __launch_bounds__(256) k_strata_fast(Film F) {
         for (int k = 0; k < 4; ++k) nt[k] = th[k] * sc;
       }
     }
+    if (hc > 0.f && !(nt[0] + nt[1] + nt[2] + nt[3] > 0.f)) list_append(F.fill_list, &F.stats->fill_count, c);
   }
   F.sh2[c] = make_float4(nt[0], nt[1], nt[2], nt[3]);
   F.scu2[c] = cu;
@@ -633,7 +641,6 @@ __global__ void __launch_bounds__(256) k_strata_fast(Film F) {
   const bool dbg = P.flags[0] == 1u;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    PigIO<MODE>::copy(F, F.pig2, c, k, F.pig, c, k);
     if (nt[k] > 0.f) {
       float pg[16];
       PigIO<MODE>::load(F, F.pig, c, k, pg);
@@ -646,89 +653,225 @@ __global__ void __launch_bounds__(256) k_strata_fast(Film F) {
   F.color[c] = acc.color(P, cm, hc, F.m[c]);
 }
 
-// Strata pass, part 2: the cells of active tiles that needs_full selects.
-// strata_limit (strata.wgsl:157-173) of the tile and its 1-cell halo goes to
-// shared memory (only in blocks that have such a cell), then the full
-// strata_update (:238-273) builds the new stack, which is stored into the
-// next generation, shaded and composed.
+// strata.wgsl:175-188 with one cell per half-warp: the material that
+// neighbour cn sends over a face (volumes f, one per stratum; positive =
+// towards this cell) scaled by the neighbour's alpha.  The neighbour is read
+// only when some stratum flows in, and then it is active with its alpha
+// written by part 1 (a nonzero face flags both of its cells), or inactive,
+// where strata_limit leaves alpha at 1.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_strata_full(Film F) {
+__device__ __forceinline__ void lane_inflow(const Film& F, const cf_params& P, const HalfWarp& H, LaneStack& s,
+                                            int ni, int nj, float4 f) {
+  if (!(f.x > 0.f || f.y > 0.f || f.z > 0.f || f.w > 0.f)) return;
+  const uint32_t cn = idx(F, ni, nj);
+  const float4 an4 = cell_active(F, ni, nj) ? F.alpha_s[cn] : make_float4(1.f, 1.f, 1.f, 1.f);
+  const float4 th4 = F.sh[cn], cu4 = F.scu[cn];
+  float z0 = 0.f;
+#pragma unroll 1
+  for (int k = 0; k < 4; ++k) {
+    const float thn = sel4(th4, k);
+    const float z1 = z0 + thn;
+    const float v = sel4(f, k) * sel4(an4, k) * P.inv_dx;
+    if (v > 0.f && thn > 0.f) {
+      const float pin = PigLane<MODE>::load(F, F.pig, cn, k, H.q);
+      lane_add_band(H, s, z0, z1, v, pin, sel4(cu4, k), P.misc[0], P.misc[1]);
+    }
+    z0 = z1;
+  }
+}
+
+// Strata pass, part 2: the listed cells, one per half-warp, over a grid of a
+// few blocks per SM.  The full strata_update (strata.wgsl:238-273) builds the
+// new stack: own outflow, inflow from the 8 neighbours, renormalisation to h
+// and compaction.  Thicknesses go to the next generation, pigment slots to
+// the side plane (copied back by k_strata_commit), then the cell is shaded
+// and composed from the stored (rounded) slots.
+template <int MODE>
+__global__ void __launch_bounds__(256, 3) k_strata_full(Film F) {
   __shared__ float tab[480];
   __shared__ float cm[48];
   __shared__ float ltab[12];
-  __shared__ float4 s_alpha[18 * 18];
-  if ((F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) == 0u) return;
-  const int tid = threadIdx.y * 16 + threadIdx.x;
-  const cf_params& P = F.P->p;
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
-  const bool inside = i < (int)F.w && j < (int)F.h;
-  const uint32_t c = inside ? idx(F, i, j) : 0u;
-  const float hc = inside ? F.hh[c] : 0.f;
-  const bool mine = inside && needs_full(F, P, i, j, c, hc);
-  if (!__syncthreads_or(mine)) return;
-  load_tables(F, tab, cm, ltab, tid, 256);
-  for (int q = tid; q < 18 * 18; q += 256) {
-    int x = (int)blockIdx.x * 16 - 1 + q % 18, y = (int)blockIdx.y * 16 - 1 + q / 18;
-    float4 a = make_float4(1.f, 1.f, 1.f, 1.f);
-    if (in_grid(F, x, y) && cell_active(F, x, y)) a = strata_limit_at(F, P, x, y);
-    s_alpha[q] = a;
-  }
+  const uint32_t count = F.stats->full_count;
+  if (count == 0u) return;
+  load_tables(F, tab, cm, ltab, threadIdx.x, 256);
   __syncthreads();
-  if (!mine) return;
-  auto sa = [&](int di, int dj) { return s_alpha[(threadIdx.y + 1 + dj) * 18 + threadIdx.x + 1 + di]; };
-  const float4 fr4 = acc_face(F, c, 0), fu4 = acc_face(F, c, 1), fd4 = acc_face(F, c, 2), fe4 = acc_face(F, c, 3);
+  const HalfWarp H((int)(threadIdx.x & 31u));
+  const cf_params& P = F.P->p;
+  const bool dbg = P.flags[0] == 1u;
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 fl4 = z4, fdn4 = z4, fll4 = z4, flu4 = z4;
-  bool hl = false, hd = false, hll = false, hlu = false;
-  if (i > 0 && cell_active(F, i - 1, j)) { hl = true; fl4 = acc_face(F, c - 1, 0); }
-  if (j > 0 && cell_active(F, i, j - 1)) { hd = true; fdn4 = acc_face(F, c - F.w, 1); }
-  if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1)) { hll = true; fll4 = acc_face(F, c - F.w - 1, 2); }
-  if (i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1)) { hlu = true; flu4 = acc_face(F, c + F.w - 1, 3); }
-  Stack s;
-  stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
-  const float4 a4 = sa(0, 0);
+  const uint32_t stride = gridDim.x * (blockDim.x >> 4);
+  for (uint32_t e = blockIdx.x * (blockDim.x >> 4) + (threadIdx.x >> 4); e < count; e += stride) {
+    const uint32_t c = F.full_list[e];
+    const int i = (int)(c % F.w), j = (int)(c / F.w);
+    const float hc = F.hh[c];
+    const bool hl = i > 0 && cell_active(F, i - 1, j);
+    const bool hd = j > 0 && cell_active(F, i, j - 1);
+    const bool hll = i > 0 && j > 0 && cell_active(F, i - 1, j - 1);
+    const bool hlu = i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1);
+    // face nb of the 8 (towards this cell positive): the cell's own 4 faces
+    // (right, up, up-right, down-right) negated, then the 4 faces its left,
+    // lower, lower-left and upper-left neighbours own; zero where absent
+    auto face_in = [&](int nb) -> float4 {
+      switch (nb) {
+        case 0: return neg4(acc_face(F, c, 0));
+        case 1: return neg4(acc_face(F, c, 1));
+        case 2: return neg4(acc_face(F, c, 2));
+        case 3: return neg4(acc_face(F, c, 3));
+        case 4: return hl ? acc_face(F, c - 1, 0) : z4;
+        case 5: return hd ? acc_face(F, c - F.w, 1) : z4;
+        case 6: return hll ? acc_face(F, c - F.w - 1, 2) : z4;
+        default: return hlu ? acc_face(F, c + F.w - 1, 3) : z4;
+      }
+    };
+    LaneStack s;
+    {
+      const float4 t = F.sh[c], u = F.scu[c];
+      s.th[0] = t.x; s.th[1] = t.y; s.th[2] = t.z; s.th[3] = t.w;
+      s.cu[0] = u.x; s.cu[1] = u.y; s.cu[2] = u.z; s.cu[3] = u.w;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    float out = fmaxf(sel4(fr4, k), 0.f) + fmaxf(sel4(fu4, k), 0.f) + fmaxf(sel4(fd4, k), 0.f) +
-                fmaxf(sel4(fe4, k), 0.f) + fmaxf(-sel4(fl4, k), 0.f) + fmaxf(-sel4(fdn4, k), 0.f) +
-                fmaxf(-sel4(fll4, k), 0.f) + fmaxf(-sel4(flu4, k), 0.f);
-    s.th[k] = fmaxf(s.th[k] - out * sel4(a4, k) * P.inv_dx, 0.f);
+      for (int k = 0; k < 4; ++k) s.pg[k] = PigLane<MODE>::load(F, F.pig, c, k, H.q);
+    }
+    {
+      float4 out = z4;
+#pragma unroll
+      for (int nb = 0; nb < 8; ++nb) {
+        const float4 f = face_in(nb);
+        out.x += fmaxf(-f.x, 0.f);
+        out.y += fmaxf(-f.y, 0.f);
+        out.z += fmaxf(-f.z, 0.f);
+        out.w += fmaxf(-f.w, 0.f);
+      }
+      const float4 a4 = F.alpha_s[c];
+      s.th[0] = fmaxf(s.th[0] - out.x * a4.x * P.inv_dx, 0.f);
+      s.th[1] = fmaxf(s.th[1] - out.y * a4.y * P.inv_dx, 0.f);
+      s.th[2] = fmaxf(s.th[2] - out.z * a4.z * P.inv_dx, 0.f);
+      s.th[3] = fmaxf(s.th[3] - out.w * a4.w * P.inv_dx, 0.f);
+    }
+    // the 8 inflows in the reference's order; one copy of the stack code
+    // serves all of them
+#pragma unroll 1
+    for (int nb = 0; nb < 8; ++nb) {
+      int di, dj;
+      bool ok;
+      switch (nb) {
+        case 0: di = 1; dj = 0; ok = i + 1 < (int)F.w; break;
+        case 1: di = 0; dj = 1; ok = j + 1 < (int)F.h; break;
+        case 2: di = 1; dj = 1; ok = i + 1 < (int)F.w && j + 1 < (int)F.h; break;
+        case 3: di = 1; dj = -1; ok = i + 1 < (int)F.w && j > 0; break;
+        case 4: di = -1; dj = 0; ok = hl; break;
+        case 5: di = 0; dj = -1; ok = hd; break;
+        case 6: di = -1; dj = -1; ok = hll; break;
+        default: di = -1; dj = 1; ok = hlu; break;
+      }
+      if (ok) lane_inflow<MODE>(F, P, H, s, i + di, j + dj, face_in(nb));
+    }
+    const float sum = s.th[0] + s.th[1] + s.th[2] + s.th[3];
+    if (hc <= 0.f) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { s.th[k] = 0.f; s.cu[k] = 0.f; }
+    } else if (sum > 0.f) {
+      const float kk = hc / sum;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s.th[k] *= kk;
+    }
+    lane_compact(H, s, P.misc[0]);
+    if (H.q == 0) {
+      F.sh2[c] = make_float4(s.th[0], s.th[1], s.th[2], s.th[3]);
+      F.scu2[c] = make_float4(s.cu[0], s.cu[1], s.cu[2], s.cu[3]);
+      if (hc > 0.f && !(s.th[0] + s.th[1] + s.th[2] + s.th[3] > 0.f)) {
+        const uint32_t at = atomicAdd(&F.stats->fill_count, 1u);
+        F.fill_list[at] = c;
+      }
+    }
+    LaneAcc acc;
+    acc.begin(H, F.refl + (size_t)c * 16);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float pk = get4(s.pg, k);
+      PigLane<MODE>::store(F, F.pig2, c, k, H.q, pk);
+      acc.add(H, k, get4(s.th, k), get4(s.cu, k), PigLane<MODE>::round(pk), hc, ltab, tab, dbg);
+    }
+    const float4 agg = acc.agg(P);
+    const ushort4 col = acc.color(H, P, cm, hc, F.m[c]);
+    if (H.q == 0) {
+      F.agg[c] = agg;
+      F.color[c] = col;
+    }
   }
-  if (i + 1 < (int)F.w) inflow_from<MODE>(F, P, s, c + 1, sa(1, 0), neg4(fr4));
-  if (j + 1 < (int)F.h) inflow_from<MODE>(F, P, s, c + F.w, sa(0, 1), neg4(fu4));
-  if (i + 1 < (int)F.w && j + 1 < (int)F.h) inflow_from<MODE>(F, P, s, c + F.w + 1, sa(1, 1), neg4(fd4));
-  if (i + 1 < (int)F.w && j > 0) inflow_from<MODE>(F, P, s, c - F.w + 1, sa(1, -1), neg4(fe4));
-  if (hl) inflow_from<MODE>(F, P, s, c - 1, sa(-1, 0), fl4);
-  if (hd) inflow_from<MODE>(F, P, s, c - F.w, sa(0, -1), fdn4);
-  if (hll) inflow_from<MODE>(F, P, s, c - F.w - 1, sa(-1, -1), fll4);
-  if (hlu) inflow_from<MODE>(F, P, s, c + F.w - 1, sa(-1, 1), flu4);
-  float sum = s.th[0] + s.th[1] + s.th[2] + s.th[3];
-  if (hc <= 0.f) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) { s.th[k] = 0.f; s.cu[k] = 0.f; }
-  } else if (sum > 0.f) {
-    float kk = hc / sum;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) s.th[q] *= kk;
-  }
-  stack_compact(s, P.misc[0]);
-  stack_store<MODE>(F, F.sh2, F.scu2, F.pig2, c, s);
-  // the stored (rounded) slots are what the shade and later frames see
-#pragma unroll
-  for (int k = 0; k < 4; ++k) PigIO<MODE>::load(F, F.pig2, c, k, s.pg[k]);
-  if (hc > 0.f && !(s.th[0] + s.th[1] + s.th[2] + s.th[3] > 0.f)) atomicAdd(&F.stats->fill_needed, 1u);
-  float4 agg;
-  ushort4 col;
-  finish_stack(P, ltab, tab, cm, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
-  F.agg[c] = agg;
-  F.color[c] = col;
 }
 
-// strata.wgsl:288-323, Jacobi in two passes over the current generation:
-// select reads only the sums of the strata; apply writes only cells that had
-// none, whose sources always have some, so no pass reads what it writes.
+// Copies the listed cells' new pigment slots from the side plane back into
+// the pigment plane (consecutive threads take consecutive list entries).
+template <int MODE>
+__global__ void __launch_bounds__(256) k_strata_commit(Film F) {
+  constexpr uint32_t CH = 4u * PigIO<MODE>::QN;  // 16-byte chunks per cell
+  const uint32_t count = F.stats->full_count;
+  const size_t units = (size_t)count * CH;
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < units; u += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t ch = (uint32_t)(u / count), e = (uint32_t)(u % count);
+    const size_t at = (size_t)ch * F.n + F.full_list[e];
+    F.pig[at] = F.pig2[at];
+  }
+}
+
+// strata_fill (strata.wgsl:288-323) x 6 over the candidates of the strata
+// pass, in one block: select reads only strata sums, apply writes only cells
+// that had none, and a block barrier separates the two (Jacobi semantics, as
+// the reference's two dispatches per iteration).  A cell that is not a
+// candidate has h <= 0, lies in an inactive tile or has strata, and so
+// selects no source in any of the six iterations.
+template <int MODE>
+__global__ void __launch_bounds__(1024) k_fill_list(Film F) {
+  const uint32_t count = F.stats->fill_count;
+  if (count == 0u) return;
+  const cf_params& P = F.P->p;
+  __shared__ float lt[12];
+  if (threadIdx.x < 12) lt[threadIdx.x] = logf(fmaxf(F.pigtab[threadIdx.x * 40 + 32], 1e-3f));
+  __syncthreads();
+  for (int r = 0; r < 6; ++r) {
+    for (uint32_t e = threadIdx.x; e < count; e += blockDim.x) {
+      const uint32_t c = F.fill_list[e];
+      const int i = (int)(c % F.w), j = (int)(c / F.w);
+      int32_t src = -1;
+      const float4 th = F.sh[c];
+      if (!(th.x + th.y + th.z + th.w > 0.f)) {
+        uint32_t cand[4];
+        int nc = 0;
+        if (i > 0) cand[nc++] = c - 1;
+        if (j > 0) cand[nc++] = c - F.w;
+        if (i + 1 < (int)F.w) cand[nc++] = c + 1;
+        if (j + 1 < (int)F.h) cand[nc++] = c + F.w;
+        float best = 0.f;
+        for (int q = 0; q < nc; ++q) {
+          const float4 tn = F.sh[cand[q]];
+          const float ts = tn.x + tn.y + tn.z + tn.w;
+          if (ts > best) { best = ts; src = (int32_t)cand[q]; }
+        }
+      }
+      F.fill_src[e] = src;
+    }
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < count; e += blockDim.x) {
+      const int32_t src = F.fill_src[e];
+      if (src < 0) continue;
+      const uint32_t c = F.fill_list[e];
+      const float hc = F.hh[c];
+      backfill<MODE>(F, c, (uint32_t)src, hc);
+      Stack s;
+      stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
+      float4 agg;
+      ushort4 col;
+      finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
+      F.agg[c] = agg;
+      F.color[c] = col;
+    }
+    __syncthreads();
+  }
+}
+
+// strata_fill as one select + apply pair over the whole grid (inspection
+// dispatch; the frame runs k_fill_list).
 __global__ void __launch_bounds__(256) k_fill_select(Film F) {
-  if (F.stats->fill_needed == 0u) return;
   TILE_PROLOGUE
   int32_t src = -1;
   float hc = F.hh[c];
@@ -754,7 +897,6 @@ __global__ void __launch_bounds__(256) k_fill_select(Film F) {
 // ...and re-shades the filled cell and refreshes its aggregates.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_fill_apply(Film F) {
-  if (F.stats->fill_needed == 0u) return;
   TILE_PROLOGUE
   int32_t src = F.fill_src[c];
   if (src < 0) return;
@@ -820,7 +962,8 @@ __global__ void k_stats_reset(Film F) {
   F.stats->h_max_bits = 0u;
   F.stats->mu_min_bits = __float_as_uint(1e9f);
   F.stats->active_tiles = 0u;
-  F.stats->fill_needed = 0u;
+  F.stats->fill_count = 0u;
+  F.stats->full_count = 0u;
 }
 __global__ void k_mass_reset(Film F) {
   F.stats->wet_sum = 0.0;
@@ -828,7 +971,6 @@ __global__ void k_mass_reset(Film F) {
   F.stats->wet_cells = 0ull;
   F.stats->nan_cells = 0ull;
 }
-__global__ void k_set_fill_needed(Film F) { F.stats->fill_needed = 1u; }
 
 // Device-side adaptive dt (choose_substeps formulas, src/film/mod.rs:919-933,
 // one substep per frame) and the dt-dependent fields of update_params
@@ -963,7 +1105,19 @@ static inline dim3 tiles_grid(const Film& F) { return dim3(F.tw, F.th); }
 static void swap_generations(Film& F) {
   float4* t = F.sh; F.sh = F.sh2; F.sh2 = t;
   t = F.scu; F.scu = F.scu2; F.scu2 = t;
-  uint4* p = F.pig; F.pig = F.pig2; F.pig2 = p;
+}
+
+// The strata pass: part 1 over the grid (fast path, lists the rest), part 2
+// over the list, the copy back of the listed cells' pigments, then the
+// generation swap of thicknesses and cure fractions.
+template <int MODE>
+static uint32_t strata_pass_t(Film& F, cudaStream_t st) {
+  dim3 g = tiles_grid(F), b(16, 16);
+  k_strata_fast<MODE><<<g, b, 0, st>>>(F);
+  k_strata_full<MODE><<<F.persist_blocks, 256, 0, st>>>(F);
+  k_strata_commit<MODE><<<F.persist_blocks, 256, 0, st>>>(F);
+  swap_generations(F);
+  return 3;
 }
 
 // Enqueues one frame; returns the number of kernel launches.  F's strata
@@ -991,16 +1145,10 @@ static uint32_t frame_t(Film& F, uint32_t substeps, int all_active, cudaStream_t
   k_laplacian<false><<<g, b, 0, st>>>(F);
   k_strata_split<MODE><<<g, b, 0, st>>>(F);
   k_reduce_tiles<MODE><<<dim3((F.w + 63) / 64, (F.h + 63) / 64), b, 0, st>>>(F);
-  k_strata_fast<MODE><<<g, b, 0, st>>>(F);
-  k_strata_full<MODE><<<g, b, 0, st>>>(F);
-  n += 5;
-  swap_generations(F);
-  for (int r = 0; r < 6; ++r) {
-    k_fill_select<<<g, b, 0, st>>>(F);
-    k_fill_apply<MODE><<<g, b, 0, st>>>(F);
-    n += 2;
-  }
-  return n;
+  n += 3;
+  n += strata_pass_t<MODE>(F, st);
+  k_fill_list<MODE><<<1, 1024, 0, st>>>(F);
+  return n + 1;
 }
 
 uint32_t launch_frame(Film& F, int mode, uint32_t substeps, int all_active, cudaStream_t st) {
@@ -1068,7 +1216,8 @@ void launch_rheo_export(const Film& F, int mode, float2* dst, size_t n, cudaStre
 
 // Single dispatches for parity checks, named after the WGSL entry points.
 // "strata_pass" runs strata_limit + strata_update + shade (swapping the
-// generations) and "strata_fill" one select/apply pair.
+// thickness generations) and "strata_fill" one select/apply pair over the
+// whole grid.
 int launch_one(Film& F, int mode, const char* name, int all_active, cudaStream_t st) {
   dim3 g = tiles_grid(F), b(16, 16);
   uint32_t nt = F.tw * F.th;
@@ -1094,11 +1243,11 @@ int launch_one(Film& F, int mode, const char* name, int all_active, cudaStream_t
   else if (n == "strata_pass") {
     k_stats_reset<<<1, 1, 0, st>>>(F);
     k_face_flags<<<g, b, 0, st>>>(F);
-    CFK_T(k_strata_fast);
-    CFK_T(k_strata_full);
-    swap_generations(F);
+    if (mode == CF_PREC_REFERENCE) strata_pass_t<CF_PREC_REFERENCE>(F, st);
+    else if (mode == CF_PREC_FP32) strata_pass_t<CF_PREC_FP32>(F, st);
+    else strata_pass_t<CF_PREC_BF16>(F, st);
   }
-  else if (n == "strata_fill") { k_set_fill_needed<<<1, 1, 0, st>>>(F); k_fill_select<<<g, b, 0, st>>>(F); CFK_T(k_fill_apply); }
+  else if (n == "strata_fill") { k_fill_select<<<g, b, 0, st>>>(F); CFK_T(k_fill_apply); }
   else if (n == "shade_full") launch_compose(F, mode, 1, st);
   else return 0;
 #undef CFK_T
