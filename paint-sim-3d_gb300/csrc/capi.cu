@@ -147,6 +147,11 @@ static void fill_devparams(cf_film* f, DevParams& D, float dt_max) {
   D.dt_max = dt_max;
   D.implicit_steps = f->implicit_steps;
   D.frames = f->frames;
+  const cf_params& P = f->P;
+  D.hold1 = P.front[0] * (1.0f - std::exp(-0.5f * P.front[1]));
+  D.cox_theta = std::atan(P.ein[0]);
+  D.cox_span = std::fmax(P.front[0] - D.hold1, 1e-6f);
+  D.cox_adv = std::fmin(D.cox_theta + P.front2[0], 3.1f);
 }
 
 // Copies the host-packed params to the device on `st`.  The pinned staging

@@ -37,6 +37,11 @@ struct DevParams {
   float dt_max;         // adaptive step upper bound
   uint32_t implicit_steps;
   uint32_t frames;
+  // per-film constants of the front terms (settings only, never dt):
+  float hold1;          // hold_level(1) (film.wgsl:153-156)
+  float cox_theta;      // atan(tan theta) (film.wgsl:236-244)
+  float cox_span;       // max(front.x - hold_level(1), 1e-6)
+  float cox_adv;        // min(theta + front2.x, 3.1)
 };
 
 // Global reductions written by the stats kernels.
@@ -376,21 +381,19 @@ __device__ __forceinline__ float wet_threshold(const Film& F, const DevParams& D
   float ty = rtau<MODE>(F, c);
   float need = fmaxf(ty / (P.phys[0] * fmaxf(F.hh[c], 1e-4f)) - D.gxy, 0.f);
   float ycap = need / fmaxf(P.g[2], 1e-3f) * P.dx;
-  return fmaxf(hold_level(P, 1.0f), ycap);
+  return fmaxf(D.hold1, ycap);
 }
 __device__ __forceinline__ float front_dist(const Film& F, uint32_t c) {  // film.wgsl:231-234
   if (F.hh[c] <= 0.f) return 0.f;
   return nose_dist(F, c);
 }
 // film.wgsl:236-244
-__device__ __forceinline__ float cox_speed(const cf_params& P, float excess, float mu) {
+__device__ __forceinline__ float cox_speed(const DevParams& D, float excess, float mu) {
   if (excess <= 0.f) return 0.f;
-  float theta = atanf(P.ein[0]);
-  float span = fmaxf(P.front[0] - hold_level(P, 1.0f), 1e-6f);
-  float th = theta + (3.14159265f - theta) * fminf(fmaxf(excess / span, 0.f), 1.f);
-  float adv = fminf(theta + P.front2[0], 3.1f);
+  const float theta = D.cox_theta, adv = D.cox_adv;
+  float th = theta + (3.14159265f - theta) * fminf(fmaxf(excess / D.cox_span, 0.f), 1.f);
   if (th <= adv) return 0.f;
-  return P.phys[1] * (th * th * th - adv * adv * adv) / (132.0f * fmaxf(mu, 1e-4f));
+  return D.p.phys[1] * (th * th * th - adv * adv * adv) / (132.0f * fmaxf(mu, 1e-4f));
 }
 // film.wgsl:246-265
 __device__ inline float cell_excess(const Film& F, const cf_params& P, uint32_t c) {
@@ -416,7 +419,8 @@ __device__ inline float cell_excess(const Film& F, const cf_params& P, uint32_t 
 }
 // film.wgsl:267-295: (speed term, direction sign)
 template <int MODE>
-__device__ float2 rim_translation(const Film& F, const cf_params& P, uint32_t ca, uint32_t cb, float hf, float2 fd) {
+__device__ float2 rim_translation(const Film& F, const DevParams& D, uint32_t ca, uint32_t cb, float hf, float2 fd) {
+  const cf_params& P = D.p;
   if (((uint32_t)P.front2[3] & 1u) != 0u) return make_float2(0.f, 0.f);
   float da = front_dist(F, ca), db = front_dist(F, cb);
   if (fmaxf(da, db) > 3.0f / P.front[1]) return make_float2(0.f, 0.f);
@@ -439,10 +443,10 @@ __device__ float2 rim_translation(const Film& F, const cf_params& P, uint32_t ca
   if (F.hh[src] <= 0.f) return make_float2(0.f, 0.f);
   float e = cell_excess(F, P, src);
   if (e <= 0.f) return make_float2(0.f, 0.f);
-  float e_out = -hold_level(P, 1.0f);
+  float e_out = -D.hold1;
   if (F.hh[dst] > 0.f) e_out = cell_excess(F, P, dst);
   float room = fminf(fmaxf(1.0f - fmaxf(e_out, 0.f) / e, 0.f), 1.f);
-  float u = cox_speed(P, e, rmu<MODE>(F, src));
+  float u = cox_speed(D, e, rmu<MODE>(F, src));
   float t = P.front2[0];
   float mixv = 1.0f * (1.0f - t) + fabsf(s) * t;
   return make_float2(u * hf * room * mixv, sgnf(s));
@@ -516,7 +520,7 @@ __device__ FaceOut face(const Film& F, const DevParams& D, uint32_t ca, uint32_t
   if (meff <= 0.f && mtilt <= 0.f) return out;
   float fcap2 = powf(thin, P.front3[3]);
   float qn = mtilt * gtilt.x + fminf(meff, P.misc[3]) * ghyd.x + fminf(meff, P.phys[3]) * (gcap.x * fcap2);
-  float2 tr = rim_translation<MODE>(F, P, ca, cb, hf, fd);
+  float2 tr = rim_translation<MODE>(F, D, ca, cb, hf, fd);
   const float vcap = 2.f;
   if (wetting) {
     uint32_t wet = ha > 0.f ? ca : cb;

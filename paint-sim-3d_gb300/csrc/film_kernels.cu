@@ -265,8 +265,10 @@ __global__ void __launch_bounds__(256) k_plug(Film F) {
 }
 
 // film.wgsl:448-455
+// Three blocks per SM: the face code needs no more than 64 registers, and
+// the occupancy hides its dependent loads.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_fluxes(Film F) {
+__global__ void __launch_bounds__(256, 3) k_fluxes(Film F) {
   TILE_PROLOGUE
   float q[4];
 #pragma unroll 1
@@ -428,7 +430,7 @@ __device__ __forceinline__ float4 band_split(const Film& F, uint32_t cu, float h
 
 // film.wgsl:475-514 (acc_s face-major)
 template <int MODE>
-__global__ void __launch_bounds__(256) k_strata_split(Film F) {
+__global__ void __launch_bounds__(256, 3) k_strata_split(Film F) {
   TILE_PROLOGUE
   float4 a4 = F.acc[c];
   float a[4] = {a4.x, a4.y, a4.z, a4.w};
