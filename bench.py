@@ -59,13 +59,23 @@ ALG_BYTES_PER_CELL = {capi.CF_PREC_FP32: 660, capi.CF_PREC_REFERENCE: 404, capi.
 PREC_NAME = {capi.CF_PREC_FP32: "f32", capi.CF_PREC_REFERENCE: "f32+f16pig", capi.CF_PREC_BF16: "f32+bf16pig"}
 
 
+# Workloads with their own arm (not a single canvas): config 3, 64 uneven
+# canvases stepped as one batch against 64 sequential single-film launches,
+# and config 4, the Poisson-served stream.
+BATCH_WORKLOAD = "batch64_dt1e-3_fp32"
+SERVE_WORKLOAD = "serve_poisson20_fp32bf16"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD])
+    ap.add_argument("--serve-seconds", type=float, default=20.0, help="arrival window of the served workload")
+    ap.add_argument("--serve-steps-scale", type=float, default=0.01, help="scales the served 100-3000 step range")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
@@ -186,10 +196,11 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    gen, prec, dt_max, adaptive = WORKLOADS[args.workload]
+    workload = args.workload if args.workload in WORKLOADS else "blobs512_dt1e-3_fp32"  # batch / served: same physics
+    gen, prec, dt_max, adaptive = WORKLOADS[workload]
     cv = gen(0)
     per_step_budget = 150.0 / max(args.steps + args.warmup, 1)
-    cb = cpu_baseline(cv, args.workload, per_step_budget * (args.steps + args.warmup), steps_hint=args.steps + args.warmup)
+    cb = cpu_baseline(cv, workload, per_step_budget * (args.steps + args.warmup), steps_hint=args.steps + args.warmup)
     line = {"impl": "reference", "metric": "Gcell-updates/s", "value": cb["value"], "unit": "Gcell-updates/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": PREC_NAME[prec], "data": "synthetic",
@@ -337,14 +348,144 @@ def gpu_arm(args):
 
 
 def film_bytes(cells, prec):
-    pig = 4 if prec == capi.CF_PREC_FP32 else 2
-    return cells * (4 * 13 + 8 * 2 + 16 * 8 + 64 + 2 * 64 * pig + 32 + 8)
+    side = int(round(cells ** 0.5))
+    return capi.film_bytes(side, max(cells // max(side, 1), 1), prec)
+
+
+def batch64_canvases(count=64, seed=0):
+    """64 canvases: side log-uniform 256-1536 rounded to 16, own seed, blob
+    count uniform 10-200, rheology and pigments as the 512^2 blob field."""
+    import math
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for k in range(count):
+        side = int(round(math.exp(rng.uniform(math.log(256), math.log(1536))) / 16.0)) * 16
+        yield synth.blob_canvas(side, side, 1000 + k, n_blobs=int(rng.integers(10, 201)))
+
+
+def batch_arm(args):
+    """Config 3: the batch (one launch per dispatch over all canvases' tiles,
+    graph replay, autotuned) against the same canvases stepped one after the
+    other with single-film launches, fixed dt 1e-3 s, one substep."""
+    import torch
+    from canvaz_film.film import Batch, Film
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    films, cells, sides = [], 0, []
+    for cv in batch64_canvases(seed=rank):
+        f = Film(settings_for(cv), cv.w, cv.h, capi.CF_PREC_FP32)
+        f.set_tables(cv.pigtab, cv.cmf)
+        f.write_state(cv.planes)
+        f.update_params(1e-3, 1)
+        films.append(f)
+        cells += cv.w * cv.h
+        sides.append(cv.w)
+    b = Batch()
+    for f in films:
+        b.add(f)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    tuning, tune_ms = b.autotune(frames_per_trial=4, stream=sh)
+    b.step(max(args.warmup, 3), 1, 0.0, sh)
+    torch.cuda.synchronize()
+    l0 = b.info()["launches"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        b.step(args.steps, 1, 0.0, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    tb = e0.elapsed_time(e1) / 1e3
+    launches = b.info()["launches"] - l0
+    b.close()
+    # the same films, one after the other per step, single-film launches
+    seq_steps = max(min(args.steps // 4, 25), 3)
+    for f in films:
+        f.encode_frame(1, sh)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(seq_steps):
+        for f in films:
+            f.encode_frame(1, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ts = e0.elapsed_time(e1) / 1e3
+    value = cells * args.steps / tb / 1e9
+    seq = cells * seq_steps / ts / 1e9
+    peak, peak_kind = peaks()
+    achieved = ALG_BYTES_PER_CELL[capi.CF_PREC_FP32] * cells * args.steps / tb / 1e9
+    clocks = clk.summary()
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tb / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian blob fields; no public dataset)",
+            "config": {"workload": BATCH_WORKLOAD, "canvases": len(films), "cells": cells,
+                       "side_min": min(sides), "side_max": max(sides), "dt": 1e-3, "substeps": 1,
+                       "all_tiles_active": True, "tuning": tuning, "autotune_ms_per_frame": tune_ms,
+                       "l2": "working set %.1f GB > L2 (129 MB): no flush needed"
+                             % (sum(capi.film_bytes(x, x, capi.CF_PREC_FP32) for x in sides) / 1e9)},
+            "sequential": {"value": seq, "unit": "Gcell-updates/s", "steps": seq_steps,
+                           "form": "64 films one after another per step, single-film launches"},
+            "speedup_vs_sequential": value / seq,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "alg_bytes_per_cell": ALG_BYTES_PER_CELL[capi.CF_PREC_FP32],
+                         "scope": "whole batched step", "traffic": None},
+            "gpu_launches": int(launches), "clocks": clocks,
+        }), flush=True)
+    for f in films:
+        f.close()
+
+
+def serve_arm(args):
+    """Config 4: Poisson arrivals at 20/s, side log-spaced 256-2048, steps
+    uniform 100-3000 (scaled), FP32 / BF16 pigments 50/50, 150 GB budget."""
+    from canvaz_film import serve
+    rank, world, local = dist_env()
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    pool = serve.TemplatePool([256, 368, 528, 768, 1104, 1584, 2048], seed=rank)
+    jobs = serve.poisson_jobs(args.serve_seconds, 20.0, pool, steps_scale=args.serve_steps_scale, seed=1 + rank)
+    for s_ in pool.sides:  # templates resident before the clock starts
+        for p_ in (capi.CF_PREC_FP32, capi.CF_PREC_BF16):
+            pool.film(pool.sides.index(s_), p_)
+    srv = serve.Server(pool, 150e9)
+    with Clocks(local) as clk:
+        rep = srv.run(jobs)
+    srv.close()
+    seq = serve.plain_sequential(jobs[:24], pool)
+    pool.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": "served Gcell-updates/s", "value": rep["gcell_updates_per_s"], "unit": "Gcell-updates/s",
+            "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f32pig|f32+bf16pig", "data": "synthetic (seeded Gaussian blob fields)",
+            "config": {"workload": SERVE_WORKLOAD, "arrival_rate_per_s": 20.0, "window_s": args.serve_seconds,
+                       "steps_range": [max(1, round(100 * args.serve_steps_scale)), round(3000 * args.serve_steps_scale)],
+                       "sides": pool.sides, "budget_bytes": 150e9, "dt": 1e-3},
+            "step_ms_p50": rep["step_ms_p50"], "step_ms_p99": rep["step_ms_p99"],
+            "queue_wait_s_p50": rep["queue_wait_s_p50"], "queue_wait_s_p99": rep["queue_wait_s_p99"],
+            "jobs": {"arrived": rep["jobs_arrived"], "done": rep["jobs_done"], "peak_resident": rep["peak_resident_jobs"]},
+            "peak_bytes": rep["peak_bytes"], "admission_s": rep["admission_s"], "wall_s": rep["wall_s"],
+            "plain_sequential": {"value": seq["gcell_updates_per_s"], "unit": "Gcell-updates/s", "jobs": 24},
+            "speedup_vs_sequential": rep["gcell_updates_per_s"] / seq["gcell_updates_per_s"],
+            "clocks": clk.summary(),
+        }), flush=True)
 
 
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == BATCH_WORKLOAD:
+        batch_arm(args)
+    elif args.workload == SERVE_WORKLOAD:
+        serve_arm(args)
     else:
         gpu_arm(args)
 

@@ -230,6 +230,14 @@ cf_status cf_read_color(cf_film* film, uint16_t* rgba16f_host);
 /* Statistics of the last frame; synchronous. */
 cf_status cf_get_stats(cf_film* film, cf_stats* out);
 
+/* write_state(read_state(src)) into dst without a host round trip
+ * (Film::read_state / write_state, src/film/mod.rs:1281-1320): copies src's
+ * whole device state (every plane with both strata generations, tables,
+ * params, stats) into dst on `stream`, so dst steps exactly as src would.
+ * dst and src have the same size, precision and device.  A serving loop
+ * admits a job by cloning a resident template canvas. */
+cf_status cf_clone_state(cf_film* dst, const cf_film* src, void* stream);
+
 /* Params of the last update (for parity checks of update_params). */
 cf_status cf_get_params(cf_film* film, cf_params* out);
 
@@ -239,6 +247,54 @@ cf_status cf_sync(cf_film* film);
 /* Human-readable text of the last error on this film (or of the last failed
  * cf_create when film is NULL). */
 const char* cf_last_error(const cf_film* film);
+
+/* Device bytes a film of w x h cells in `precision` holds (its arena, params,
+ * stats, tables and tile table): what an admission policy budgets.  Pure host
+ * function. */
+cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* bytes);
+
+/* --- batches: many films stepped together -------------------------------- */
+
+/* A batch steps many films (canvases of any size) with one kernel launch per
+ * dispatch of encode_frame: each launch covers a table of every film's 16x16
+ * tiles (films of different precision modes form separate launches).  It is
+ * the reference's per-frame loop over films (App::encode_sim,
+ * src/main.rs:1875-1909) for many canvases at once; each film's result is the
+ * same as stepping it alone.  Films join and leave between steps; a film
+ * belongs to at most one batch, and cf_destroy takes it out of its batch. */
+typedef struct cf_batch cf_batch;
+
+typedef struct cf_batch_tuning {
+    uint32_t list_blocks_per_sm;  /* grid of the strata list kernels, blocks per SM (default 8) */
+    uint32_t use_graph;           /* 1: frames replay a captured CUDA graph (default 1)       */
+    uint32_t frames_per_graph;    /* frames captured in one graph launch (default 1)          */
+    uint32_t reserved;
+} cf_batch_tuning;
+
+cf_status cf_batch_create(cf_batch** out);
+cf_status cf_batch_destroy(cf_batch* batch);
+cf_status cf_batch_add(cf_batch* batch, cf_film* film);
+cf_status cf_batch_remove(cf_batch* batch, cf_film* film);
+cf_status cf_batch_info(cf_batch* batch, uint32_t* films, uint64_t* cells, uint64_t* launches);
+cf_status cf_batch_set_tuning(cf_batch* batch, const cf_batch_tuning* tuning);
+cf_status cf_batch_get_tuning(cf_batch* batch, cf_batch_tuning* tuning);
+
+/* `frames` frames of every film, on `stream`.  dt_max > 0: adaptive frames
+ * (each film's dt chosen on the device, one substep, as cf_step_adaptive);
+ * dt_max == 0: each film's params of its last cf_update_params, with
+ * `substeps` substeps (as cf_encode_frame). */
+cf_status cf_batch_step(cf_batch* batch, uint32_t frames, uint32_t substeps, float dt_max, void* stream);
+
+/* Project autotuner: times candidate tunings (list-kernel grid, graph or
+ * direct launches, frames per graph) on this batch, `frames_per_trial` frames
+ * each after a warm-up, keeps the fastest and reports it with its time per
+ * frame.  It steps the films (about 8 x (frames_per_trial + 2) frames):
+ * callers that need the earlier state write it back afterwards. */
+cf_status cf_batch_autotune(cf_batch* batch, uint32_t frames_per_trial, uint32_t substeps, float dt_max,
+                            void* stream, cf_batch_tuning* best, float* best_ms_per_frame);
+
+/* Human-readable text of the batch's last error. */
+const char* cf_batch_last_error(const cf_batch* batch);
 
 /* --- allocation-free CFL statistics -------------------------------------- */
 

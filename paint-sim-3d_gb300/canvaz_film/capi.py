@@ -94,6 +94,12 @@ class StateView(C.Structure):
     ]
 
 
+class BatchTuning(C.Structure):
+    """cf_batch_tuning."""
+    _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("h_max", C.c_float), ("mu_min", C.c_float), ("active_tiles", C.c_uint32),
@@ -144,6 +150,18 @@ def load_library(path=None):
         "cf_sync": ([vp], i32),
         "cf_last_error": ([vp], C.c_char_p),
         "cf_cfl_stats_noalloc": ([vp, vp, u32, u32, f32, vp, vp], i32),
+        "cf_film_bytes": ([u32, u32, i32, C.POINTER(C.c_uint64)], i32),
+        "cf_clone_state": ([vp, vp, vp], i32),
+        "cf_batch_create": ([C.POINTER(vp)], i32),
+        "cf_batch_destroy": ([vp], i32),
+        "cf_batch_add": ([vp, vp], i32),
+        "cf_batch_remove": ([vp, vp], i32),
+        "cf_batch_info": ([vp, C.POINTER(u32), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
+        "cf_batch_set_tuning": ([vp, C.POINTER(BatchTuning)], i32),
+        "cf_batch_get_tuning": ([vp, C.POINTER(BatchTuning)], i32),
+        "cf_batch_step": ([vp, u32, u32, f32, vp], i32),
+        "cf_batch_autotune": ([vp, u32, u32, f32, vp, C.POINTER(BatchTuning), C.POINTER(f32)], i32),
+        "cf_batch_last_error": ([vp], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -161,3 +179,12 @@ def header_symbols(header=None):
     txt = h.read_text()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(cf\w+)\s*\(", txt)))
+
+
+def film_bytes(w, h, precision):
+    """cf_film_bytes: device bytes of a w x h film (admission budgeting)."""
+    out = C.c_uint64()
+    st = load_library().cf_film_bytes(w, h, precision, C.byref(out))
+    if st != CF_OK:
+        raise FilmError(st, "cf_film_bytes")
+    return out.value

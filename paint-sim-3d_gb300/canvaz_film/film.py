@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .capi import FilmError, Params, Settings, StateView, Stats
+from .capi import BatchTuning, FilmError, Params, Settings, StateView, Stats
 
 _f32p = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
 
@@ -148,6 +148,11 @@ class Film:
         out["sub_refl"] = out["sub_refl"].astype(np.float32)
         return out
 
+    def clone_from(self, src, stream=None):
+        """cf_clone_state: src's whole device state into this film (same size
+        and precision), stream-ordered, no host round trip."""
+        self._check(self.L.cf_clone_state(self.p, src.p, stream), "cf_clone_state")
+
     def update_params(self, frame_dt, substeps):
         self._check(self.L.cf_update_params(self.p, frame_dt, substeps), "cf_update_params")
 
@@ -219,3 +224,69 @@ class Film:
 
     def run(self, kernel, stream=None):
         self._check(self.L.cf_debug_run(self.p, kernel.encode(), stream), kernel)
+
+
+class Batch:
+    """Many films stepped together (cf_batch_*): one launch per dispatch over
+    every film's tiles, optionally replayed from captured CUDA graphs.  Each
+    film's result equals stepping it alone with Film.encode_frame /
+    Film.step_adaptive."""
+
+    def __init__(self):
+        self.L = _lib()
+        self.p = C.c_void_p()
+        self._check(self.L.cf_batch_create(C.byref(self.p)), "cf_batch_create")
+        self.films = []
+
+    def _check(self, st, what):
+        if st != capi.CF_OK:
+            msg = self.L.cf_batch_last_error(self.p).decode() if self.p else ""
+            raise FilmError(st, "%s: %s" % (what, msg))
+
+    def add(self, film):
+        self._check(self.L.cf_batch_add(self.p, film.p), "cf_batch_add")
+        self.films.append(film)
+
+    def remove(self, film):
+        self._check(self.L.cf_batch_remove(self.p, film.p), "cf_batch_remove")
+        self.films.remove(film)
+
+    def step(self, frames=1, substeps=1, dt_max=0.0, stream=None):
+        """dt_max > 0: adaptive frames; else each film's cf_update_params
+        with `substeps` substeps."""
+        self._check(self.L.cf_batch_step(self.p, frames, substeps, dt_max, stream), "cf_batch_step")
+
+    def info(self):
+        nf, cells, launches = C.c_uint32(), C.c_uint64(), C.c_uint64()
+        self._check(self.L.cf_batch_info(self.p, C.byref(nf), C.byref(cells), C.byref(launches)), "cf_batch_info")
+        return {"films": nf.value, "cells": cells.value, "launches": launches.value}
+
+    @property
+    def tuning(self):
+        t = BatchTuning()
+        self._check(self.L.cf_batch_get_tuning(self.p, C.byref(t)), "cf_batch_get_tuning")
+        return {k: getattr(t, k) for k, _ in BatchTuning._fields_ if k != "reserved"}
+
+    @tuning.setter
+    def tuning(self, d):
+        t = BatchTuning(**{**self.tuning, **d})
+        self._check(self.L.cf_batch_set_tuning(self.p, C.byref(t)), "cf_batch_set_tuning")
+
+    def autotune(self, frames_per_trial=4, substeps=1, dt_max=0.0, stream=None):
+        """The project autotuner; steps the films.  Returns (tuning, ms per frame)."""
+        t, ms = BatchTuning(), C.c_float()
+        self._check(self.L.cf_batch_autotune(self.p, frames_per_trial, substeps, dt_max, stream, C.byref(t),
+                                             C.byref(ms)), "cf_batch_autotune")
+        return {k: getattr(t, k) for k, _ in BatchTuning._fields_ if k != "reserved"}, ms.value
+
+    def close(self):
+        if self.p:
+            self.L.cf_batch_destroy(self.p)
+            self.p = C.c_void_p()
+            self.films = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -15,49 +15,10 @@
 #include <vector>
 
 #include "../../include/canvaz_film.h"
+#include "film_handle.h"
 #include "film_kernels.h"
 
-using cfk::DevParams;
-using cfk::DevStats;
-
-struct cf_film {
-  cf_settings S;
-  uint32_t w = 0, h = 0, tw = 0, th = 0;
-  int prec = 0;
-  size_t n = 0;
-  cfk::Film F{};
-  void* arena = nullptr;
-  size_t arena_bytes = 0;
-  DevParams* d_params = nullptr;
-  DevStats* d_stats = nullptr;
-  DevParams* h_params = nullptr;  // pinned staging of the host-packed params
-  cudaEvent_t params_ev = nullptr;  // recorded after the last staging copy
-  float* d_tables = nullptr;
-  cf_params P{};
-  uint32_t implicit_steps = 0;
-  bool params_dirty = true;
-  float h_max_stat = 0.f, mu_min_stat = 1.f, h_max_pending = 0.f;
-  uint32_t frames = 0;
-  uint64_t launches = 0;  // kernels enqueued by this film
-  int device = 0, sms = 0;
-  std::string err;
-};
-
 static std::string g_create_err;
-
-#define CUDA_TRY(film, expr)                                                           \
-  do {                                                                                 \
-    cudaError_t e_ = (expr);                                                           \
-    if (e_ != cudaSuccess) {                                                           \
-      (film)->err = std::string(#expr) + ": " + cudaGetErrorString(e_);                \
-      return e_ == cudaErrorMemoryAllocation ? CF_ERR_OUT_OF_MEMORY : CF_ERR_CUDA;     \
-    }                                                                                  \
-  } while (0)
-
-static cf_status fail(cf_film* f, cf_status s, const char* msg) {
-  if (f) f->err = msg;
-  return s;
-}
 
 static float to_rad(float d) { return d * (3.14159265358979323846f / 180.0f); }
 
@@ -156,7 +117,7 @@ static void fill_devparams(cf_film* f, DevParams& D, float dt_max) {
 
 // Copies the host-packed params to the device on `st`.  The pinned staging
 // buffer is rewritten only after the previous copy out of it has executed.
-static cf_status upload_params(cf_film* f, cudaStream_t st, float dt_max = 0.f) {
+cf_status upload_params(cf_film* f, cudaStream_t st, float dt_max) {
   if (!f->params_dirty) return CF_OK;
   CUDA_TRY(f, cudaEventSynchronize(f->params_ev));
   fill_devparams(f, *f->h_params, dt_max);
@@ -202,6 +163,40 @@ cf_status cf_pack_params(const cf_settings* s, uint32_t w, uint32_t h, float fra
   return CF_OK;
 }
 
+}  // extern "C"
+
+// The device planes of a film (n cells, nt tiles) in arena order; add(p, bytes)
+// receives each plane's pointer slot and size.
+template <class Add>
+static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, Add add) {
+  const size_t pig_b = precision == CF_PREC_FP32 ? 4 : 2, rh_b = precision == CF_PREC_BF16 ? 2 : 4;
+  add((void**)&F.hh, 4 * n); add((void**)&F.m, 4 * n); add(&F.mu, rh_b * n); add(&F.tau, rh_b * n);
+  add(&F.nn, rh_b * n); add((void**)&F.delta, 4 * n); add((void**)&F.delta_old, 4 * n);
+  add((void**)&F.lay, 4 * n); add((void**)&F.pres, 8 * n); add((void**)&F.fnorm, 8 * n);
+  add((void**)&F.flux, 16 * n); add((void**)&F.acc, 16 * n); add((void**)&F.acc_s, 64 * n);
+  add((void**)&F.alpha_s, 16 * n); add((void**)&F.alpha, 4 * n); add((void**)&F.tmp, 4 * n);
+  add((void**)&F.h_frame, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
+  add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
+  add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n);
+  add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
+  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, n);
+  add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
+}
+
+extern "C" {
+
+cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* bytes) {
+  if (!bytes || w == 0 || h == 0 || w > 65536 || h > 65536 || precision < 0 || precision > 2)
+    return CF_ERR_INVALID_ARG;
+  const size_t n = (size_t)w * h, nt = (size_t)((w + 15) / 16) * ((h + 15) / 16);
+  cfk::Film F{};
+  size_t total = 0;
+  carve_planes(F, n, nt, precision, [&](void**, size_t b) { total += (b + 255) & ~(size_t)255; });
+  total += sizeof(DevParams) + sizeof(DevStats) + sizeof(float) * 528 + 2 * sizeof(cfk::Film) + sizeof(uint2) * nt;
+  *bytes = total;
+  return CF_OK;
+}
+
 cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precision, cf_film** out) {
   if (!s || !out || w == 0 || h == 0 || w > 65536 || h > 65536 || precision < 0 || precision > 2) {
     g_create_err = "cf_create: invalid argument";
@@ -224,24 +219,12 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
   };
   if (cudaGetDevice(&f->device) != cudaSuccess) { f->err = "no CUDA device"; return bail(CF_ERR_CUDA); }
   cudaDeviceGetAttribute(&f->sms, cudaDevAttrMultiProcessorCount, f->device);
-  size_t n = f->n, nt = (size_t)f->tw * f->th, n64 = (size_t)((w + 63) / 64) * ((h + 63) / 64);
-  size_t pig_b = precision == CF_PREC_FP32 ? 4 : 2, rh_b = precision == CF_PREC_BF16 ? 2 : 4;
+  size_t n = f->n, nt = (size_t)f->tw * f->th;
   // carve the arena (256-byte aligned planes)
   struct Slot { void** p; size_t bytes; };
   std::vector<Slot> slots;
   cfk::Film& F = f->F;
-  auto add = [&](void** p, size_t b) { slots.push_back({p, b}); };
-  add((void**)&F.hh, 4 * n); add((void**)&F.m, 4 * n); add(&F.mu, rh_b * n); add(&F.tau, rh_b * n);
-  add(&F.nn, rh_b * n); add((void**)&F.delta, 4 * n); add((void**)&F.delta_old, 4 * n);
-  add((void**)&F.lay, 4 * n); add((void**)&F.pres, 8 * n); add((void**)&F.fnorm, 8 * n);
-  add((void**)&F.flux, 16 * n); add((void**)&F.acc, 16 * n); add((void**)&F.acc_s, 64 * n);
-  add((void**)&F.alpha_s, 16 * n); add((void**)&F.alpha, 4 * n); add((void**)&F.tmp, 4 * n);
-  add((void**)&F.h_frame, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
-  add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
-  add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n); add((void**)&F.color, 8 * n);
-  add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt); add((void**)&F.stats64, 8 * n64);
-  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, n);
-  add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
+  carve_planes(F, n, nt, precision, [&](void** p, size_t b) { slots.push_back({p, b}); });
   size_t total = 0;
   for (auto& sl : slots) total += (sl.bytes + 255) & ~(size_t)255;
   cudaError_t e = cudaMalloc(&f->arena, total);
@@ -267,8 +250,24 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
   }
   F.w = w; F.h = h; F.tw = f->tw; F.th = f->th; F.n = (uint32_t)n;
   F.persist_blocks = (uint32_t)std::max(f->sms, 1) * 8u;
+  F.all_active = s->all_active ? 1u : 0u;
   F.P = f->d_params; F.stats = f->d_stats;
   F.pigtab = f->d_tables; F.cmf = f->d_tables + 480;
+  {  // the film's own packed view (see solo_view)
+    cfk::Film rec[2] = {F, F};
+    std::swap(rec[1].sh, rec[1].sh2);
+    std::swap(rec[1].scu, rec[1].scu2);
+    std::vector<uint2> tiles(nt);
+    for (size_t t = 0; t < nt; ++t) tiles[t] = make_uint2(0u, (uint32_t)t);
+    if (cudaMalloc(&f->d_recs, sizeof(rec)) != cudaSuccess || cudaMalloc(&f->d_tiles, sizeof(uint2) * nt) != cudaSuccess ||
+        cudaMemcpy(f->d_recs, rec, sizeof(rec), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(f->d_tiles, tiles.data(), sizeof(uint2) * nt, cudaMemcpyHostToDevice) != cudaSuccess) {
+      f->err = "cudaMalloc film records";
+      cudaGetLastError();
+      return bail(CF_ERR_OUT_OF_MEMORY);
+    }
+    f->sh_created = F.sh;
+  }
   // Film::new: zeroed buffers, substrate refl, weave relief, rheo = (1, 0)
   if (cudaMemset(f->arena, 0, total) != cudaSuccess || cudaMemset(f->d_tables, 0, sizeof(float) * 528) != cudaSuccess ||
       cudaMemset(f->d_stats, 0, sizeof(DevStats)) != cudaSuccess) {
@@ -339,12 +338,15 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
 cf_status cf_destroy(cf_film* f) {
   if (!f) return CF_ERR_INVALID_ARG;
   cudaDeviceSynchronize();
+  if (f->batch) batch_forget(f);
   if (f->arena) cudaFree(f->arena);
   if (f->d_params) cudaFree(f->d_params);
   if (f->d_stats) cudaFree(f->d_stats);
   if (f->d_tables) cudaFree(f->d_tables);
   if (f->h_params) cudaFreeHost(f->h_params);
   if (f->params_ev) cudaEventDestroy(f->params_ev);
+  if (f->d_recs) cudaFree(f->d_recs);
+  if (f->d_tiles) cudaFree(f->d_tiles);
   delete f;
   return CF_OK;
 }
@@ -408,9 +410,9 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   CUDA_TRY(f, cudaMemset(F.alpha_s, 0, 16 * n));
   cfk::launch_fill_u32(F.tile_moved, 1u, (size_t)f->tw * f->th, 0);
   // aggregates of the uploaded strata for the first cure, and its colour
-  cfk::launch_compose(F, f->prec, 1, 0);
+  cfk::launch_compose(solo_view(f), f->prec, 1, 0);
   // current stats so that the first adaptive step sees this state
-  cfk::launch_reduce(F, f->prec, 0);
+  cfk::launch_reduce(solo_view(f), f->prec, 0);
   CUDA_TRY(f, cudaGetLastError());
   DevStats ds;
   CUDA_TRY(f, cudaMemcpy(&ds, f->d_stats, sizeof(ds), cudaMemcpyDeviceToHost));
@@ -420,6 +422,30 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   f->h_max_stat = hm;
   f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
   CUDA_TRY(f, cudaDeviceSynchronize());
+  return CF_OK;
+}
+
+cf_status cf_clone_state(cf_film* dst, const cf_film* src, void* stream) {
+  if (!dst || !src || dst == src) return fail(dst, CF_ERR_INVALID_ARG, "cf_clone_state: null or same film");
+  if (dst->w != src->w || dst->h != src->h || dst->prec != src->prec || dst->device != src->device)
+    return fail(dst, CF_ERR_INVALID_ARG, "cf_clone_state: size, precision or device differ");
+  cudaStream_t st = (cudaStream_t)stream;
+  // identical (w, h, precision) give identical arena layouts: one copy moves
+  // every plane, both strata generations included
+  CUDA_TRY(dst, cudaMemcpyAsync(dst->arena, src->arena, src->arena_bytes, cudaMemcpyDeviceToDevice, st));
+  CUDA_TRY(dst, cudaMemcpyAsync(dst->d_tables, src->d_tables, sizeof(float) * 528, cudaMemcpyDeviceToDevice, st));
+  CUDA_TRY(dst, cudaMemcpyAsync(dst->d_stats, src->d_stats, sizeof(DevStats), cudaMemcpyDeviceToDevice, st));
+  CUDA_TRY(dst, cudaMemcpyAsync(dst->d_params, src->d_params, sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
+  dst->S = src->S;
+  dst->P = src->P;
+  dst->implicit_steps = src->implicit_steps;
+  dst->params_dirty = false;
+  dst->h_max_stat = src->h_max_stat;
+  dst->mu_min_stat = src->mu_min_stat;
+  dst->h_max_pending = src->h_max_pending;
+  dst->frames = src->frames;
+  const bool src_swapped = src->F.sh != src->sh_created, dst_swapped = dst->F.sh != dst->sh_created;
+  if (src_swapped != dst_swapped) swap_generations(dst);
   return CF_OK;
 }
 
@@ -508,7 +534,8 @@ cf_status cf_encode_frame(cf_film* f, uint32_t substeps, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
-  f->launches += cfk::launch_frame(f->F, f->prec, substeps, f->S.all_active, st);
+  f->launches += cfk::launch_frame_packed(solo_view(f), f->prec, substeps, 0, st);
+  swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
   f->frames++;
   return CF_OK;
@@ -521,8 +548,8 @@ cf_status cf_step_adaptive(cf_film* f, float dt_max, void* stream) {
   if (f->h_params->dt_max != dt_max) f->params_dirty = true;
   cf_status s = upload_params(f, st, dt_max);
   if (s != CF_OK) return s;
-  cfk::launch_adaptive_params(f->d_params, f->d_stats, st);
-  f->launches += 1 + cfk::launch_frame(f->F, f->prec, 1, f->S.all_active, st);
+  f->launches += cfk::launch_frame_packed(solo_view(f), f->prec, 1, 1, st);
+  swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
   f->frames++;
   return CF_OK;
@@ -536,7 +563,7 @@ cf_status cf_dry_now(cf_film* f, void* stream) {  // src/film/mod.rs:1230-1244
   f->params_dirty = true;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
-  cfk::launch_cure(f->F, f->prec, st);
+  cfk::launch_cure(solo_view(f), f->prec, st);
   if ((s = check_launch(f)) != CF_OK) return s;
   CUDA_TRY(f, cudaStreamSynchronize(st));  // the pinned staging is reused below
   f->P = saved;
@@ -712,7 +739,9 @@ cf_status cf_debug_run(cf_film* f, const char* kernel, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
-  if (!cfk::launch_one(f->F, f->prec, kernel, f->S.all_active, st)) return fail(f, CF_ERR_INVALID_ARG, "unknown kernel");
+  const int r = cfk::launch_one(solo_view(f), f->prec, kernel, st);
+  if (!r) return fail(f, CF_ERR_INVALID_ARG, "unknown kernel");
+  if (r == 2) swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
   CUDA_TRY(f, cudaStreamSynchronize(st));
   return CF_OK;

@@ -113,12 +113,12 @@ struct Film {
   ushort4* color;  // rgba16f
   uint32_t* tile_flags;
   uint32_t* tile_moved;
-  float2* stats64; // per 64x64 tile (h_max, mu_min)
   int32_t* fill_src;
   uint8_t* fflags;  // bit f: strata_split wrote a nonzero acc_s face f this frame
   uint32_t* full_list;  // cells of the strata full path (DevStats::full_count)
   uint32_t* fill_list;  // strata fill candidates (DevStats::fill_count)
   uint32_t persist_blocks;  // grid of the list kernels: a few blocks per SM
+  uint32_t all_active;      // keep every tile active (settings.all_active)
   const float* pigtab;  // 12 x 40
   const float* cmf;     // 16 x 3
 };

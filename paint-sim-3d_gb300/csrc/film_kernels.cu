@@ -30,10 +30,17 @@
 
 namespace cfk {
 
+// A kernel body works on one 16x16 tile T of film F.  The single-film
+// kernels bind T to blockIdx; the packed kernels (k*_packed) take film and
+// tile from an entry of a tile table that spans many films.
+struct TileId {
+  uint32_t x, y;
+};
+
 #define TILE_PROLOGUE                                              \
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x);              \
-  const int j = (int)(blockIdx.y * 16 + threadIdx.y);              \
-  if ((F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) == 0u) return; \
+  const int i = (int)(T.x * 16 + threadIdx.x);                     \
+  const int j = (int)(T.y * 16 + threadIdx.y);                     \
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;     \
   if (i >= (int)F.w || j >= (int)F.h) return;                      \
   const uint32_t c = idx(F, i, j);                                 \
   const DevParams& D = *F.P;                                       \
@@ -46,42 +53,38 @@ __device__ __forceinline__ float sel4(float4 v, int k) {
 __device__ __forceinline__ float4 neg4(float4 v) { return make_float4(-v.x, -v.y, -v.z, -v.w); }
 __device__ __forceinline__ bool nb_ok(const Film& F, int i, int j) { return in_grid(F, i, j) && cell_active(F, i, j); }
 
-// film.wgsl:1365-1391
-__global__ void __launch_bounds__(256) k_mark_tiles(Film F) {
-  __shared__ uint32_t any;
-  if (threadIdx.x == 0 && threadIdx.y == 0) any = 0u;
-  __syncthreads();
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
-  uint32_t bits = 0u;
-  if (i < (int)F.w && j < (int)F.h) {
-    uint32_t c = idx(F, i, j);
-    float hv = F.hh[c];
-    if (hv > 0.f) {
-      bits = 1u;
-      if (threadIdx.x < 8) bits |= 2u;
-      if (threadIdx.x >= 8) bits |= 4u;
-      if (threadIdx.y < 8) bits |= 8u;
-      if (threadIdx.y >= 8) bits |= 16u;
-      if (fabsf(hv - F.h_frame[c]) > FRAME_EPS) bits |= MOVED;
-    }
+// film.wgsl:1365-1391, one warp per 16x16 tile: lane l takes half a row
+// (row l/2, columns 8(l%2)..+7), every load of the tile is issued before any
+// is used, and a warp OR replaces the workgroup atomics.
+__device__ __forceinline__ void mark_tile(const Film& F, uint32_t t) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t moved_before = lane == 0u ? F.tile_moved[t] : 0u;
+  const int i0 = (int)((t % F.tw) * 16u + (lane & 1u) * 8u), j = (int)((t / F.tw) * 16u + (lane >> 1));
+  float hv[8], hf[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const bool in = i0 + k < (int)F.w && j < (int)F.h;
+    const uint32_t c = in ? idx(F, i0 + k, j) : 0u;
+    hv[k] = in ? F.hh[c] : 0.f;
+    hf[k] = in ? F.h_frame[c] : 0.f;
   }
+  uint32_t bits = 0u;
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (hv[k] > 0.f) {
+      bits |= 1u | ((lane & 1u) ? 4u : 2u) | ((lane >> 1) < 8u ? 8u : 16u);
+      if (fabsf(hv[k] - hf[k]) > FRAME_EPS) bits |= MOVED;
+    }
   bits = __reduce_or_sync(0xffffffffu, bits);
-  if ((threadIdx.x & 31) == 0 && bits) atomicOr(&any, bits);
-  __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    uint32_t t = blockIdx.x + blockIdx.y * F.tw;
-    uint32_t flags = any;
-    if (F.tile_moved[t] != 0u) flags |= MOVED;
+  if (lane == 0u) {
+    if (moved_before != 0u) bits |= MOVED;
     F.tile_moved[t] = 0u;
-    F.tile_flags[t] = flags;
+    F.tile_flags[t] = bits;
   }
 }
 
 // film.wgsl:1393-1425 (bit 32 is written in place; the bits read are not it)
-__global__ void __launch_bounds__(256) k_compact_tiles(Film F, int all_active) {
-  uint32_t nt = F.tw * F.th;
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nt) return;
+__device__ __forceinline__ void compact_tile(const Film& F, uint32_t t, int all_active) {
   int tx = (int)(t % F.tw), ty = (int)(t / F.tw);
   uint32_t own = F.tile_flags[t];
   uint32_t any = own & MOVED;
@@ -117,8 +120,8 @@ __device__ __forceinline__ void lnmu_table(const float* pigtab, float out[12]) {
 // from agg (written by the last strata pass); the stack is only read when
 // the bottom stratum commits.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_cure(Film F) {
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+__device__ __forceinline__ void cure_tile(const Film& F, TileId T) {
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   const cf_params& P = F.P->p;
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(256) k_cure(Film F) {
 }
 
 // film.wgsl:1427-1434
-__global__ void __launch_bounds__(256) k_clear_acc(Film F) {
+__device__ __forceinline__ void clear_acc_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
   F.h_frame[c] = F.hh[c];
@@ -182,21 +185,31 @@ __global__ void __launch_bounds__(256) k_clear_acc(Film F) {
 
 // film.wgsl:16-42; with CLEAR the kernel also does clear_acc (film.wgsl:1427-1434)
 // for its cell, which the reference dispatches just before the first laplacian.
+// The surface level usurf (film.wgsl:147-151, one exp each) of the tile and
+// its 1-cell halo is evaluated once into shared memory, so a cell costs about
+// 1.3 evaluations instead of 9; the 9-point sum keeps the reference's order.
 template <bool CLEAR>
-__global__ void __launch_bounds__(256) k_laplacian(Film F) {
-  TILE_PROLOGUE
-  float hv = F.hh[c];
+__device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  __shared__ float su[18][18];
+  const cf_params& P = F.P->p;
+  const int i0 = (int)T.x * 16 - 1, j0 = (int)T.y * 16 - 1;
+  for (int q = threadIdx.y * 16 + threadIdx.x; q < 18 * 18; q += 256)
+    su[q / 18][q % 18] = usurf(F, P, i0 + q % 18, j0 + q / 18);
+  __syncthreads();
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const uint32_t c = idx(F, i, j);
+  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+  const float hv = F.hh[c];
   if (CLEAR) {
     F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
     F.h_frame[c] = hv;
   }
-  float s0 = hv + F.m[c];
-  float hold = 0.f, pl = 0.f;
-  if (hv > 0.f) hold = hold_level(P, nose_dist(F, c));
-  float u0 = s0 - hold;
-  float ax = usurf(F, P, i - 1, j) + usurf(F, P, i + 1, j) + usurf(F, P, i, j - 1) + usurf(F, P, i, j + 1);
-  float dg = usurf(F, P, i - 1, j - 1) + usurf(F, P, i + 1, j - 1) + usurf(F, P, i - 1, j + 1) +
-             usurf(F, P, i + 1, j + 1);
+  const float u0 = su[y][x];  // = s0 - hold_level of this cell
+  float pl = 0.f;
+  float ax = su[y][x - 1] + su[y][x + 1] + su[y - 1][x] + su[y + 1][x];
+  float dg = su[y - 1][x - 1] + su[y - 1][x + 1] + su[y + 1][x - 1] + su[y + 1][x + 1];
   float l = (W_AXIS * ax + W_DIAG_LAP * dg - (4.0f * W_AXIS + 4.0f * W_DIAG_LAP) * u0) * P.inv_dx * P.inv_dx;
   if (hv > 0.f) {
     float d = nose_dist(F, c);
@@ -205,7 +218,7 @@ __global__ void __launch_bounds__(256) k_laplacian(Film F) {
       if (n.x * n.x + n.y * n.y > 0.5f) pl = line_pressure(F, P, i, j) * expf(-(d - 1.0f) * 0.7f);
     }
   }
-  F.pres[c] = make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * (s0 - hold) + pl);
+  F.pres[c] = make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * u0 + pl);
 }
 
 // film.wgsl:58-87.  The HB flux of every cell of the tile and its 3-cell
@@ -213,15 +226,15 @@ __global__ void __launch_bounds__(256) k_laplacian(Film F) {
 // window in the reference's row-major order, so the result is identical to
 // evaluating the flux 49 times per cell.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_plug(Film F) {
+__device__ __forceinline__ void plug_tile(const Film& F, TileId T) {
   constexpr int R = 3, S = 16 + 2 * R;
   __shared__ float sq[S * S], sm[S * S];  // flux q and mass h of each window cell
   __shared__ uint8_t sy[S * S];           // bit 0: wet cell in the grid, bit 1: tau_y > 0
-  if ((F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) == 0u) return;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
   const DevParams& D = *F.P;
   const cf_params& P = D.p;
   const float gb = P.phys[0] * D.gxy;
-  const int x0 = (int)blockIdx.x * 16 - R, y0 = (int)blockIdx.y * 16 - R;
+  const int x0 = (int)T.x * 16 - R, y0 = (int)T.y * 16 - R;
   const int tid = threadIdx.y * 16 + threadIdx.x;
   for (int q = tid; q < S * S; q += 256) {
     int x = x0 + q % S, y = y0 + q / S;
@@ -243,7 +256,7 @@ __global__ void __launch_bounds__(256) k_plug(Film F) {
     sy[q] = yl;
   }
   __syncthreads();
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   F.tmp[c] = 0.f;
@@ -268,7 +281,7 @@ __global__ void __launch_bounds__(256) k_plug(Film F) {
 // Three blocks per SM: the face code needs no more than 64 registers, and
 // the occupancy hides its dependent loads.
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) k_fluxes(Film F) {
+__device__ __forceinline__ void fluxes_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   float q[4];
 #pragma unroll 1
@@ -277,7 +290,7 @@ __global__ void __launch_bounds__(256, 3) k_fluxes(Film F) {
 }
 
 // film.wgsl:516-537
-__global__ void __launch_bounds__(256) k_limiter(Film F) {
+__device__ __forceinline__ void limiter_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   float4 f = F.flux[c];
   float out = fmaxf(f.x, 0.f) + fmaxf(f.y, 0.f) + fmaxf(f.z, 0.f) + fmaxf(f.w, 0.f);
@@ -311,9 +324,12 @@ __device__ __forceinline__ void backfill(const Film& F, uint32_t c, uint32_t src
 
 // film.wgsl:539-561, 803-863
 template <int MODE>
-__global__ void __launch_bounds__(256) k_apply(Film F) {
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
-  if ((F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) == 0u) return;
+// Every tile (active or not) also snapshots delta into delta_old for the
+// nose that follows (apply does not write delta).
+__device__ __forceinline__ void apply_tile(const Film& F, TileId T) {
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  if (i < (int)F.w && j < (int)F.h) F.delta_old[idx(F, i, j)] = F.delta[idx(F, i, j)];
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
   bool moved = false;
   if (i < (int)F.w && j < (int)F.h) {
     const cf_params& P = F.P->p;
@@ -360,11 +376,11 @@ __global__ void __launch_bounds__(256) k_apply(Film F) {
     F.acc[c] = make_float4(a.x + accv[0] * P.dt, a.y + accv[1] * P.dt, a.z + accv[2] * P.dt, a.w + accv[3] * P.dt);
   }
   if (__syncthreads_or(moved) && threadIdx.x == 0 && threadIdx.y == 0)
-    F.tile_moved[blockIdx.x + blockIdx.y * F.tw] = 1u;
+    F.tile_moved[T.x + T.y * F.tw] = 1u;
 }
 
 // film.wgsl:680-723, reading delta_old (Jacobi)
-__global__ void __launch_bounds__(256) k_nose(Film F) {
+__device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   if (F.hh[c] <= 0.f) {
     F.delta[c] = 0u;
@@ -430,7 +446,7 @@ __device__ __forceinline__ float4 band_split(const Film& F, uint32_t cu, float h
 
 // film.wgsl:475-514 (acc_s face-major)
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) k_strata_split(Film F) {
+__device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   float4 a4 = F.acc[c];
   float a[4] = {a4.x, a4.y, a4.z, a4.w};
@@ -452,37 +468,32 @@ __global__ void __launch_bounds__(256, 3) k_strata_split(Film F) {
   F.fflags[c] = (uint8_t)flags;
 }
 
-// film.wgsl:1330-1361, plus the device-wide max/min the adaptive step reads
+// film.wgsl:1330-1361 over one 16x16 tile: the device-wide max / min the
+// adaptive step reads (order-independent, so the tile shape does not matter).
 template <int MODE>
-__global__ void __launch_bounds__(256) k_reduce_tiles(Film F) {
+__device__ __forceinline__ void reduce16_tile(const Film& F, TileId T) {
   const cf_params& P = F.P->p;
   float hm = 0.f, mm = 1e9f;
-  for (int dy = 0; dy < 4; ++dy)
-    for (int dx = 0; dx < 4; ++dx) {
-      int i = blockIdx.x * 64 + threadIdx.x * 4 + dx, j = blockIdx.y * 64 + threadIdx.y * 4 + dy;
-      if (i < (int)F.w && j < (int)F.h) {
-        uint32_t c = idx(F, i, j);
-        float v = F.hh[c];
-        if (v > 4.0f * P.ein[3]) { hm = fmaxf(hm, v); mm = fminf(mm, rmu<MODE>(F, c)); }
-      }
-    }
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  if (i < (int)F.w && j < (int)F.h) {
+    uint32_t c = idx(F, i, j);
+    float v = F.hh[c];
+    if (v > 4.0f * P.ein[3]) { hm = v; mm = rmu<MODE>(F, c); }
+  }
   for (int o = 16; o > 0; o >>= 1) {
     hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
     mm = fminf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
   }
+  // one pair of atomics per tile, and none for a tile without such a cell
+  // (its partials are the identities 0 and 1e9)
   __shared__ float sh[8], sm[8];
-  int lane = (threadIdx.y * 16 + threadIdx.x) & 31, wid = (threadIdx.y * 16 + threadIdx.x) >> 5;
-  if (lane == 0) { sh[wid] = hm; sm[wid] = mm; }
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  if ((tid & 31) == 0) { sh[tid >> 5] = hm; sm[tid >> 5] = mm; }
   __syncthreads();
-  if (wid == 0) {
-    hm = lane < 8 ? sh[lane] : 0.f;
-    mm = lane < 8 ? sm[lane] : 1e9f;
-    for (int o = 4; o > 0; o >>= 1) {
-      hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
-      mm = fminf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
-    }
-    if (lane == 0) {
-      F.stats64[blockIdx.x + blockIdx.y * gridDim.x] = make_float2(hm, mm);
+  if (tid == 0) {
+#pragma unroll
+    for (int w = 1; w < 8; ++w) { hm = fmaxf(hm, sh[w]); mm = fminf(mm, sm[w]); }
+    if (hm > 0.f) {
       atomicMax(&F.stats->h_max_bits, __float_as_uint(hm));
       atomicMin(&F.stats->mu_min_bits, __float_as_uint(mm));
     }
@@ -518,14 +529,14 @@ __device__ __forceinline__ float4 strata_limit_at(const Film& F, const cf_params
 
 // strata_limit as a dispatch of its own (inspection only; the strata pass
 // computes the same values in shared memory)
-__global__ void __launch_bounds__(256) k_strata_limit(Film F) {
+__device__ __forceinline__ void strata_limit_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   F.alpha_s[c] = strata_limit_at(F, P, i, j);
 }
 
 // Face flags from acc_s as strata_split writes them (for an inspection
 // dispatch of the strata pass that does not follow a strata_split).
-__global__ void __launch_bounds__(256) k_face_flags(Film F) {
+__device__ __forceinline__ void face_flags_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   uint32_t flags = 0u;
 #pragma unroll
@@ -595,18 +606,18 @@ __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm
 // are shaded, as the reference's full-grid shade does.  Active wet cells left
 // without strata become strata_fill candidates.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_strata_fast(Film F) {
+__device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   __shared__ float tab[480];
   __shared__ float cm[48];
   __shared__ float ltab[12];
   const int tid = threadIdx.y * 16 + threadIdx.x;
   load_tables(F, tab, cm, ltab, tid, 256);
   __syncthreads();
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   const cf_params& P = F.P->p;
-  const bool act = (F.tile_flags[blockIdx.x + blockIdx.y * F.tw] & ACTIVE) != 0u;
+  const bool act = (F.tile_flags[T.x + T.y * F.tw] & ACTIVE) != 0u;
   const float hc = F.hh[c];
   float4 t4 = F.sh[c], cu = F.scu[c];
   if (act) {
@@ -688,21 +699,16 @@ __device__ __forceinline__ void lane_inflow(const Film& F, const cf_params& P, c
 // and compaction.  Thicknesses go to the next generation, pigment slots to
 // the side plane (copied back by k_strata_commit), then the cell is shaded
 // and composed from the stored (rounded) slots.
+// List entries first, first + stride, ... of film F; the tables are in
+// shared memory.
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) k_strata_full(Film F) {
-  __shared__ float tab[480];
-  __shared__ float cm[48];
-  __shared__ float ltab[12];
-  const uint32_t count = F.stats->full_count;
-  if (count == 0u) return;
-  load_tables(F, tab, cm, ltab, threadIdx.x, 256);
-  __syncthreads();
+__device__ __forceinline__ void strata_full_film(const Film& F, const float* tab, const float* cm, const float* ltab,
+                                                 uint32_t count, uint32_t first, uint32_t stride) {
   const HalfWarp H((int)(threadIdx.x & 31u));
   const cf_params& P = F.P->p;
   const bool dbg = P.flags[0] == 1u;
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  const uint32_t stride = gridDim.x * (blockDim.x >> 4);
-  for (uint32_t e = blockIdx.x * (blockDim.x >> 4) + (threadIdx.x >> 4); e < count; e += stride) {
+  for (uint32_t e = first; e < count; e += stride) {
     const uint32_t c = F.full_list[e];
     const int i = (int)(c % F.w), j = (int)(c / F.w);
     const float hc = F.hh[c];
@@ -801,21 +807,19 @@ __global__ void __launch_bounds__(256, 3) k_strata_full(Film F) {
     }
   }
 }
-
 // Copies the listed cells' new pigment slots from the side plane back into
 // the pigment plane (consecutive threads take consecutive list entries).
 template <int MODE>
-__global__ void __launch_bounds__(256) k_strata_commit(Film F) {
+__device__ __forceinline__ void strata_commit_film(const Film& F, size_t first, size_t stride) {
   constexpr uint32_t CH = 4u * PigIO<MODE>::QN;  // 16-byte chunks per cell
   const uint32_t count = F.stats->full_count;
   const size_t units = (size_t)count * CH;
-  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < units; u += (size_t)gridDim.x * blockDim.x) {
+  for (size_t u = first; u < units; u += stride) {
     const uint32_t ch = (uint32_t)(u / count), e = (uint32_t)(u % count);
     const size_t at = (size_t)ch * F.n + F.full_list[e];
     F.pig[at] = F.pig2[at];
   }
 }
-
 // strata_fill (strata.wgsl:288-323) x 6 over the candidates of the strata
 // pass, in one block: select reads only strata sums, apply writes only cells
 // that had none, and a block barrier separates the two (Jacobi semantics, as
@@ -823,11 +827,10 @@ __global__ void __launch_bounds__(256) k_strata_commit(Film F) {
 // candidate has h <= 0, lies in an inactive tile or has strata, and so
 // selects no source in any of the six iterations.
 template <int MODE>
-__global__ void __launch_bounds__(1024) k_fill_list(Film F) {
+__device__ __forceinline__ void fill_list_film(const Film& F, float* lt) {
   const uint32_t count = F.stats->fill_count;
   if (count == 0u) return;
   const cf_params& P = F.P->p;
-  __shared__ float lt[12];
   if (threadIdx.x < 12) lt[threadIdx.x] = logf(fmaxf(F.pigtab[threadIdx.x * 40 + 32], 1e-3f));
   __syncthreads();
   for (int r = 0; r < 6; ++r) {
@@ -870,10 +873,9 @@ __global__ void __launch_bounds__(1024) k_fill_list(Film F) {
     __syncthreads();
   }
 }
-
 // strata_fill as one select + apply pair over the whole grid (inspection
 // dispatch; the frame runs k_fill_list).
-__global__ void __launch_bounds__(256) k_fill_select(Film F) {
+__device__ __forceinline__ void fill_select_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   int32_t src = -1;
   float hc = F.hh[c];
@@ -898,7 +900,7 @@ __global__ void __launch_bounds__(256) k_fill_select(Film F) {
 }
 // ...and re-shades the filled cell and refreshes its aggregates.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_fill_apply(Film F) {
+__device__ __forceinline__ void fill_apply_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   int32_t src = F.fill_src[c];
   if (src < 0) return;
@@ -918,8 +920,8 @@ __global__ void __launch_bounds__(256) k_fill_apply(Film F) {
 // Aggregates and colour of the current state (after a state upload, or for
 // an inspection dispatch of cure or shade).
 template <int MODE>
-__global__ void __launch_bounds__(256) k_compose(Film F, int shade) {
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
+__device__ __forceinline__ void compose_tile(const Film& F, TileId T, int shade) {
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   const cf_params& P = F.P->p;
@@ -960,7 +962,7 @@ __global__ void __launch_bounds__(256) k_mass(Film F) {
   }
 }
 
-__global__ void k_stats_reset(Film F) {
+__device__ __forceinline__ void stats_reset_film(const Film& F) {
   F.stats->h_max_bits = 0u;
   F.stats->mu_min_bits = __float_as_uint(1e9f);
   F.stats->active_tiles = 0u;
@@ -978,7 +980,7 @@ __global__ void k_mass_reset(Film F) {
 // one substep per frame) and the dt-dependent fields of update_params
 // (src/film/mod.rs:869-917).  Round-to-nearest intrinsics keep the f32
 // arithmetic identical to the host's (no contraction).
-__global__ void k_adaptive_params(DevParams* Dp, DevStats* S) {
+__device__ __forceinline__ void adaptive_params_film(DevParams* Dp, DevStats* S) {
   DevParams D = *Dp;
   cf_params& P = D.p;
   float h_stat = __uint_as_float(S->h_max_bits);
@@ -1100,86 +1102,169 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
   if (q < n) p[q] = v;
 }
 
+// delta -> delta_old for one tile (the inspection dispatch of nose; in the
+// frame, apply takes this snapshot)
+__device__ __forceinline__ void copy_delta_tile(const Film& F, TileId T) {
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  if (i < (int)F.w && j < (int)F.h) {
+    const uint32_t c = idx(F, i, j);
+    F.delta_old[c] = F.delta[c];
+  }
+}
+
+// ------------------------------------------------------ packed kernels --
+// One launch per dispatch for many films: block b takes entry b of a tile
+// table (film index, tile index), so canvases of any size share the grid.
+// The film records are read-only for the launch.
+
+#define PACKED_ARGS const Film* __restrict__ films, const uint2* __restrict__ tiles, uint32_t ntiles
+#define PACKED_TILE                    \
+  if (blockIdx.x >= ntiles) return;    \
+  const uint2 pe_ = tiles[blockIdx.x]; \
+  const Film& F = films[pe_.x];        \
+  const TileId T{pe_.y % F.tw, pe_.y / F.tw};
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_cure(PACKED_ARGS) { PACKED_TILE cure_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256) kp_clear_acc(PACKED_ARGS) { PACKED_TILE clear_acc_tile(F, T); }
+template <bool CLEAR>
+__global__ void __launch_bounds__(256) kp_laplacian(PACKED_ARGS) { PACKED_TILE laplacian_tile<CLEAR>(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILE plug_tile<MODE>(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256, 3) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILE copy_delta_tile(F, T); }
+__global__ void __launch_bounds__(256) kp_nose(PACKED_ARGS) { PACKED_TILE nose_tile(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256, 3) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILE reduce16_tile<MODE>(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_strata_fast(PACKED_ARGS) { PACKED_TILE strata_fast_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256) kp_strata_limit(PACKED_ARGS) { PACKED_TILE strata_limit_tile(F, T); }
+__global__ void __launch_bounds__(256) kp_face_flags(PACKED_ARGS) { PACKED_TILE face_flags_tile(F, T); }
+__global__ void __launch_bounds__(256) kp_fill_select(PACKED_ARGS) { PACKED_TILE fill_select_tile(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_fill_apply(PACKED_ARGS) { PACKED_TILE fill_apply_tile<MODE>(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_compose(PACKED_ARGS, int shade) { PACKED_TILE compose_tile<MODE>(F, T, shade); }
+__global__ void __launch_bounds__(256) kp_mark_tiles(PACKED_ARGS) {
+  const uint32_t e = blockIdx.x * 8u + (threadIdx.x >> 5);
+  if (e >= ntiles) return;
+  const uint2 pe = tiles[e];
+  mark_tile(films[pe.x], pe.y);
+}
+__global__ void __launch_bounds__(256) kp_compact_tiles(PACKED_ARGS) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ntiles) return;
+  const uint2 pe = tiles[e];
+  compact_tile(films[pe.x], pe.y, (int)films[pe.x].all_active);
+}
+#undef PACKED_TILE
+#undef PACKED_ARGS
+// per film: one thread each
+__global__ void kp_stats_reset(const Film* __restrict__ films, uint32_t nfilms) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < nfilms) stats_reset_film(films[f]);
+}
+__global__ void kp_adaptive_params(const Film* __restrict__ films, uint32_t nfilms) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < nfilms) adaptive_params_film(const_cast<DevParams*>(films[f].P), films[f].stats);
+}
+// the strata full path over every film's list, with the film's tables
+template <int MODE>
+__global__ void __launch_bounds__(256, 3) kp_strata_full(const Film* __restrict__ films, uint32_t nfilms) {
+  __shared__ float tab[480];
+  __shared__ float cm[48];
+  __shared__ float ltab[12];
+  for (uint32_t f = 0; f < nfilms; ++f) {
+    const Film& F = films[f];
+    const uint32_t count = F.stats->full_count;
+    const uint32_t first = blockIdx.x * (blockDim.x >> 4);
+    if (first >= count) continue;  // the same for the whole block
+    __syncthreads();
+    load_tables(F, tab, cm, ltab, threadIdx.x, 256);
+    __syncthreads();
+    strata_full_film<MODE>(F, tab, cm, ltab, count, first + (threadIdx.x >> 4), gridDim.x * (blockDim.x >> 4));
+  }
+}
+template <int MODE>
+__global__ void __launch_bounds__(256) kp_strata_commit(const Film* __restrict__ films, uint32_t nfilms) {
+  for (uint32_t f = 0; f < nfilms; ++f)
+    strata_commit_film<MODE>(films[f], blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+// one block per film
+template <int MODE>
+__global__ void __launch_bounds__(1024) kp_fill_list(const Film* __restrict__ films, uint32_t nfilms) {
+  __shared__ float lt[12];
+  if (blockIdx.x < nfilms) fill_list_film<MODE>(films[blockIdx.x], lt);
+}
+
 // ---------------------------------------------------------------- host --
 
-static inline dim3 tiles_grid(const Film& F) { return dim3(F.tw, F.th); }
+// Launches K<MODE> for the run-time precision `mode`.
+#define CFK_LAUNCH(K, G, B, ST, ...)                                    \
+  do {                                                                  \
+    if (mode == CF_PREC_REFERENCE) K<CF_PREC_REFERENCE><<<G, B, 0, ST>>>(__VA_ARGS__); \
+    else if (mode == CF_PREC_FP32) K<CF_PREC_FP32><<<G, B, 0, ST>>>(__VA_ARGS__);     \
+    else K<CF_PREC_BF16><<<G, B, 0, ST>>>(__VA_ARGS__);                 \
+  } while (0)
 
-static void swap_generations(Film& F) {
-  float4* t = F.sh; F.sh = F.sh2; F.sh2 = t;
-  t = F.scu; F.scu = F.scu2; F.scu2 = t;
-}
-
-// The strata pass: part 1 over the grid (fast path, lists the rest), part 2
-// over the list, the copy back of the listed cells' pigments, then the
-// generation swap of thicknesses and cure fractions.
 template <int MODE>
-static uint32_t strata_pass_t(Film& F, cudaStream_t st) {
-  dim3 g = tiles_grid(F), b(16, 16);
-  k_strata_fast<MODE><<<g, b, 0, st>>>(F);
-  k_strata_full<MODE><<<F.persist_blocks, 256, 0, st>>>(F);
-  k_strata_commit<MODE><<<F.persist_blocks, 256, 0, st>>>(F);
-  swap_generations(F);
-  return 3;
-}
-
-// Enqueues one frame; returns the number of kernel launches.  F's strata
-// generations are swapped in place.
-template <int MODE>
-static uint32_t frame_t(Film& F, uint32_t substeps, int all_active, cudaStream_t st) {
-  dim3 g = tiles_grid(F), b(16, 16);
-  uint32_t nt = F.tw * F.th, n = 0;
-  k_stats_reset<<<1, 1, 0, st>>>(F); ++n;
-  k_mark_tiles<<<g, b, 0, st>>>(F); ++n;
-  k_compact_tiles<<<(nt + 255) / 256, 256, 0, st>>>(F, all_active); ++n;
-  k_cure<MODE><<<g, b, 0, st>>>(F); ++n;
-  if (substeps == 0) { k_clear_acc<<<g, b, 0, st>>>(F); ++n; }
+static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adaptive, cudaStream_t st) {
+  const Film* A = V.films;
+  const uint2* T = V.tiles;
+  const uint32_t nt = V.ntiles, nf = V.nfilms;
+  if (nf == 0u || nt == 0u) return 0u;
+  const uint32_t fb = (nf + 127u) / 128u;
+  uint32_t n = 0;
+  dim3 b(16, 16);
+  if (adaptive) { kp_adaptive_params<<<fb, 128, 0, st>>>(A, nf); ++n; }
+  kp_stats_reset<<<fb, 128, 0, st>>>(A, nf);
+  kp_mark_tiles<<<(nt + 7u) / 8u, 256, 0, st>>>(A, T, nt);
+  kp_compact_tiles<<<(nt + 255u) / 256u, 256, 0, st>>>(A, T, nt);
+  kp_cure<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  n += 4;
+  if (substeps == 0) { kp_clear_acc<<<nt, b, 0, st>>>(A, T, nt); ++n; }
   for (uint32_t s = 0; s < substeps; ++s) {
-    if (s == 0) k_laplacian<true><<<g, b, 0, st>>>(F);
-    else k_laplacian<false><<<g, b, 0, st>>>(F);
-    k_plug<MODE><<<g, b, 0, st>>>(F);
-    k_fluxes<MODE><<<g, b, 0, st>>>(F);
-    k_limiter<<<g, b, 0, st>>>(F);
-    k_apply<MODE><<<g, b, 0, st>>>(F);
-    cudaMemcpyAsync(F.delta_old, F.delta, sizeof(uint32_t) * (size_t)F.w * F.h, cudaMemcpyDeviceToDevice, st);
-    k_nose<<<g, b, 0, st>>>(F);
+    if (s == 0) kp_laplacian<true><<<nt, b, 0, st>>>(A, T, nt);
+    else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+    kp_plug<MODE><<<nt, b, 0, st>>>(A, T, nt);
+    kp_fluxes<MODE><<<nt, b, 0, st>>>(A, T, nt);
+    kp_limiter<<<nt, b, 0, st>>>(A, T, nt);
+    kp_apply<MODE><<<nt, b, 0, st>>>(A, T, nt);
+    kp_nose<<<nt, b, 0, st>>>(A, T, nt);
     n += 6;
   }
-  k_laplacian<false><<<g, b, 0, st>>>(F);
-  k_strata_split<MODE><<<g, b, 0, st>>>(F);
-  k_reduce_tiles<MODE><<<dim3((F.w + 63) / 64, (F.h + 63) / 64), b, 0, st>>>(F);
-  n += 3;
-  n += strata_pass_t<MODE>(F, st);
-  k_fill_list<MODE><<<1, 1024, 0, st>>>(F);
-  return n + 1;
+  kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+  kp_strata_split<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  kp_reduce<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  kp_strata_fast<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
+  kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
+  kp_fill_list<MODE><<<nf, 1024, 0, st>>>(V.films_next, nf);
+  return n + 7;
 }
 
-uint32_t launch_frame(Film& F, int mode, uint32_t substeps, int all_active, cudaStream_t st) {
-  if (mode == CF_PREC_REFERENCE) return frame_t<CF_PREC_REFERENCE>(F, substeps, all_active, st);
-  if (mode == CF_PREC_FP32) return frame_t<CF_PREC_FP32>(F, substeps, all_active, st);
-  return frame_t<CF_PREC_BF16>(F, substeps, all_active, st);
+uint32_t launch_frame_packed(const PackedFrame& V, int mode, uint32_t substeps, int adaptive, cudaStream_t st) {
+  if (mode == CF_PREC_REFERENCE) return frame_packed_t<CF_PREC_REFERENCE>(V, substeps, adaptive, st);
+  if (mode == CF_PREC_FP32) return frame_packed_t<CF_PREC_FP32>(V, substeps, adaptive, st);
+  return frame_packed_t<CF_PREC_BF16>(V, substeps, adaptive, st);
 }
 
-void launch_adaptive_params(DevParams* Dp, DevStats* S, cudaStream_t st) { k_adaptive_params<<<1, 1, 0, st>>>(Dp, S); }
-
-void launch_cure(const Film& F, int mode, cudaStream_t st) {
-  dim3 g = tiles_grid(F), b(16, 16);
-  if (mode == CF_PREC_REFERENCE) k_cure<CF_PREC_REFERENCE><<<g, b, 0, st>>>(F);
-  else if (mode == CF_PREC_FP32) k_cure<CF_PREC_FP32><<<g, b, 0, st>>>(F);
-  else k_cure<CF_PREC_BF16><<<g, b, 0, st>>>(F);
+void launch_cure(const PackedFrame& V, int mode, cudaStream_t st) {
+  CFK_LAUNCH(kp_cure, V.ntiles, dim3(16, 16), st, V.films, V.tiles, V.ntiles);
 }
 
-void launch_compose(const Film& F, int mode, int shade, cudaStream_t st) {
-  dim3 g = tiles_grid(F), b(16, 16);
-  if (mode == CF_PREC_REFERENCE) k_compose<CF_PREC_REFERENCE><<<g, b, 0, st>>>(F, shade);
-  else if (mode == CF_PREC_FP32) k_compose<CF_PREC_FP32><<<g, b, 0, st>>>(F, shade);
-  else k_compose<CF_PREC_BF16><<<g, b, 0, st>>>(F, shade);
+void launch_compose(const PackedFrame& V, int mode, int shade, cudaStream_t st) {
+  CFK_LAUNCH(kp_compose, V.ntiles, dim3(16, 16), st, V.films, V.tiles, V.ntiles, shade);
 }
 
-void launch_reduce(const Film& F, int mode, cudaStream_t st) {
-  dim3 g((F.w + 63) / 64, (F.h + 63) / 64), b(16, 16);
-  k_stats_reset<<<1, 1, 0, st>>>(F);
-  if (mode == CF_PREC_BF16) k_reduce_tiles<CF_PREC_BF16><<<g, b, 0, st>>>(F);
-  else k_reduce_tiles<CF_PREC_FP32><<<g, b, 0, st>>>(F);
+void launch_reduce(const PackedFrame& V, int mode, cudaStream_t st) {
+  kp_stats_reset<<<(V.nfilms + 127u) / 128u, 128, 0, st>>>(V.films, V.nfilms);
+  CFK_LAUNCH(kp_reduce, V.ntiles, dim3(16, 16), st, V.films, V.tiles, V.ntiles);
 }
 
 void launch_mass(const Film& F, int sms, cudaStream_t st) {
@@ -1216,43 +1301,50 @@ void launch_rheo_export(const Film& F, int mode, float2* dst, size_t n, cudaStre
   else k_rheo_export<float><<<g, 256, 0, st>>>(F, dst, n);
 }
 
-// Single dispatches for parity checks, named after the WGSL entry points.
-// "strata_pass" runs strata_limit + strata_update + shade (swapping the
-// thickness generations) and "strata_fill" one select/apply pair over the
-// whole grid.
-int launch_one(Film& F, int mode, const char* name, int all_active, cudaStream_t st) {
-  dim3 g = tiles_grid(F), b(16, 16);
-  uint32_t nt = F.tw * F.th;
+// Single dispatches for parity checks, named after the WGSL entry points,
+// on the same kernels as the frame.  "strata_pass" runs strata_limit +
+// strata_update + shade into the other thickness generation (returns 2: the
+// caller swaps the film's generations) and "strata_fill" one select/apply pair
+// over the whole grid.  Returns 0 for an unknown name.
+int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st) {
+  const Film* A = V.films;
+  const uint2* T = V.tiles;
+  const uint32_t nt = V.ntiles, nf = V.nfilms, fb = (nf + 127u) / 128u;
+  const dim3 b(16, 16);
   std::string_view n(name);
-#define CFK_T(K) \
-  (mode == CF_PREC_REFERENCE ? (void)K<CF_PREC_REFERENCE><<<g, b, 0, st>>>(F) : mode == CF_PREC_FP32 ? (void)K<CF_PREC_FP32><<<g, b, 0, st>>>(F) : (void)K<CF_PREC_BF16><<<g, b, 0, st>>>(F))
-  if (n == "mark_tiles") k_mark_tiles<<<g, b, 0, st>>>(F);
-  else if (n == "compact_tiles") { k_stats_reset<<<1, 1, 0, st>>>(F); k_compact_tiles<<<(nt + 255) / 256, 256, 0, st>>>(F, all_active); }
-  else if (n == "cure_step") { launch_compose(F, mode, 0, st); CFK_T(k_cure); }
-  else if (n == "clear_acc") k_clear_acc<<<g, b, 0, st>>>(F);
-  else if (n == "laplacian") k_laplacian<false><<<g, b, 0, st>>>(F);
-  else if (n == "plug") CFK_T(k_plug);
-  else if (n == "fluxes") CFK_T(k_fluxes);
-  else if (n == "limiter") k_limiter<<<g, b, 0, st>>>(F);
-  else if (n == "apply") CFK_T(k_apply);
+  if (n == "mark_tiles") kp_mark_tiles<<<(nt + 7u) / 8u, 256, 0, st>>>(A, T, nt);
+  else if (n == "compact_tiles") {
+    kp_stats_reset<<<fb, 128, 0, st>>>(A, nf);
+    kp_compact_tiles<<<(nt + 255u) / 256u, 256, 0, st>>>(A, T, nt);
+  }
+  else if (n == "cure_step") { launch_compose(V, mode, 0, st); launch_cure(V, mode, st); }
+  else if (n == "clear_acc") kp_clear_acc<<<nt, b, 0, st>>>(A, T, nt);
+  else if (n == "laplacian") kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+  else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
+  else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
+  else if (n == "limiter") kp_limiter<<<nt, b, 0, st>>>(A, T, nt);
+  else if (n == "apply") CFK_LAUNCH(kp_apply, nt, b, st, A, T, nt);
   else if (n == "nose") {
-    cudaMemcpyAsync(F.delta_old, F.delta, sizeof(uint32_t) * (size_t)F.w * F.h, cudaMemcpyDeviceToDevice, st);
-    k_nose<<<g, b, 0, st>>>(F);
+    kp_copy_delta<<<nt, b, 0, st>>>(A, T, nt);  // the snapshot the frame's apply takes
+    kp_nose<<<nt, b, 0, st>>>(A, T, nt);
   }
-  else if (n == "strata_split") CFK_T(k_strata_split);
-  else if (n == "reduce_tiles") launch_reduce(F, mode, st);
-  else if (n == "strata_limit") k_strata_limit<<<g, b, 0, st>>>(F);
+  else if (n == "strata_split") CFK_LAUNCH(kp_strata_split, nt, b, st, A, T, nt);
+  else if (n == "reduce_tiles") launch_reduce(V, mode, st);
+  else if (n == "strata_limit") kp_strata_limit<<<nt, b, 0, st>>>(A, T, nt);
   else if (n == "strata_pass") {
-    k_stats_reset<<<1, 1, 0, st>>>(F);
-    k_face_flags<<<g, b, 0, st>>>(F);
-    if (mode == CF_PREC_REFERENCE) strata_pass_t<CF_PREC_REFERENCE>(F, st);
-    else if (mode == CF_PREC_FP32) strata_pass_t<CF_PREC_FP32>(F, st);
-    else strata_pass_t<CF_PREC_BF16>(F, st);
+    kp_stats_reset<<<fb, 128, 0, st>>>(A, nf);
+    kp_face_flags<<<nt, b, 0, st>>>(A, T, nt);
+    CFK_LAUNCH(kp_strata_fast, nt, b, st, A, T, nt);
+    CFK_LAUNCH(kp_strata_full, V.persist_blocks, 256, st, A, nf);
+    CFK_LAUNCH(kp_strata_commit, V.persist_blocks, 256, st, A, nf);
+    return 2;
   }
-  else if (n == "strata_fill") { k_fill_select<<<g, b, 0, st>>>(F); CFK_T(k_fill_apply); }
-  else if (n == "shade_full") launch_compose(F, mode, 1, st);
+  else if (n == "strata_fill") {
+    kp_fill_select<<<nt, b, 0, st>>>(A, T, nt);
+    CFK_LAUNCH(kp_fill_apply, nt, b, st, A, T, nt);
+  }
+  else if (n == "shade_full") launch_compose(V, mode, 1, st);
   else return 0;
-#undef CFK_T
   return 1;
 }
 

@@ -7,15 +7,35 @@
 
 namespace cfk {
 
-// One frame of Film::encode_frame with `substeps` film substeps; swaps F's
-// strata generations; returns the number of kernel launches.
-uint32_t launch_frame(Film& F, int mode, uint32_t substeps, int all_active, cudaStream_t st);
-// Device-side adaptive dt and dt-dependent params from the last frame's stats.
-void launch_adaptive_params(DevParams* Dp, DevStats* S, cudaStream_t st);
-void launch_cure(const Film& F, int mode, cudaStream_t st);
+// What one launch of the frame kernels covers: the records of one or more
+// films of one precision mode and a table of all their 16x16 tiles.  A film
+// stepped alone is a view of its own two records and tiles; a batch is a view
+// of many films; both run the same compiled kernels, so a film's result does
+// not depend on what else shares the launch.
+struct PackedFrame {
+  const Film* films;       // device array: the films as the frame starts
+  const Film* films_next;  // the same films with the strata generations swapped
+  const uint2* tiles;      // entries (film index, 16x16 tile index)
+  uint32_t ntiles;
+  uint32_t nfilms;
+  uint32_t persist_blocks; // grid of the strata list kernels
+};
+
+// One frame of Film::encode_frame for every film of V with `substeps`
+// substeps (adaptive: each film's dt chosen on the device first, one
+// substep); returns the number of kernel launches.  The caller swaps each
+// film's generations afterwards (films_next is the next frame's films).
+uint32_t launch_frame_packed(const PackedFrame& V, int mode, uint32_t substeps, int adaptive, cudaStream_t st);
+// cure_step on its own (dry_now).
+void launch_cure(const PackedFrame& V, int mode, cudaStream_t st);
 // Composition aggregates (and, with shade, the colour) of the current state.
-void launch_compose(const Film& F, int mode, int shade, cudaStream_t st);
-void launch_reduce(const Film& F, int mode, cudaStream_t st);
+void launch_compose(const PackedFrame& V, int mode, int shade, cudaStream_t st);
+// Stats reset + the CFL reduction (h_max, mu_min) of the current state.
+void launch_reduce(const PackedFrame& V, int mode, cudaStream_t st);
+// A single named dispatch (inspection); 0: unknown name, 2: the caller swaps
+// the strata generations.
+int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st);
+
 void launch_mass(const Film& F, int sms, cudaStream_t st);
 void launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 // Pigments between the reference layout [cell][stratum][slot] (element
@@ -24,6 +44,5 @@ void launch_pig_import(const Film& F, int mode, uint4* chunks, const void* src, 
 void launch_pig_export(const Film& F, int mode, const uint4* chunks, void* dst, int fmt, cudaStream_t st);
 void launch_rheo_import(const Film& F, int mode, const float2* src, float n_global, size_t n, cudaStream_t st);
 void launch_rheo_export(const Film& F, int mode, float2* dst, size_t n, cudaStream_t st);
-int launch_one(Film& F, int mode, const char* name, int all_active, cudaStream_t st);
 
 }  // namespace cfk
