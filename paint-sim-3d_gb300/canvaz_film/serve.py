@@ -111,6 +111,11 @@ def _pct(xs, q):
 
 
 class Server:
+    """Films of retired jobs are kept per (side, precision) and reused by the
+    next job of that shape: admission is then a device-side clone into an
+    existing arena.  Idle films count against the budget and are freed when a
+    job of another shape needs the room."""
+
     def __init__(self, pool, budget_bytes, tuning=None, keep=None):
         self.pool = pool
         self.budget = int(budget_bytes)
@@ -119,10 +124,28 @@ class Server:
             self.batch.tuning = tuning
         self.keep = set(keep or ())   # job ids whose final state is read back
         self.results = {}
+        self.idle = {}                # (side, precision) -> [Film]
+        self.idle_bytes = 0
+
+    def fits(self, job, used):
+        """Whether the job can be admitted now (freeing idle films if needed)."""
+        key = (job.side, job.precision)
+        if self.idle.get(key):
+            return True
+        while used + self.idle_bytes + job.nbytes > self.budget and self.idle_bytes > 0:
+            k = max((k for k in self.idle if self.idle[k]), key=lambda k: capi.film_bytes(k[0], k[0], k[1]))
+            self.idle[k].pop().close()
+            self.idle_bytes -= capi.film_bytes(k[0], k[0], k[1])
+        return used + self.idle_bytes + job.nbytes <= self.budget
 
     def admit(self, job, now):
         src = self.pool.film(job.template, job.precision)
-        f = Film(src.settings, src.w, src.h, job.precision)
+        key = (job.side, job.precision)
+        if self.idle.get(key):
+            f = self.idle[key].pop()
+            self.idle_bytes -= job.nbytes
+        else:
+            f = Film(src.settings, src.w, src.h, job.precision)
         f.clone_from(src)
         job.film = f
         job.admit = now
@@ -135,7 +158,8 @@ class Server:
             st["color"] = job.film.color()
             self.results[job.jid] = st
         self.batch.remove(job.film)
-        job.film.close()
+        self.idle.setdefault((job.side, job.precision), []).append(job.film)
+        self.idle_bytes += job.nbytes
         job.film = None
 
     def run(self, jobs, max_wall_s=None):
@@ -143,6 +167,7 @@ class Server:
         pending = deque(sorted(jobs, key=lambda j: j.arrival))
         for j in pending:
             j.nbytes = capi.film_bytes(j.side, j.side, j.precision)
+        pending = deque(j for j in pending if j.nbytes <= self.budget)
         resident, done = [], []
         used = peak_used = peak_resident = 0
         admit_s = 0.0
@@ -153,15 +178,13 @@ class Server:
             if max_wall_s is not None and now > max_wall_s:
                 break
             ta = time.perf_counter()
-            while pending and pending[0].arrival <= now and used + pending[0].nbytes <= self.budget:
+            while pending and pending[0].arrival <= now and self.fits(pending[0], used):
                 j = pending.popleft()
-                if j.nbytes > self.budget:
-                    continue
                 self.admit(j, now)
                 resident.append(j)
                 used += j.nbytes
             admit_s += time.perf_counter() - ta
-            peak_used = max(peak_used, used)
+            peak_used = max(peak_used, used + self.idle_bytes)
             peak_resident = max(peak_resident, len(resident))
             if not resident:
                 if pending:
@@ -201,25 +224,41 @@ class Server:
 
     def close(self):
         self.batch.close()
+        for fs in self.idle.values():
+            for f in fs:
+                f.close()
+        self.idle, self.idle_bytes = {}, 0
 
 
-def plain_sequential(jobs, pool):
+def plain_sequential(jobs, pool, budget_s=None):
     """The same jobs one at a time in arrival order, each with single-film
-    launches (cf_encode_frame per step); Gcell-updates/s over the stepping."""
-    cell_steps, busy = 0, 0.0
+    launches (cf_encode_frame per step); Gcell-updates/s over the stepping.
+    With budget_s, stops once that much stepping time is spent (the last job
+    may be cut short)."""
+    cell_steps, busy, njobs = 0, 0.0, 0
     for j in sorted(jobs, key=lambda j: j.arrival):
         src = pool.film(j.template, j.precision)
         f = Film(src.settings, src.w, src.h, j.precision)
         f.clone_from(src)
         f.sync()
         t = time.perf_counter()
-        for _ in range(j.steps):
-            f.encode_frame(1)
+        done = 0
+        while done < j.steps:
+            k = min(16, j.steps - done)
+            for _ in range(k):
+                f.encode_frame(1)
+            done += k
+            if budget_s is not None and busy + time.perf_counter() - t > budget_s:
+                break
         f.sync()
         busy += time.perf_counter() - t
-        cell_steps += j.side * j.side * j.steps
+        cell_steps += j.side * j.side * done
+        njobs += 1
         f.close()
-    return {"gcell_updates_per_s": cell_steps / max(busy, 1e-12) / 1e9, "cell_steps": cell_steps, "busy_s": busy}
+        if budget_s is not None and busy > budget_s:
+            break
+    return {"gcell_updates_per_s": cell_steps / max(busy, 1e-12) / 1e9, "cell_steps": cell_steps, "busy_s": busy,
+            "jobs": njobs}
 
 
 def main():
@@ -227,17 +266,17 @@ def main():
     ap.add_argument("--duration", type=float, default=60.0, help="arrival window (s)")
     ap.add_argument("--rate", type=float, default=20.0, help="arrivals per second")
     ap.add_argument("--budget-gb", type=float, default=150.0)
-    ap.add_argument("--steps-scale", type=float, default=0.01, help="scales the 100-3000 step range")
+    ap.add_argument("--steps-scale", type=float, default=1.0, help="scales the 100-3000 step range")
     ap.add_argument("--sides", default="256,368,528,768,1104,1584,2048")
     ap.add_argument("--max-wall", type=float, default=None)
-    ap.add_argument("--sequential-jobs", type=int, default=24)
+    ap.add_argument("--sequential-seconds", type=float, default=30.0)
     args = ap.parse_args()
     pool = TemplatePool([int(s) for s in args.sides.split(",")])
     jobs = poisson_jobs(args.duration, args.rate, pool, steps_scale=args.steps_scale)
     srv = Server(pool, args.budget_gb * 1e9)
     rep = srv.run(jobs, args.max_wall)
     srv.close()
-    seq = plain_sequential(jobs[: args.sequential_jobs], pool)
+    seq = plain_sequential(jobs, pool, args.sequential_seconds)
     rep["plain_sequential_gcell_updates_per_s"] = seq["gcell_updates_per_s"]
     pool.close()
     print(json.dumps(rep))

@@ -179,7 +179,7 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, Add a
   add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
   add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n);
   add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
-  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, n);
+  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n);
   add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
 }
 
@@ -198,7 +198,8 @@ cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* byt
 }
 
 cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precision, cf_film** out) {
-  if (!s || !out || w == 0 || h == 0 || w > 65536 || h > 65536 || precision < 0 || precision > 2) {
+  if (!s || !out || w == 0 || h == 0 || w > 65536 || h > 65536 || (uint64_t)w * h > (1ull << 30) || precision < 0 ||
+      precision > 2) {
     g_create_err = "cf_create: invalid argument";
     return CF_ERR_INVALID_ARG;
   }

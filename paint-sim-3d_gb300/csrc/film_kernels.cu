@@ -277,18 +277,6 @@ __device__ __forceinline__ void plug_tile(const Film& F, TileId T) {
   F.tmp[c] = sum / mass;
 }
 
-// film.wgsl:448-455
-// Three blocks per SM: the face code needs no more than 64 registers, and
-// the occupancy hides its dependent loads.
-template <int MODE>
-__device__ __forceinline__ void fluxes_tile(const Film& F, TileId T) {
-  TILE_PROLOGUE
-  float q[4];
-#pragma unroll 1
-  for (int k = 0; k < 4; ++k) q[k] = face_k<MODE>(F, D, i, j, k).q;
-  F.flux[c] = make_float4(q[0], q[1], q[2], q[3]);
-}
-
 // film.wgsl:516-537
 __device__ __forceinline__ void limiter_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
@@ -444,30 +432,6 @@ __device__ __forceinline__ float4 band_split(const Film& F, uint32_t cu, float h
   return make_float4(fr[0] * total, fr[1] * total, fr[2] * total, fr[3] * total);
 }
 
-// film.wgsl:475-514 (acc_s face-major)
-template <int MODE>
-__device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
-  TILE_PROLOGUE
-  float4 a4 = F.acc[c];
-  float a[4] = {a4.x, a4.y, a4.z, a4.w};
-  const int ni[4] = {1, 0, 1, 1}, nj[4] = {0, 1, 1, -1};
-  bool ok[4] = {i + 1 < (int)F.w, j + 1 < (int)F.h, i + 1 < (int)F.w && j + 1 < (int)F.h, i + 1 < (int)F.w && j > 0};
-  uint32_t flags = 0u;
-#pragma unroll 1
-  for (int k = 0; k < 4; ++k) {
-    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a[k] != 0.f && ok[k]) {  // a face with no frame flux needs no recompute
-      FaceOut ff = face_k<MODE>(F, D, i, j, k);
-      uint32_t cb = idx(F, i + ni[k], j + nj[k]);
-      uint32_t cu = a[k] < 0.f ? cb : c;
-      o = band_split(F, cu, 0.5f * (F.hh[c] + F.hh[cb]), ff.y, ff.up, a[k], ff.n);
-      if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f) flags |= 1u << k;
-    }
-    F.acc_s[(size_t)k * F.n + c] = o;
-  }
-  F.fflags[c] = (uint8_t)flags;
-}
-
 // film.wgsl:1330-1361 over one 16x16 tile: the device-wide max / min the
 // adaptive step reads (order-independent, so the tile shape does not matter).
 template <int MODE>
@@ -544,7 +508,7 @@ __device__ __forceinline__ void face_flags_tile(const Film& F, TileId T) {
     float4 o = acc_face(F, c, k);
     if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f) flags |= 1u << k;
   }
-  F.fflags[c] = (uint8_t)flags;
+  F.fflags[c] = flags;
 }
 
 // Whether any of the 8 faces of active cell (i, j) carries a strata flux (the
@@ -588,6 +552,107 @@ __device__ __forceinline__ void list_append(uint32_t* list, uint32_t* count, uin
   if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
   base = __shfl_sync(m, base, leader);
   list[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
+// ---- face passes: fluxes and strata_split over the live faces of a tile ----
+// Face k of cell (i, j) joins cell (i + FACE_DI[k], j + FACE_DJ[k]).
+__device__ __constant__ int FACE_DI[4] = {1, 0, 1, 1};
+__device__ __constant__ int FACE_DJ[4] = {0, 1, 1, -1};
+
+// The block's faces that need evaluation, compacted in shared memory and
+// grouped by direction: a warp then evaluates 32 faces of (mostly) one
+// direction instead of 32 cells of which few have a live face, and no lane
+// waits on a dry neighbour.  Entries are cell positions within the tile.
+struct TileFaces {
+  uint8_t cell[4][256];
+  uint32_t count[4];
+};
+// Lists face k of this thread's cell when `live` (every thread of the block
+// calls this, with the same k).
+__device__ __forceinline__ void tile_faces_add(TileFaces& S, int k, bool live) {
+  const int tid = threadIdx.y * 16 + threadIdx.x, lane = tid & 31;
+  const unsigned m = __ballot_sync(0xffffffffu, live);
+  uint32_t base = 0;
+  if (lane == 0 && m) base = atomicAdd(&S.count[k], (uint32_t)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (live) S.cell[k][base + __popc(m & ((1u << lane) - 1u))] = (uint8_t)tid;
+}
+// Runs fn(k, i, j, c) for every listed face, the block's threads in turn.
+template <class Fn>
+__device__ __forceinline__ void tile_faces_each(const Film& F, TileId T, const TileFaces& S, Fn fn) {
+  const uint32_t n0 = S.count[0], n1 = n0 + S.count[1], n2 = n1 + S.count[2], n3 = n2 + S.count[3];
+  for (uint32_t e = threadIdx.y * 16 + threadIdx.x; e < n3; e += 256) {
+    const int k = e < n0 ? 0 : e < n1 ? 1 : e < n2 ? 2 : 3;
+    const uint32_t base = k == 0 ? 0u : k == 1 ? n0 : k == 2 ? n1 : n2;
+    const uint32_t t = S.cell[k][e - base];
+    const int i = (int)(T.x * 16 + (t & 15u)), j = (int)(T.y * 16 + (t >> 4));
+    fn(k, i, j, idx(F, i, j));
+  }
+}
+
+// fluxes (film.wgsl:448-455) for one tile: the active cells' flux is zeroed,
+// then the faces that face_k does not return zero for at once (the neighbour
+// in the grid and active, 0.5 (h_a + h_b) > 0) are evaluated.
+template <int MODE>
+__device__ __forceinline__ void fluxes_tile(const Film& F, TileId T) {
+  __shared__ TileFaces S;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  const bool in = i < (int)F.w && j < (int)F.h;
+  if (threadIdx.y == 0 && threadIdx.x < 4) S.count[threadIdx.x] = 0u;
+  __syncthreads();
+  const uint32_t c = in ? idx(F, i, j) : 0u;
+  const float hc = in ? F.hh[c] : 0.f;
+  if (in) F.flux[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int x = i + FACE_DI[k], y = j + FACE_DJ[k];
+    tile_faces_add(S, k, in && in_grid(F, x, y) && cell_active(F, x, y) && 0.5f * (hc + F.hh[idx(F, x, y)]) > 0.f);
+  }
+  __syncthreads();
+  const DevParams& D = *F.P;
+  float* fl = reinterpret_cast<float*>(F.flux);
+  tile_faces_each(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
+    fl[4 * (size_t)fc + k] = face_k<MODE>(F, D, fi, fj, k).q;
+  });
+}
+
+// strata_split (film.wgsl:475-514) for one tile: acc_s of the active cells
+// is zeroed, then every face with a frame flux is recomputed and its flux
+// split over the upstream cell's strata; the face flags are gathered in
+// shared memory.
+template <int MODE>
+__device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
+  __shared__ TileFaces S;
+  __shared__ uint32_t flags[256];
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const bool in = i < (int)F.w && j < (int)F.h;
+  if (tid < 4) S.count[tid] = 0u;
+  flags[tid] = 0u;
+  __syncthreads();
+  const uint32_t c = in ? idx(F, i, j) : 0u;
+  const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (in) F.acc_s[(size_t)k * F.n + c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    tile_faces_add(S, k, in && sel4(a4, k) != 0.f && in_grid(F, i + FACE_DI[k], j + FACE_DJ[k]));
+  }
+  __syncthreads();
+  const DevParams& D = *F.P;
+  tile_faces_each(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
+    const float a = sel4(F.acc[fc], k);
+    const FaceOut ff = face_k<MODE>(F, D, fi, fj, k);
+    const uint32_t cb = idx(F, fi + FACE_DI[k], fj + FACE_DJ[k]);
+    const uint32_t cu = a < 0.f ? cb : fc;
+    const float4 o = band_split(F, cu, 0.5f * (F.hh[fc] + F.hh[cb]), ff.y, ff.up, a, ff.n);
+    F.acc_s[(size_t)k * F.n + fc] = o;
+    if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f)
+      atomicOr(&flags[(fj - (int)T.y * 16) * 16 + (fi - (int)T.x * 16)], 1u << k);
+  });
+  __syncthreads();
+  if (in) F.fflags[c] = flags[tid];
 }
 
 __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm, float* ltab, int tid, int nthreads) {
@@ -1130,15 +1195,18 @@ template <bool CLEAR>
 __global__ void __launch_bounds__(256) kp_laplacian(PACKED_ARGS) { PACKED_TILE laplacian_tile<CLEAR>(F, T); }
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILE plug_tile<MODE>(F, T); }
+// three blocks per SM: the face code needs no more than 64 registers, and
+// the occupancy hides its dependent loads
 template <int MODE>
 __global__ void __launch_bounds__(256, 3) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
+template <int MODE>
+__global__ void __launch_bounds__(256, 3) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILE copy_delta_tile(F, T); }
 __global__ void __launch_bounds__(256) kp_nose(PACKED_ARGS) { PACKED_TILE nose_tile(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(256, 3) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
+
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILE reduce16_tile<MODE>(F, T); }
 template <int MODE>
