@@ -223,11 +223,11 @@ def drip_canvas(w, h, seed, n_lines=200, segs=(2, 6), width_cells=(2, 8), height
 
 
 def config(k, seed=0, scale=1):
-    """The workloads: 0 = 512^2 blobs, 1 = 2048^2 tilted drips,
-    2 = 4096^2 blobs over a cured ground.  `scale` divides the side (tests)."""
+    """The workloads: 0 = 512^2 blobs (K, S over 8 bands), 1 = 2048^2 tilted
+    drips, 2 = 4096^2 blobs over a cured ground.  `scale` divides the side."""
     if k == 0:
         s = 512 // scale
-        return blob_canvas(s, s, seed, n_blobs=20)
+        return blob_canvas(s, s, seed, n_blobs=20, nband=8)
     if k == 1:
         s = 2048 // scale
         return drip_canvas(s, s, seed, n_lines=max(200 // (scale * scale), 4))

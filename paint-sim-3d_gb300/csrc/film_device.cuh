@@ -328,7 +328,7 @@ __device__ __forceinline__ uint32_t feeders(const Film& F, const cf_params& P, u
   return n;
 }
 // film.wgsl:160-180
-__device__ inline float2 front_normal(const Film& F, const cf_params& P, uint32_t c) {
+static __device__ __noinline__ float2 front_normal(const Film& F, const cf_params& P, uint32_t c) {
   int i = (int)(c % F.w), j = (int)(c / F.w);
   float dx = 0.f, dy = 0.f;
 #pragma unroll
@@ -359,7 +359,7 @@ __device__ __forceinline__ float wet_gain(float2 n) {
   return 1.0f / (mm * fmaxf(w, 1e-3f));
 }
 // film.wgsl:203-222
-__device__ inline float front_shape(const Film& F, const cf_params& P, uint32_t c, float2 n) {
+static __device__ __noinline__ float front_shape(const Film& F, const cf_params& P, uint32_t c, float2 n) {
   int i = (int)(c % F.w), j = (int)(c / F.w);
   float w = 0.f, w0 = 0.f;
   for (int dj = -3; dj <= 3; ++dj)
@@ -396,7 +396,7 @@ __device__ __forceinline__ float cox_speed(const DevParams& D, float excess, flo
   return D.p.phys[1] * (th * th * th - adv * adv * adv) / (132.0f * fmaxf(mu, 1e-4f));
 }
 // film.wgsl:246-265
-__device__ inline float cell_excess(const Film& F, const cf_params& P, uint32_t c) {
+static __device__ __noinline__ float cell_excess(const Film& F, const cf_params& P, uint32_t c) {
   float e = F.hh[c] - hold_level(P, front_dist(F, c));
   int ox, oy;
   unpack_off(F.delta[c], ox, oy);
@@ -558,75 +558,54 @@ __device__ __forceinline__ float2 pres_wet(const Film& F, int i, int j, float2 f
   return make_float2(fb.x, p.y);
 }
 
-// film.wgsl:375-446, face k in {0: +x, 1: +y, 2: +x+y, 3: +x-y}
+// film.wgsl:375-446, face k in {0: +x, 1: +y, 2: +x+y, 3: +x-y}.  The
+// direction only selects the neighbour, the pressure-gradient stencil, the
+// tilt components and the weight; face() then runs once, so a kernel holds a
+// single copy of it.
 template <int MODE>
 __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k) {
   const cf_params& P = D.p;
   FaceOut z = {0.f, 0.f, 0.f, 0.f};
   const float s2 = 0.70710678f;
-  uint32_t c = idx(F, i, j);
-  float2 p00 = pres_at(F, i, j);
-  float2 gxy = make_float2(P.phys[0] * P.g[0], P.phys[0] * P.g[1]);
-  if (k == 0) {
-    if (!(i + 1 < (int)F.w && cell_active(F, i + 1, j))) return z;
-    uint32_t cb = idx(F, i + 1, j);
-    if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;  // face() is zero on a dry pair
-    float2 p10 = pres_at(F, i + 1, j);
-    float2 gm = make_float2(-(p10.x - p00.x) * P.inv_dx, -(p10.y - p00.y) * P.inv_dx);
-    float2 a = pres_wet(F, i, j + 1, p00), b = pres_wet(F, i + 1, j + 1, p10);
-    float2 cc = pres_wet(F, i, j - 1, p00), d = pres_wet(F, i + 1, j - 1, p10);
-    float2 pt = make_float2(a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y);
-    float2 gt = make_float2(-pt.x * 0.25f * P.inv_dx, -pt.y * 0.25f * P.inv_dx);
-    FaceOut f = face<MODE>(F, D, c, cb, make_float2(gm.x, gt.x), make_float2(gm.y, gt.y), gxy, false,
-                           make_float2(1.f, 0.f));
-    f.q *= W_AXIS;
-    return f;
-  }
-  if (k == 1) {
-    if (!(j + 1 < (int)F.h && cell_active(F, i, j + 1))) return z;
-    uint32_t cb = idx(F, i, j + 1);
-    if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;
-    float2 p01 = pres_at(F, i, j + 1);
-    float2 gm = make_float2(-(p01.x - p00.x) * P.inv_dx, -(p01.y - p00.y) * P.inv_dx);
-    float2 a = pres_wet(F, i + 1, j, p00), b = pres_wet(F, i + 1, j + 1, p01);
-    float2 cc = pres_wet(F, i - 1, j, p00), d = pres_wet(F, i - 1, j + 1, p01);
-    float2 pt = make_float2(a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y);
-    float2 gt = make_float2(-pt.x * 0.25f * P.inv_dx, -pt.y * 0.25f * P.inv_dx);
-    FaceOut f = face<MODE>(F, D, c, cb, make_float2(gm.x, gt.x), make_float2(gm.y, gt.y), make_float2(gxy.y, gxy.x),
-                           false, make_float2(0.f, 1.f));
-    f.q *= W_AXIS;
-    return f;
-  }
-  float hs = P.ein[3];
-  if (k == 2) {
-    if (!(i + 1 < (int)F.w && j + 1 < (int)F.h && cell_active(F, i + 1, j + 1))) return z;
-    uint32_t cb = idx(F, i + 1, j + 1);
-    if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;
-    float2 p11 = pres_at(F, i + 1, j + 1);
-    float2 ga = make_float2(-(p11.x - p00.x) * P.inv_dx * s2, -(p11.y - p00.y) * P.inv_dx * s2);
-    float2 pa = pres_wet(F, i + 1, j, p00), pb = pres_wet(F, i, j + 1, p11);
-    float2 gp = make_float2(-(pa.x - pb.x) * P.inv_dx * s2, -(pa.y - pb.y) * P.inv_dx * s2);
-    float2 gt = make_float2((gxy.x + gxy.y) * s2, (gxy.x - gxy.y) * s2);
-    bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j + 1)] > hs;
-    if (!open) return z;
-    FaceOut f = face<MODE>(F, D, c, cb, make_float2(ga.x, gp.x), make_float2(ga.y, gp.y), gt, true,
-                           make_float2(s2, s2));
-    f.q *= W_DIAG_FLUX;
-    return f;
-  }
-  if (!(i + 1 < (int)F.w && j > 0 && cell_active(F, i + 1, j - 1))) return z;
-  uint32_t cb = idx(F, i + 1, j - 1);
+  const bool diag = k >= 2;
+  const int di = k == 1 ? 0 : 1, dj = k == 0 ? 0 : (k == 3 ? -1 : 1);
+  const int x = i + di, y = j + dj;
+  if (!(in_grid(F, x, y) && cell_active(F, x, y))) return z;
+  const uint32_t c = idx(F, i, j), cb = idx(F, x, y);
   if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;  // face() is zero on a dry pair
-  float2 p1m = pres_at(F, i + 1, j - 1);
-  float2 ga = make_float2(-(p1m.x - p00.x) * P.inv_dx * s2, -(p1m.y - p00.y) * P.inv_dx * s2);
-  float2 pa = pres_wet(F, i + 1, j, p00), pb = pres_wet(F, i, j - 1, p1m);
-  float2 gp = make_float2(-(pa.x - pb.x) * P.inv_dx * s2, -(pa.y - pb.y) * P.inv_dx * s2);
-  float2 gt = make_float2((gxy.x - gxy.y) * s2, (gxy.x + gxy.y) * s2);
-  bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j - 1)] > hs;
-  if (!open) return z;
-  FaceOut f = face<MODE>(F, D, c, cb, make_float2(ga.x, gp.x), make_float2(ga.y, gp.y), gt, true,
-                         make_float2(s2, -s2));
-  f.q *= W_DIAG_FLUX;
+  const float2 p00 = pres_at(F, i, j), pb = pres_at(F, x, y);
+  const float2 gxy = make_float2(P.phys[0] * P.g[0], P.phys[0] * P.g[1]);
+  float2 gcap, ghyd, gt, fd;
+  float wgt;
+  if (!diag) {
+    // normal gradient across the face, tangential one from the 4 cells beside it
+    const int ti = k == 0 ? 0 : 1, tj = k == 0 ? 1 : 0;
+    const float2 gm = make_float2(-(pb.x - p00.x) * P.inv_dx, -(pb.y - p00.y) * P.inv_dx);
+    const float2 a = pres_wet(F, i + ti, j + tj, p00), b = pres_wet(F, x + ti, y + tj, pb);
+    const float2 cc = pres_wet(F, i - ti, j - tj, p00), d = pres_wet(F, x - ti, y - tj, pb);
+    const float2 pt = make_float2(a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y);
+    const float2 gtt = make_float2(-pt.x * 0.25f * P.inv_dx, -pt.y * 0.25f * P.inv_dx);
+    gcap = make_float2(gm.x, gtt.x);
+    ghyd = make_float2(gm.y, gtt.y);
+    gt = k == 0 ? gxy : make_float2(gxy.y, gxy.x);
+    fd = k == 0 ? make_float2(1.f, 0.f) : make_float2(0.f, 1.f);
+    wgt = W_AXIS;
+  } else {
+    const float2 ga = make_float2(-(pb.x - p00.x) * P.inv_dx * s2, -(pb.y - p00.y) * P.inv_dx * s2);
+    const float2 pa = pres_wet(F, i + 1, j, p00), pc = pres_wet(F, i, j + dj, pb);
+    const float2 gp = make_float2(-(pa.x - pc.x) * P.inv_dx * s2, -(pa.y - pc.y) * P.inv_dx * s2);
+    const float hs = P.ein[3];
+    const bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j + dj)] > hs;
+    if (!open) return z;
+    gcap = make_float2(ga.x, gp.x);
+    ghyd = make_float2(ga.y, gp.y);
+    gt = k == 2 ? make_float2((gxy.x + gxy.y) * s2, (gxy.x - gxy.y) * s2)
+                : make_float2((gxy.x - gxy.y) * s2, (gxy.x + gxy.y) * s2);
+    fd = make_float2(s2, k == 2 ? s2 : -s2);
+    wgt = W_DIAG_FLUX;
+  }
+  FaceOut f = face<MODE>(F, D, c, cb, gcap, ghyd, gt, diag, fd);
+  f.q *= wgt;
   return f;
 }
 

@@ -116,29 +116,12 @@ __device__ __forceinline__ void lnmu_table(const float* pigtab, float out[12]) {
   for (int q = 0; q < 12; ++q) out[q] = logf(fmaxf(pigtab[q * 40 + 32], 1e-3f));
 }
 
-// cure.wgsl:119-159 (full grid).  The pigment part of the composition comes
-// from agg (written by the last strata pass); the stack is only read when
-// the bottom stratum commits.
+// The commit of the bottom stratum into the relief (cure.wgsl:119-159), the
+// rare branch of cure_tile: out of line so that the common path keeps few
+// registers.
 template <int MODE>
-__device__ __forceinline__ void cure_tile(const Film& F, TileId T) {
-  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
-  if (i >= (int)F.w || j >= (int)F.h) return;
-  const uint32_t c = idx(F, i, j);
-  const cf_params& P = F.P->p;
-  float hv = F.hh[c];
-  if (hv <= 0.f) { set_rheo<MODE>(F, c, 1.f, 0.f, P.phys[2]); return; }
-  float rate = P.cure[0] * P.frame_dt;
-  float4 t4 = F.sh[c], c4 = F.scu[c];
-  float t[4] = {t4.x, t4.y, t4.z, t4.w}, u[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-  for (int k = 0; k < 4; ++k) u[k] = t[k] > 0.f ? fminf(u[k] + rate, 1.f) : u[k];
-  if (!(t[0] > 0.f && u[0] >= 1.f)) {
-    F.scu[c] = make_float4(u[0], u[1], u[2], u[3]);
-    float mu, ty, n;
-    rheo_from_parts(P, F.agg[c], t, u, mu, ty, n);
-    set_rheo<MODE>(F, c, mu, ty, n);
-    return;
-  }
+static __device__ __noinline__ void cure_commit(const Film& F, const cf_params& P, uint32_t c, float4 u4) {
+  const float u[4] = {u4.x, u4.y, u4.z, u4.w};
   Stack s;
   stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
 #pragma unroll
@@ -174,6 +157,31 @@ __device__ __forceinline__ void cure_tile(const Film& F, TileId T) {
   set_rheo<MODE>(F, c, mu, ty, n);
   stack_store<MODE>(F, F.sh, F.scu, F.pig, c, s);
   F.agg[c] = agg;
+}
+// cure.wgsl:119-159 (full grid).  The pigment part of the composition comes
+// from agg (written by the last strata pass); the stack is only read when
+// the bottom stratum commits.
+template <int MODE>
+__device__ __forceinline__ void cure_tile(const Film& F, TileId T) {
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const uint32_t c = idx(F, i, j);
+  const cf_params& P = F.P->p;
+  float hv = F.hh[c];
+  if (hv <= 0.f) { set_rheo<MODE>(F, c, 1.f, 0.f, P.phys[2]); return; }
+  float rate = P.cure[0] * P.frame_dt;
+  float4 t4 = F.sh[c], c4 = F.scu[c];
+  float t[4] = {t4.x, t4.y, t4.z, t4.w}, u[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) u[k] = t[k] > 0.f ? fminf(u[k] + rate, 1.f) : u[k];
+  if (!(t[0] > 0.f && u[0] >= 1.f)) {
+    F.scu[c] = make_float4(u[0], u[1], u[2], u[3]);
+    float mu, ty, n;
+    rheo_from_parts(P, F.agg[c], t, u, mu, ty, n);
+    set_rheo<MODE>(F, c, mu, ty, n);
+    return;
+  }
+  cure_commit<MODE>(F, P, c, make_float4(u[0], u[1], u[2], u[3]));
 }
 
 // film.wgsl:1427-1434
@@ -1189,7 +1197,7 @@ __device__ __forceinline__ void copy_delta_tile(const Film& F, TileId T) {
   const Film& F = films[pe_.x];        \
   const TileId T{pe_.y % F.tw, pe_.y / F.tw};
 template <int MODE>
-__global__ void __launch_bounds__(256) kp_cure(PACKED_ARGS) { PACKED_TILE cure_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256, 4) kp_cure(PACKED_ARGS) { PACKED_TILE cure_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_clear_acc(PACKED_ARGS) { PACKED_TILE clear_acc_tile(F, T); }
 template <bool CLEAR>
 __global__ void __launch_bounds__(256) kp_laplacian(PACKED_ARGS) { PACKED_TILE laplacian_tile<CLEAR>(F, T); }
