@@ -253,6 +253,27 @@ const char* cf_last_error(const cf_film* film);
  * function. */
 cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* bytes);
 
+/* --- display epilogue ------------------------------------------------------ */
+
+/* The Res uniform of the resolve pass (shaders/resolve.wgsl:4-8). */
+typedef struct cf_resolve_params {
+    float scale;        /* R.a.x: input scale                          */
+    float exposure_ev;  /* R.a.y: exposure in stops                    */
+    float bloom;        /* R.a.z: bloom strength (0 = off)             */
+    float grain;        /* R.a.w: film grain (0 = off)                 */
+    float vignette;     /* R.b.x                                       */
+    float sharpen;      /* R.c.x: (0 = off)                            */
+    int32_t agx;        /* R.b.w >= 0.5: AgX tone map, else ACES       */
+    int32_t reserved;
+} cf_resolve_params;
+
+/* The resolve fragment (shaders/resolve.wgsl:76-121: exposure, bloom,
+ * sharpen, vignette, AgX / ACES, grain, sRGB) over the film's colour plane,
+ * one pixel per cell, into rgba8_device (w x h x 4 bytes, device memory), on
+ * `stream`.  The reference runs it on the renderer's HDR image; here the
+ * film's linear RGB is the image (no graphics pipeline). */
+cf_status cf_resolve(cf_film* film, const cf_resolve_params* params, void* rgba8_device, void* stream);
+
 /* --- batches: many films stepped together -------------------------------- */
 
 /* A batch steps many films (canvases of any size) with one kernel launch per

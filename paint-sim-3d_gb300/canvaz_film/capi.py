@@ -94,6 +94,12 @@ class StateView(C.Structure):
     ]
 
 
+class ResolveParams(C.Structure):
+    """cf_resolve_params (the Res uniform of shaders/resolve.wgsl)."""
+    _fields_ = [("scale", C.c_float), ("exposure_ev", C.c_float), ("bloom", C.c_float), ("grain", C.c_float),
+                ("vignette", C.c_float), ("sharpen", C.c_float), ("agx", C.c_int32), ("reserved", C.c_int32)]
+
+
 class BatchTuning(C.Structure):
     """cf_batch_tuning."""
     _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
@@ -152,6 +158,7 @@ def load_library(path=None):
         "cf_cfl_stats_noalloc": ([vp, vp, u32, u32, f32, vp, vp], i32),
         "cf_film_bytes": ([u32, u32, i32, C.POINTER(C.c_uint64)], i32),
         "cf_clone_state": ([vp, vp, vp], i32),
+        "cf_resolve": ([vp, C.POINTER(ResolveParams), vp, vp], i32),
         "cf_batch_create": ([C.POINTER(vp)], i32),
         "cf_batch_destroy": ([vp], i32),
         "cf_batch_add": ([vp, vp], i32),

@@ -192,6 +192,14 @@ class Film:
         self._check(self.L.cf_read_color(self.p, out.ctypes.data_as(C.POINTER(C.c_uint16))), "cf_read_color")
         return out.view(np.float16).astype(np.float32)
 
+    def resolve(self, out_ptr, stream=None, **params):
+        """cf_resolve: the display epilogue of the colour plane into a device
+        buffer of w x h RGBA8 pixels at out_ptr."""
+        p = capi.ResolveParams(scale=1.0, exposure_ev=0.0, bloom=0.0, grain=0.0, vignette=0.0, sharpen=0.0, agx=1)
+        for k, v in params.items():
+            setattr(p, k, v)
+        self._check(self.L.cf_resolve(self.p, C.byref(p), out_ptr, stream), "cf_resolve")
+
     def color_device_ptr(self):
         p = C.c_void_p()
         self._check(self.L.cf_color_device_ptr(self.p, C.byref(p)), "cf_color_device_ptr")

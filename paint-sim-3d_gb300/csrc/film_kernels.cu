@@ -679,19 +679,10 @@ __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm
 // are shaded, as the reference's full-grid shade does.  Active wet cells left
 // without strata become strata_fill candidates.
 template <int MODE>
-__device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
-  __shared__ float tab[480];
-  __shared__ float cm[48];
-  __shared__ float ltab[12];
-  const int tid = threadIdx.y * 16 + threadIdx.x;
-  load_tables(F, tab, cm, ltab, tid, 256);
-  __syncthreads();
-  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
-  if (i >= (int)F.w || j >= (int)F.h) return;
-  const uint32_t c = idx(F, i, j);
-  const cf_params& P = F.P->p;
+__device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
+                                                 uint32_t c, float hc, const float* tab, const float* cm,
+                                                 const float* ltab) {
   const bool act = (F.tile_flags[T.x + T.y * F.tw] & ACTIVE) != 0u;
-  const float hc = F.hh[c];
   float4 t4 = F.sh[c], cu = F.scu[c];
   if (act) {
     const bool ft = flux_touched(F, i, j, c);
@@ -735,8 +726,45 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
       acc.ssum += nt[k];
     }
   }
-  F.agg[c] = acc.agg(P);
+  // the next cure reads the aggregates of wet cells only
+  if (hc > 0.f) F.agg[c] = acc.agg(P);
   F.color[c] = acc.color(P, cm, hc, F.m[c]);
+}
+// ... for one tile, together with the CFL reduction of reduce_tiles
+// (film.wgsl:1330-1361; the strata pass changes neither h nor mu, so the
+// order-independent max / min equal the reference's).
+template <int MODE>
+__device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
+  __shared__ float tab[480];
+  __shared__ float cm[48];
+  __shared__ float ltab[12];
+  __shared__ float red_h[8], red_m[8];
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  load_tables(F, tab, cm, ltab, tid, 256);
+  __syncthreads();
+  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
+  const cf_params& P = F.P->p;
+  float hm = 0.f, mm = 1e9f;
+  if (i < (int)F.w && j < (int)F.h) {
+    const uint32_t c = idx(F, i, j);
+    const float hc = F.hh[c];
+    if (hc > 4.0f * P.ein[3]) { hm = hc; mm = rmu<MODE>(F, c); }
+    strata_fast_cell<MODE>(F, P, T, i, j, c, hc, tab, cm, ltab);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    mm = fminf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
+  }
+  if ((tid & 31) == 0) { red_h[tid >> 5] = hm; red_m[tid >> 5] = mm; }
+  __syncthreads();
+  if (tid == 0) {
+#pragma unroll
+    for (int w = 1; w < 8; ++w) { hm = fmaxf(hm, red_h[w]); mm = fminf(mm, red_m[w]); }
+    if (hm > 0.f) {
+      atomicMax(&F.stats->h_max_bits, __float_as_uint(hm));
+      atomicMin(&F.stats->mu_min_bits, __float_as_uint(mm));
+    }
+  }
 }
 
 // strata.wgsl:175-188 with one cell per half-warp: the material that
@@ -1218,7 +1246,7 @@ __global__ void __launch_bounds__(256) kp_nose(PACKED_ARGS) { PACKED_TILE nose_t
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILE reduce16_tile<MODE>(F, T); }
 template <int MODE>
-__global__ void __launch_bounds__(256) kp_strata_fast(PACKED_ARGS) { PACKED_TILE strata_fast_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256, 3) kp_strata_fast(PACKED_ARGS) { PACKED_TILE strata_fast_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_strata_limit(PACKED_ARGS) { PACKED_TILE strata_limit_tile(F, T); }
 __global__ void __launch_bounds__(256) kp_face_flags(PACKED_ARGS) { PACKED_TILE face_flags_tile(F, T); }
 __global__ void __launch_bounds__(256) kp_fill_select(PACKED_ARGS) { PACKED_TILE fill_select_tile(F, T); }
@@ -1316,12 +1344,11 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
   }
   kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
   kp_strata_split<MODE><<<nt, b, 0, st>>>(A, T, nt);
-  kp_reduce<MODE><<<nt, b, 0, st>>>(A, T, nt);
-  kp_strata_fast<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  kp_strata_fast<MODE><<<nt, b, 0, st>>>(A, T, nt);  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_fill_list<MODE><<<nf, 1024, 0, st>>>(V.films_next, nf);
-  return n + 7;
+  return n + 6;
 }
 
 uint32_t launch_frame_packed(const PackedFrame& V, int mode, uint32_t substeps, int adaptive, cudaStream_t st) {
