@@ -179,7 +179,7 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, Add a
   add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
   add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n);
   add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
-  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n);
+  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n); add((void**)&F.dry_shaded, n);
   add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
 }
 
@@ -356,6 +356,7 @@ cf_status cf_set_tables(cf_film* f, const float* pigtab, const float* cmf) {
   if (!f || !pigtab || !cmf) return fail(f, CF_ERR_INVALID_ARG, "cf_set_tables: null");
   CUDA_TRY(f, cudaMemcpy(f->d_tables, pigtab, sizeof(float) * 480, cudaMemcpyHostToDevice));
   CUDA_TRY(f, cudaMemcpy(f->d_tables + 480, cmf, sizeof(float) * 48, cudaMemcpyHostToDevice));
+  CUDA_TRY(f, cudaMemset(f->F.dry_shaded, 0, f->n));  // dry colours depend on the CMF table
   return CF_OK;
 }
 
@@ -710,6 +711,7 @@ cf_status cf_debug_write(cf_film* f, const char* name, const void* host, size_t 
   PlaneRef r;
   if (!find_plane(f, name, r) || r.bytes != bytes) return fail(f, CF_ERR_INVALID_ARG, "plane name or size");
   CUDA_TRY(f, cudaDeviceSynchronize());
+  CUDA_TRY(f, cudaMemset(f->F.dry_shaded, 0, f->n));  // any plane may feed a colour
   std::string n(name);
   if (n == "strata_pig" || n == "strata_pig2") {
     void* tmp = nullptr;

@@ -115,6 +115,7 @@ struct Film {
   uint32_t* tile_moved;
   int32_t* fill_src;
   uint32_t* fflags;  // bit f: strata_split wrote a nonzero acc_s face f this frame
+  uint8_t* dry_shaded;  // 1: color holds the colour of a dry cell for the current sub_refl, m and cmf
   uint32_t* full_list;  // cells of the strata full path (DevStats::full_count)
   uint32_t* fill_list;  // strata fill candidates (DevStats::fill_count)
   uint32_t persist_blocks;  // grid of the list kernels: a few blocks per SM

@@ -713,6 +713,16 @@ __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params&
   }
   F.sh2[c] = make_float4(nt[0], nt[1], nt[2], nt[3]);
   F.scu2[c] = cu;
+  // A dry cell's colour depends on its substrate reflectance, its relief and
+  // the CMF table only (the stack and the params enter wet cells' colour),
+  // and those do not change while it stays dry: when the last shade already
+  // saw it dry, its colour is current.
+  if (hc <= 0.f) {
+    if (F.dry_shaded[c]) return;
+    F.dry_shaded[c] = 1u;
+  } else {
+    F.dry_shaded[c] = 0u;
+  }
   CellAcc acc;
   acc.begin(F.refl + (size_t)c * 16);
   const bool dbg = P.flags[0] == 1u;
@@ -905,6 +915,7 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     if (H.q == 0) {
       F.agg[c] = agg;
       F.color[c] = col;
+      F.dry_shaded[c] = hc <= 0.f ? 1u : 0u;
     }
   }
 }
@@ -970,6 +981,7 @@ __device__ __forceinline__ void fill_list_film(const Film& F, float* lt) {
       finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
       F.agg[c] = agg;
       F.color[c] = col;
+      F.dry_shaded[c] = hc <= 0.f ? 1u : 0u;
     }
     __syncthreads();
   }
@@ -1016,6 +1028,7 @@ __device__ __forceinline__ void fill_apply_tile(const Film& F, TileId T) {
   finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
   F.agg[c] = agg;
   F.color[c] = col;
+  F.dry_shaded[c] = hc <= 0.f ? 1u : 0u;
 }
 
 // Aggregates and colour of the current state (after a state upload, or for
@@ -1034,7 +1047,10 @@ __device__ __forceinline__ void compose_tile(const Film& F, TileId T, int shade)
   ushort4 col;
   finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, F.hh[c], F.m[c], s, agg, col);
   F.agg[c] = agg;
-  if (shade) F.color[c] = col;
+  if (shade) {
+    F.color[c] = col;
+    F.dry_shaded[c] = F.hh[c] <= 0.f ? 1u : 0u;
+  }
 }
 
 // FP64 mass / NaN census (compute_stats, src/main.rs:1679-1773)
