@@ -78,13 +78,17 @@ struct LaneStack {
   float pg[4];  // this lane's slot of each stratum
 };
 
-// pig_mix (strata.wgsl:45-60) for this lane's slot
+// pig_mix (strata.wgsl:45-60) for this lane's slot: slots 14 and 15
+// (ln mu + 10, flow index) mix over the carriers that have a value.  Every
+// lane runs the same instructions (selects, one fast division of at most 2
+// ulp): the half-warp does not split on the slot.
 __device__ __forceinline__ float lane_mix(int q, float a, float wa, float b, float wb) {
-  if (q >= 14) {
-    float va = a > 0.f ? wa : 0.f, vb = b > 0.f ? wb : 0.f;
-    return (va + vb > 0.f) ? (a * va + b * vb) / (va + vb) : 0.f;
-  }
-  return (a * wa + b * wb) / fmaxf(wa + wb, 1e-20f);
+  const bool carried = q >= 14;
+  const float va = (carried && !(a > 0.f)) ? 0.f : wa;
+  const float vb = (carried && !(b > 0.f)) ? 0.f : wb;
+  const float den = carried ? va + vb : fmaxf(wa + wb, 1e-20f);
+  const float r = __fdividef(a * va + b * vb, den);
+  return (carried && !(den > 0.f)) ? 0.f : r;
 }
 // pig_dist (strata.wgsl:37-43) over slots 0..12
 __device__ __forceinline__ float lane_dist(const HalfWarp& H, float a, float b) {
@@ -101,7 +105,7 @@ __device__ __forceinline__ uint32_t lane_count(const LaneStack& s) {  // strata.
 __device__ __forceinline__ void lane_merge(const HalfWarp& H, LaneStack& s, int a) {
   const float ta = get4(s.th, a), tb = get4(s.th, a + 1);
   const float pm = lane_mix(H.q, get4(s.pg, a), ta, get4(s.pg, a + 1), tb);
-  const float cm = (get4(s.cu, a) * ta + get4(s.cu, a + 1) * tb) / fmaxf(ta + tb, 1e-20f);
+  const float cm = __fdividef(get4(s.cu, a) * ta + get4(s.cu, a + 1) * tb, fmaxf(ta + tb, 1e-20f));
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     if (k == a) {
@@ -147,7 +151,7 @@ __device__ __forceinline__ void lane_push_top(const HalfWarp& H, LaneStack& s, f
     const bool close = lane_dist(H, pt, pin) < close_d || tt < tiny;
     if (close) {
       set4(s.pg, t, lane_mix(H.q, pt, tt, pin, vol));
-      set4(s.cu, t, (get4(s.cu, t) * tt + cv * vol) / (tt + vol));
+      set4(s.cu, t, __fdividef(get4(s.cu, t) * tt + cv * vol, tt + vol));
       set4(s.th, t, tt + vol);
       return;
     }
@@ -180,10 +184,10 @@ __device__ __forceinline__ void lane_add_band(const HalfWarp& H, LaneStack& s, f
     if (tk <= 0.f) break;
     const float z1 = z0 + tk;
     const float ov = fmaxf(fminf(zhi, z1) - fmaxf(zlo, z0), 0.f);
-    const float part = vol * ov / span;
+    const float part = vol * ov / span;  // exact: `above` below is compared with 1e-14
     if (part > 0.f) {
       s.pg[k] = lane_mix(H.q, s.pg[k], tk, pin, part);
-      s.cu[k] = (s.cu[k] * tk + cv * part) / (tk + part);
+      s.cu[k] = __fdividef(s.cu[k] * tk + cv * part, tk + part);
       s.th[k] = tk + part;
       above -= part;
     }
