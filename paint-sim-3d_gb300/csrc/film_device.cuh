@@ -616,15 +616,17 @@ __device__ __forceinline__ void km_layer(float k, float s, float t, float& r, fl
   float bs = sqrtf(fmaxf(k * (k + 2.0f * s), 0.f));
   float arg = fminf(bs * t, 20.0f);
   float e = expf(arg);
-  float sh = 0.5f * (e - 1.0f / e);
-  float ch = 0.5f * (e + 1.0f / e);
+  const float ie = __frcp_rn(e);  // e >= 1: a correctly rounded reciprocal
+  float sh = 0.5f * (e - ie);
+  float ch = 0.5f * (e + ie);
   float den = (k + s) * sh + bs * ch;
   if (den < 1e-12f) { r = 0.f; tr = 1.f; return; }
-  r = s * sh / den;
-  tr = bs / den;
+  const float iden = __frcp_rn(den);
+  r = s * sh * iden;
+  tr = bs * iden;
 }
 __device__ __forceinline__ float composite(float r, float t, float rb) {  // km.wgsl:13-15
-  return r + t * t * rb / fmaxf(1.0f - r * rb, 1e-4f);
+  return r + __fdividef(t * t * rb, fmaxf(1.0f - r * rb, 1e-4f));
 }
 
 }  // namespace cfk

@@ -264,7 +264,7 @@ struct CellAcc {
     float X = 0.f, Y = 0.f, Z = 0.f;
 #pragma unroll
     for (int b = 0; b < 16; ++b) {
-      float rb = (1.0f - k1) * (1.0f - k2) * r[b] / fmaxf(1.0f - k2 * r[b], 1e-3f);
+      float rb = __fdividef((1.0f - k1) * (1.0f - k2) * r[b], fmaxf(1.0f - k2 * r[b], 1e-3f));  // colour is stored as f16
       X += rb * cm[3 * b];
       Y += rb * cm[3 * b + 1];
       Z += rb * cm[3 * b + 2];

@@ -267,7 +267,7 @@ struct LaneAcc {
     const float k1 = 0.04f;
     const float wt = hv > 0.f ? wet : 0.f;
     const float k2 = 0.4f * (1.0f - wt) + 0.6f * wt;
-    const float rb = (1.0f - k1) * (1.0f - k2) * r / fmaxf(1.0f - k2 * r, 1e-3f);
+    const float rb = __fdividef((1.0f - k1) * (1.0f - k2) * r, fmaxf(1.0f - k2 * r, 1e-3f));  // colour is stored as f16
     const float X = H.sum(rb * cm[3 * H.q]), Y = H.sum(rb * cm[3 * H.q + 1]), Z = H.sum(rb * cm[3 * H.q + 2]);
     float rgb[3] = {3.2406f * X - 1.5372f * Y - 0.4986f * Z, -0.9689f * X + 1.8758f * Y + 0.0415f * Z,
                     0.0557f * X - 0.2040f * Y + 1.0570f * Z};
