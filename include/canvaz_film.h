@@ -253,6 +253,32 @@ const char* cf_last_error(const cf_film* film);
  * function. */
 cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* bytes);
 
+/* --- painting files (src/session.rs) ----------------------------------------- */
+
+/* The header fields of a Canvaz painting file (src/session.rs:248-310). */
+typedef struct cf_snapshot_info {
+    uint32_t w, h;
+    float tilt_deg, tilt_dir_deg, cure_rate, h_max, s_max;
+    double total_deposited;
+} cf_snapshot_info;
+
+/* App::save_painting's bytes (src/session.rs:248-266: "PSIM", version 1,
+ * w, h, the five header floats, total_deposited, then pack() of the eight
+ * read_state planes in 32 MiB LZ4 chunks, src/session.rs:58-74).  The film's
+ * w and h are written; info supplies the other header fields.  *out is
+ * allocated by the library: release it with cf_snapshot_free. */
+cf_status cf_snapshot_save(cf_film* film, const cf_snapshot_info* info, uint8_t** out, uint64_t* len);
+cf_status cf_snapshot_free(uint8_t* buf);
+/* App::open_painting (src/session.rs:277-310): checks magic, version and
+ * canvas size, unpacks (src/session.rs:76-99) and writes the state
+ * (write_state); fills info (may be NULL) from the header. */
+cf_status cf_snapshot_load(cf_film* film, const uint8_t* data, uint64_t len, cf_snapshot_info* info);
+/* The chunk coder of the painting file (lz4_flex 0.11 compress_prepend_size /
+ * decompress_size_prepended): a u32 uncompressed size, then an LZ4 block.
+ * Host functions.  cf_lz4_decompress with dst NULL only reports the size. */
+cf_status cf_lz4_compress(const uint8_t* src, uint64_t n, uint8_t* dst, uint64_t cap, uint64_t* out_len);
+cf_status cf_lz4_decompress(const uint8_t* src, uint64_t n, uint8_t* dst, uint64_t cap, uint64_t* out_len);
+
 /* --- display epilogue ------------------------------------------------------ */
 
 /* The Res uniform of the resolve pass (shaders/resolve.wgsl:4-8). */

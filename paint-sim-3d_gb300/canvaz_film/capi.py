@@ -100,6 +100,12 @@ class ResolveParams(C.Structure):
                 ("vignette", C.c_float), ("sharpen", C.c_float), ("agx", C.c_int32), ("reserved", C.c_int32)]
 
 
+class SnapshotInfo(C.Structure):
+    """cf_snapshot_info: the painting-file header fields (src/session.rs:248-310)."""
+    _fields_ = [("w", C.c_uint32), ("h", C.c_uint32), ("tilt_deg", C.c_float), ("tilt_dir_deg", C.c_float),
+                ("cure_rate", C.c_float), ("h_max", C.c_float), ("s_max", C.c_float), ("total_deposited", C.c_double)]
+
+
 class BatchTuning(C.Structure):
     """cf_batch_tuning."""
     _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
@@ -159,6 +165,11 @@ def load_library(path=None):
         "cf_film_bytes": ([u32, u32, i32, C.POINTER(C.c_uint64)], i32),
         "cf_clone_state": ([vp, vp, vp], i32),
         "cf_resolve": ([vp, C.POINTER(ResolveParams), vp, vp], i32),
+        "cf_snapshot_save": ([vp, C.POINTER(SnapshotInfo), C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_uint64)], i32),
+        "cf_snapshot_free": ([C.POINTER(C.c_uint8)], i32),
+        "cf_snapshot_load": ([vp, C.c_char_p, C.c_uint64, C.POINTER(SnapshotInfo)], i32),
+        "cf_lz4_compress": ([C.c_char_p, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)], i32),
+        "cf_lz4_decompress": ([C.c_char_p, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)], i32),
         "cf_batch_create": ([C.POINTER(vp)], i32),
         "cf_batch_destroy": ([vp], i32),
         "cf_batch_add": ([vp, vp], i32),

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .capi import BatchTuning, FilmError, Params, Settings, StateView, Stats
+from .capi import BatchTuning, FilmError, Params, Settings, SnapshotInfo, StateView, Stats
 
 _f32p = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
 
@@ -152,6 +152,26 @@ class Film:
         """cf_clone_state: src's whole device state into this film (same size
         and precision), stream-ordered, no host round trip."""
         self._check(self.L.cf_clone_state(self.p, src.p, stream), "cf_clone_state")
+
+    def save_snapshot(self, **header):
+        """App::save_painting's bytes (cf_snapshot_save); header fields:
+        tilt_deg, tilt_dir_deg, cure_rate, h_max, s_max, total_deposited."""
+        info = SnapshotInfo(w=self.w, h=self.h, tilt_deg=self.settings.tilt_deg,
+                            tilt_dir_deg=self.settings.tilt_dir_deg, cure_rate=self.settings.cure_rate)
+        for k, v in header.items():
+            setattr(info, k, v)
+        buf, n = C.POINTER(C.c_uint8)(), C.c_uint64()
+        self._check(self.L.cf_snapshot_save(self.p, C.byref(info), C.byref(buf), C.byref(n)), "cf_snapshot_save")
+        try:
+            return C.string_at(buf, n.value)
+        finally:
+            self.L.cf_snapshot_free(buf)
+
+    def load_snapshot(self, data):
+        """App::open_painting (cf_snapshot_load); returns the header fields."""
+        info = SnapshotInfo()
+        self._check(self.L.cf_snapshot_load(self.p, data, len(data), C.byref(info)), "cf_snapshot_load")
+        return {k: getattr(info, k) for k, _ in SnapshotInfo._fields_}
 
     def update_params(self, frame_dt, substeps):
         self._check(self.L.cf_update_params(self.p, frame_dt, substeps), "cf_update_params")
