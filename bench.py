@@ -22,6 +22,7 @@ Multi-GPU: one replica canvas per rank (independent canvases; no collective
 on the data path), `value` = all ranks' cell-updates / max time.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -64,6 +65,13 @@ PREC_NAME = {capi.CF_PREC_FP32: "f32", capi.CF_PREC_REFERENCE: "f32+f16pig", cap
 # and config 4, the Poisson-served stream.
 BATCH_WORKLOAD = "batch64_dt1e-3_fp32"
 SERVE_WORKLOAD = "serve_poisson20_fp32bf16"
+# The deposit rasteriser alone: 4096 strokes per step onto a 4096^2 FP32 film.
+DEPOSIT_WORKLOAD = "deposit4096_strokes4096_fp32"
+# Compulsory bytes per cell that receives paint (FP32 storage): reads h, m,
+# strata_h, strata_cure, 64 f32 pigment slots, 16 f16 substrate bands;
+# writes h, strata_h, strata_cure, pigments, lay, the dry bit and the
+# composition aggregates.
+DEPOSIT_BYTES_PER_CELL = (4 + 4 + 16 + 16 + 256 + 32) + (4 + 16 + 16 + 256 + 4 + 1 + 16)
 
 
 def parse():
@@ -73,7 +81,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD])
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, DEPOSIT_WORKLOAD])
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="arrival window of the served workload")
     ap.add_argument("--serve-wall", type=float, default=60.0, help="wall-clock cut-off of the served run")
     ap.add_argument("--serve-steps-scale", type=float, default=1.0, help="scales the served 100-3000 step range")
@@ -192,10 +200,160 @@ def cpu_baseline(cv, workload, budget_s, steps_hint=3):
             % (n, cv.w, cv.h, os.cpu_count(), el)}
 
 
+def deposit_strokes(n, side_m, dx, seed):
+    """n strokes / capsules (radius 1.5-6 cells, length 0-40 cells, random
+    pigments and laying method) built by the library's Deposit constructors."""
+    from canvaz_film import deposit as dep
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(0.01, 0.99, (n, 2)) * side_m
+    ang = rng.uniform(0, 2 * np.pi, n)
+    ln = rng.uniform(0, 40, n) * dx
+    b = a + ln[:, None] * np.stack([np.cos(ang), np.sin(ang)], 1)
+    r = rng.uniform(1.5, 6.0, n) * dx
+    pig = np.zeros((n, 16))
+    pig[:, :12] = rng.dirichlet(np.full(12, 0.5), n)
+    pig[:, 13] = rng.uniform(0.5, 2.0, n)
+    method = rng.integers(1, 7, n)
+    out = np.zeros(n, dep.DEPOSIT_DTYPE)
+    for k in range(n):
+        vol = float(np.pi * r[k] * r[k] * (ln[k] + r[k]) * 0.3)
+        ctor = dep.capsule if k % 3 == 0 else dep.stroke
+        d = ctor(a[k], b[k], float(r[k]), vol, dep.pack_pig(pig[k]), float(dx))
+        d["kind"] |= int(method[k]) << dep.METHOD_SHIFT
+        out[k] = d
+    return out
+
+
+def tiles_touched(deps, side, dx):
+    """Entries of the 64x64-cell tile lists a set of deposits makes (each
+    deposit is listed in every tile its bounding box touches)."""
+    rb = np.maximum(deps["r0"], deps["r1"])
+    tile = 64 * float(dx)
+    lo = np.floor((np.minimum(deps["p0"], deps["p1"]) - rb[:, None]) / tile).clip(0, side // 64 - 1)
+    hi = np.floor((np.maximum(deps["p0"], deps["p1"]) + rb[:, None]) / tile).clip(0, side // 64 - 1)
+    return int(np.prod(hi - lo + 1, axis=1).sum())
+
+
+DEPOSIT_SIDE, DEPOSIT_COUNT, DEPOSIT_SETS = 4096, 4096, 4
+DEPOSIT_CPU_SIDE = 1024  # CPU sample: the same stroke density on a 1024^2 film
+
+
+def deposit_cpu(budget_s, threads_note=True):
+    """The oracle's FP32 deposit pass (run_deposit, OpenMP over rows) on a
+    1024^2 film with 256 strokes per launch (the workload's density)."""
+    import pyoracle as po
+    po.build()
+    side = DEPOSIT_CPU_SIDE
+    st = capi.Settings.default(width_m=side * 1e-3, height_m=side * 1e-3)
+    cv = synth.blob_canvas(16, 16, 1, n_blobs=1, tables="reference")
+    o = po.Oracle(side, side, st, capi.CF_PIG_F32, 32)
+    o.set_tables(cv.pigtab, cv.cmf)
+    n = DEPOSIT_COUNT * side * side // (DEPOSIT_SIDE * DEPOSIT_SIDE)
+    sets = [deposit_strokes(n, side * 1e-3, np.float32(1e-3), 100 + k) for k in range(2)]
+    el, launches = 0.0, 0
+    while True:
+        o.upload_deposits(sets[launches % 2])
+        t0 = time.perf_counter()
+        o.run("deposit")
+        el += time.perf_counter() - t0
+        launches += 1
+        if el > budget_s or launches >= 200:
+            break
+    return {"value": n * launches / el / 1e6, "unit": "Mdeposits/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d launches of %d strokes on a %dx%d FP32 film (the %dx%d workload's stroke density), "
+                      "oracle run_deposit, OpenMP %d threads, %.1f s" % (launches, n, side, side, DEPOSIT_SIDE,
+                                                                          DEPOSIT_SIDE, os.cpu_count(), el)}
+
+
+def deposit_arm(args):
+    """The deposit rasteriser on one GPU: every step uploads one set of 4096
+    strokes (cf_upload_deposits: host binning + copies) and lays it
+    (cf_lay_deposits).  `value` = strokes per second of device time (CUDA
+    events around each launch); `e2e` = strokes per second of the whole
+    upload + lay + cf_get_stats (device -> host) loop."""
+    import torch
+    from canvaz_film.film import Film
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    side = DEPOSIT_SIDE
+    dx = np.float32(1e-3)
+    st = capi.Settings.default(width_m=side * 1e-3, height_m=side * 1e-3)
+    cv = synth.blob_canvas(16, 16, 1, n_blobs=1, tables="reference")
+    film = Film(st, side, side, capi.CF_PREC_FP32)
+    film.set_tables(cv.pigtab, cv.cmf)
+    sets = [deposit_strokes(DEPOSIT_COUNT, side * 1e-3, dx, 10 * rank + k) for k in range(DEPOSIT_SETS)]
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    # cells one launch paints (first set on the bare film)
+    film.upload_deposits(sets[0])
+    film.lay_deposits(sh)
+    torch.cuda.synchronize()
+    covered = int(np.count_nonzero(film.plane("h")))
+    for k in range(args.warmup):
+        film.upload_deposits(sets[k % DEPOSIT_SETS])
+        film.lay_deposits(sh)
+    torch.cuda.synchronize()
+    l0 = film.stats()["launches"]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            film.upload_deposits(sets[k % DEPOSIT_SETS])
+            evs[k][0].record(stream)
+            film.lay_deposits(sh)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    t = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    launches = film.stats()["launches"] - l0
+    value = DEPOSIT_COUNT * args.steps / t / 1e6
+    peak, peak_kind = peaks()
+    achieved = DEPOSIT_BYTES_PER_CELL * covered * args.steps / t / 1e9
+    e2e = None
+    if args.e2e_steps > 0:
+        pinned = [torch.from_numpy(s.view(np.uint8)).pin_memory().numpy().view(s.dtype) for s in sets]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.e2e_steps):
+            film.upload_deposits(pinned[k % DEPOSIT_SETS])
+            film.lay_deposits(sh)
+            film.stats()
+        te = time.perf_counter() - t0
+        items = float(np.mean([tiles_touched(s_, side, dx) for s_ in sets]))
+        e2e = {"value": DEPOSIT_COUNT * args.e2e_steps / te / 1e6, "unit": "Mdeposits/s",
+               "h2d_bytes_per_step": int(96 * DEPOSIT_COUNT + 8 * (side // 64) ** 2 + 4 * items),
+               "d2h_bytes_per_step": int(ctypes.sizeof(capi.Stats)),
+               "steps": args.e2e_steps, "path": "cf_upload_deposits(host records) + cf_lay_deposits + cf_get_stats"}
+    cb = None if args.no_cpu_baseline else deposit_cpu(args.cpu_seconds)
+    line = {
+        "metric": "Mdeposits/s", "value": value, "unit": "Mdeposits/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded strokes and capsules)",
+        "config": {"workload": DEPOSIT_WORKLOAD, "w": side, "h": side, "strokes_per_step": DEPOSIT_COUNT,
+                   "cells_painted_per_step": covered, "precision": "f32",
+                   "l2": "each step paints new cells of a 4096^2 film (9.9 GB of state): no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "alg_bytes_per_painted_cell": DEPOSIT_BYTES_PER_CELL,
+                     "scope": "k_deposit", "traffic": None},
+        "gpu_launches": int(launches), "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(args):
     """CPU reference path, same workload / metric / unit; rank 0 only."""
     rank, world, _ = dist_env()
     if rank != 0:
+        return
+    if args.workload == DEPOSIT_WORKLOAD:
+        cb = deposit_cpu(min(150.0, 10.0 * (args.steps + args.warmup)))
+        print(json.dumps({"impl": "reference", "metric": "Mdeposits/s", "value": cb["value"], "unit": "Mdeposits/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                          "config": {"workload": args.workload}, "cpu_baseline": cb,
+                          "e2e": {"value": cb["value"], "unit": "Mdeposits/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
         return
     workload = args.workload if args.workload in WORKLOADS else "blobs512_dt1e-3_fp32"  # batch / served: same physics
     gen, prec, dt_max, adaptive = WORKLOADS[workload]
@@ -489,6 +647,8 @@ def main():
         batch_arm(args)
     elif args.workload == SERVE_WORKLOAD:
         serve_arm(args)
+    elif args.workload == DEPOSIT_WORKLOAD:
+        deposit_arm(args)
     else:
         gpu_arm(args)
 

@@ -253,6 +253,49 @@ const char* cf_last_error(const cf_film* film);
  * function. */
 cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* bytes);
 
+/* --- deposits: paint laid on the film ------------------------------------------ */
+
+/* Deposit (src/film/mod.rs:25-39): a ribbon segment p0 -> p1 with end
+ * normals n0, n1 and radii r0, r1 (metres), peak height h0, volume vol, kind
+ * (bit 0 recycled, bit 1 cap start, bit 2 cap end, bits 8+ laying method) and
+ * 16 pigment slots packed as f16 pairs.  96 bytes, the reference's layout. */
+typedef struct cf_deposit {
+    float p0[2], p1[2], n0[2], n1[2];
+    float r0, r1, h0, vol;
+    uint32_t kind;
+    uint32_t pad[3];
+    uint32_t pig[8];
+} cf_deposit;
+
+/* Deposit::ribbon / capsule / stroke (src/film/mod.rs:63-93): h0 is set so
+ * that the profile sampled on a 0.25 dx lattice holds `volume`.  Host
+ * functions; f32 arithmetic in the reference's order. */
+cf_status cf_deposit_ribbon(const float p0[2], const float p1[2], const float n0[2], const float n1[2], float r0,
+                            float r1, uint32_t caps, float volume, const uint32_t pig[8], float dx, cf_deposit* out);
+cf_status cf_deposit_capsule(const float p0[2], const float p1[2], float r, float volume, const uint32_t pig[8],
+                             float dx, cf_deposit* out);
+cf_status cf_deposit_stroke(const float p0[2], const float p1[2], float r, float volume, const uint32_t pig[8],
+                            float dx, cf_deposit* out);
+/* Deposit::sampled_volume and the profile height (src/film/mod.rs:115-185). */
+cf_status cf_deposit_sampled_volume(const cf_deposit* d, float lattice, float* out);
+cf_status cf_deposit_height_at(const cf_deposit* d, const float p[2], float* out);
+/* upload_deposits (src/film/mod.rs:1175-1224): bins the first
+ * min(count, CF_MAX_DEPOSITS) deposits into the film's 64x64-cell tiles
+ * (at most 16 tile entries per deposit in all); the next frame
+ * (cf_encode_frame, cf_step_adaptive or a batch step) lays them
+ * (shaders/deposit.wgsl) before its mark_tiles.  *sent (may be NULL) gets the
+ * number taken; the caller holds the rest for the next frame, as
+ * src/main.rs:1882-1890 does.  *total_deposited (may be NULL) gets the running
+ * volume laid inside the canvas.  Synchronous with the device. */
+#define CF_MAX_DEPOSITS 65536u
+cf_status cf_upload_deposits(cf_film* film, const cf_deposit* deps, uint32_t count, uint32_t* sent,
+                             double* total_deposited);
+/* Lays the uploaded deposits now, enqueued on `stream`, instead of at the
+ * start of the next frame (no counterpart in the reference, which lays them
+ * only inside Film::encode_frame; used where paint is laid while the film is
+ * not stepped).  No-op when none are pending.  Asynchronous. */
+cf_status cf_lay_deposits(cf_film* film, void* stream);
+
 /* --- painting files (src/session.rs) ----------------------------------------- */
 
 /* The header fields of a Canvaz painting file (src/session.rs:248-310). */

@@ -31,7 +31,8 @@ cf_status cf_debug_read(cf_film* film, const char* name, void* host, size_t byte
 cf_status cf_debug_write(cf_film* film, const char* name, const void* host, size_t bytes);
 
 /* Runs one dispatch of Film::encode_frame by its WGSL entry-point name
- * ("laplacian", "fluxes", "strata_update", "shade_full", ...). */
+ * ("laplacian", "fluxes", "strata_update", "shade_full", ...; "deposit" lays
+ * the deposits uploaded since the last frame and drops them). */
 cf_status cf_debug_run(cf_film* film, const char* kernel, void* stream);
 
 /* Overwrites the device params with `params` (no re-packing). */

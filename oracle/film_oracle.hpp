@@ -1438,9 +1438,11 @@ struct Film {
         hmx = std::max(hmx, hm);
         mmn = std::min(mmn, mm);
       }
-    // poll_stats (src/film/mod.rs:944-953)
+    // poll_stats (src/film/mod.rs:944-968): the pending deposit height is
+    // forgotten once stats that include the deposits arrive
     h_max_stat = (float)hmx;
     mu_min_stat = mmn > F(1e8f) ? 1.0f : (float)mmn;
+    if (dep_items.empty()) h_max_pending = 0.0f;
   }
 
   // ---- dispatch helpers ----
@@ -1492,9 +1494,108 @@ struct Film {
     for (long c = 0; c < (long)N; ++c) k_shade_cell((size_t)c);
   }
 
+  // ---- deposits (shaders/deposit.wgsl; tables binned by upload_deposits,
+  // src/film/mod.rs:1175-1224, on the host) ----
+  std::vector<cf_deposit> deps;
+  std::vector<uint32_t> dep_start, dep_count, dep_items;  // per 64x64-cell tile
+
+  // deposit.wgsl:6-29; mix(a, b, t) = a (1 - t) + b t as WGSL defines it
+  static R ribbon_height(R px, R py, const cf_deposit& d) {
+    R abx = (R)d.p1[0] - (R)d.p0[0], aby = (R)d.p1[1] - (R)d.p0[1];
+    R l2 = abx * abx + aby * aby;
+    R r0 = d.r0, r1 = d.r1, h0 = d.h0;
+    if (l2 <= 0) {
+      R qx = px - (R)d.p0[0], qy = py - (R)d.p0[1];
+      R x = std::sqrt(qx * qx + qy * qy) / r0;
+      return x < 1 ? h0 * (1 - x * x) : R(0);
+    }
+    R l = std::sqrt(l2);
+    R ux = abx / l, uy = aby / l;
+    R q0x = px - (R)d.p0[0], q0y = py - (R)d.p0[1], q1x = px - (R)d.p1[0], q1y = py - (R)d.p1[1];
+    bool cs = (d.kind & 2u) != 0u, ce = (d.kind & 4u) != 0u;
+    if (!cs && q0x * (R)d.n0[0] + q0y * (R)d.n0[1] < 0) return 0;
+    if (!ce && q1x * (R)d.n1[0] + q1y * (R)d.n1[1] >= 0) return 0;
+    R u = q0x * ux + q0y * uy;
+    if (u < -r0 || u > l + r1) return 0;
+    R dist = std::fabs(q0x * uy - q0y * ux);
+    if (cs && u < 0) dist = std::sqrt(q0x * q0x + q0y * q0y);
+    if (ce && u > l) dist = std::sqrt(q1x * q1x + q1y * q1y);
+    R t = std::min(std::max(u / l, R(0)), R(1));
+    R rt = r0 * (1 - t) + r1 * t;
+    R x = dist / rt;
+    return x < 1 ? h0 * (rt / r0) * (1 - x * x) : R(0);
+  }
+  // common.wgsl:81-84
+  static uint32_t lay_pack(uint32_t method, R ux, R uy) {
+    R turn = std::atan2(uy, ux) / R(6.2831853f) + R(0.5f);
+    return (method & 0xffu) | ((uint32_t)(std::min(std::max(turn, R(0)), R(1)) * R(65535)) << 8);
+  }
+  // deposit.wgsl:31-75 over every cell of the grid
+  void run_deposit() {
+    if (dep_items.empty() || dep_count.empty()) return;
+    uint32_t t64 = (W + 63) / 64;
+#pragma omp parallel for schedule(static)
+    for (long jj = 0; jj < (long)H; ++jj) {
+      uint32_t j = (uint32_t)jj;
+      for (uint32_t i = 0; i < W; ++i) {
+        uint32_t tile = i / 64 + (j / 64) * t64;
+        uint32_t n = dep_count[tile];
+        if (n == 0) continue;
+        uint32_t start = dep_start[tile];
+        size_t c = idx(i, j);
+        R px = ((R)i + R(0.5)) * dx, py = ((R)j + R(0.5)) * dx;
+        Stack s;
+        stack_load(c, s);
+        R added = 0, top_add = 0;
+        uint32_t top_lay = 0;
+        for (uint32_t q = 0; q < n; ++q) {
+          const cf_deposit& d = deps[dep_items[start + q]];
+          R abx = (R)d.p1[0] - (R)d.p0[0], aby = (R)d.p1[1] - (R)d.p0[1];
+          R along = std::min(std::max(((px - (R)d.p0[0]) * abx + (py - (R)d.p0[1]) * aby) /
+                                          std::max(abx * abx + aby * aby, (R)1e-30f),
+                                      R(0)),
+                             R(1));
+          R reach = R(1.415f) * (R)std::max(d.r0, d.r1) + R(0.6f) * dx;
+          R ox = px - (R)d.p0[0] - along * abx, oy = py - (R)d.p0[1] - along * aby;
+          if (ox * ox + oy * oy > reach * reach) continue;
+          R add = 0;
+          for (int sy = 0; sy < 4; ++sy)
+            for (int sx = 0; sx < 4; ++sx)
+              add += R(0.0625f) * ribbon_height(px + ((R)sx - R(1.5)) * (R(0.25f) * dx),
+                                                py + ((R)sy - R(1.5)) * (R(0.25f) * dx), d);
+          if (add > 0) {
+            R pg[16];
+            for (int k = 0; k < 8; ++k) {  // unpack2x16float pairs (common.wgsl:173-180)
+              pg[2 * k] = (R)f16_value((uint16_t)(d.pig[k] & 0xffffu));
+              pg[2 * k + 1] = (R)f16_value((uint16_t)(d.pig[k] >> 16));
+            }
+            stack_push_top(s, add, pg, R(0));
+            added += add;
+            if (add > top_add) {
+              top_add = add;
+              R ex = abx + (R)1e-9f, ey = aby;
+              R el = std::sqrt(ex * ex + ey * ey);
+              top_lay = lay_pack(d.kind >> 8, ex / el, ey / el);
+            }
+          }
+        }
+        if (added > 0) {
+          h[c] = h[c] + added;
+          lay[c] = top_lay;
+          tile_moved[i / 16 + (j / 16) * TW] = 1u;  // mark_moved
+          stack_compact(s);
+          stack_store_to(c, s, sh, scu, pig);
+        }
+      }
+    }
+  }
+
   // Film::encode_frame, src/film/mod.rs:1322-1462 (simulation portion;
-  // journal / brush / deposit / knife / CG / slump / pool8 are not on the path)
+  // journal / brush / knife / CG / slump / pool8 are not on the path).  The
+  // deposits uploaded since the last frame are laid first, then dropped.
   void encode_frame(uint32_t substeps) {
+    if (!dep_items.empty()) run_deposit();
+    dep_items.clear();
     k_mark_tiles();
     k_compact_tiles();
     run_cure();

@@ -123,6 +123,24 @@ float cfo_step_adaptive(void* p, float dt_max) {
 
 void cfo_dry_now(void* p) { DISPATCH((Handle*)p, F.dry_now()); }
 
+// Deposits for the next frame, already binned into 64x64-cell tiles
+// (start[nt], count[nt], items[ni]) by the upload_deposits restatement, with
+// the host's h_max_pending after the upload.
+void cfo_set_deposits(void* p, const cf_deposit* deps, uint32_t n, const uint32_t* start, const uint32_t* count,
+                      uint32_t nt, const uint32_t* items, uint32_t ni, float h_max_pending) {
+  DISPATCH((Handle*)p, {
+    F.deps.assign(deps, deps + n);
+    F.dep_start.assign(start, start + nt);
+    F.dep_count.assign(count, count + nt);
+    F.dep_items.assign(items, items + ni);
+    F.h_max_pending = h_max_pending;
+  });
+}
+
+void cfo_host_stats(void* p, float* h_max_stat, float* h_max_pending) {
+  DISPATCH((Handle*)p, { *h_max_stat = F.h_max_stat; *h_max_pending = F.h_max_pending; });
+}
+
 // stats: h_max, mu_min, active tiles, mass
 void cfo_stats(void* p, float* h_max, float* mu_min, uint32_t* active, double* mass) {
   DISPATCH((Handle*)p, {
@@ -152,6 +170,7 @@ int cfo_run(void* p, const char* kernel) {
     else if (k == "strata_copy_back") F.run_copy_back();
     else if (k == "strata_fill") F.run_strata_fill();
     else if (k == "shade_full") F.run_shade();
+    else if (k == "deposit") F.run_deposit();
     else ok = 0;
   });
   return ok;

@@ -72,6 +72,10 @@ def lib():
         L.cfo_dry_now.argtypes = [vp]
         L.cfo_stats.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_double)]
+        u32p = C.POINTER(C.c_uint32)
+        L.cfo_set_deposits.argtypes = [vp, C.c_void_p, C.c_uint32, u32p, u32p, C.c_uint32, u32p, C.c_uint32,
+                                       C.c_float]
+        L.cfo_host_stats.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.cfo_run.argtypes = [vp, C.c_char_p]
         L.cfo_run.restype = C.c_int
         L.cfo_buffer_len.argtypes = [vp, C.c_char_p]
@@ -154,6 +158,27 @@ class Oracle:
     def dry_now(self):
         self.L.cfo_dry_now(self.p)
 
+    def host_stats(self):
+        hm, hp = C.c_float(), C.c_float()
+        self.L.cfo_host_stats(self.p, C.byref(hm), C.byref(hp))
+        return hm.value, hp.value
+
+    total_deposited = 0.0
+
+    def upload_deposits(self, deps):
+        """Film::upload_deposits: bins the records (deposit_ref.DEPOSIT_DTYPE)
+        for the next frame; returns the number taken."""
+        import deposit_ref as dr
+        deps = np.ascontiguousarray(np.asarray(deps, dr.DEPOSIT_DTYPE).reshape(-1))
+        hm, hp = self.host_stats()
+        sent, start, cnt, items, self.total_deposited, hp = dr.bin_deposits(
+            deps, self.w, self.h, self.settings.width_m, self.settings.height_m, hm, hp, self.total_deposited)
+        u = C.POINTER(C.c_uint32)
+        items = np.ascontiguousarray(items, np.uint32)
+        self.L.cfo_set_deposits(self.p, deps.ctypes.data if sent else None, sent, start.ctypes.data_as(u),
+                                cnt.ctypes.data_as(u), start.size, items.ctypes.data_as(u), items.size, hp)
+        return sent
+
     def run(self, kernel):
         assert self.L.cfo_run(self.p, kernel.encode()), kernel
 
@@ -179,6 +204,8 @@ def ref_lib():
         L.wgr_encode_frame.argtypes = [C.c_uint32]
         L.wgr_run.argtypes = [C.c_char_p]
         L.wgr_run.restype = C.c_int
+        u32p = C.POINTER(C.c_uint32)
+        L.wgr_set_deposits.argtypes = [C.c_void_p, C.c_uint32, u32p, u32p, C.c_uint32, u32p, C.c_uint32]
         L.wgr_buffer.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_int]
         L.wgr_buffer.restype = C.c_int
         L.wgr_active_count.restype = C.c_uint32
@@ -236,6 +263,16 @@ class RefShaders:
 
     def run(self, kernel):
         assert self.L.wgr_run(kernel.encode()), kernel
+
+    def set_deposits(self, deps, start, cnt, items):
+        """Deposits for the next frame with tile tables from the
+        upload_deposits restatement (deposit_ref.bin_deposits)."""
+        import deposit_ref as dr
+        deps = np.ascontiguousarray(np.asarray(deps, dr.DEPOSIT_DTYPE).reshape(-1))
+        u = C.POINTER(C.c_uint32)
+        start, cnt, items = (np.ascontiguousarray(a, np.uint32) for a in (start, cnt, items))
+        self.L.wgr_set_deposits(deps.ctypes.data if deps.size else None, deps.size, start.ctypes.data_as(u),
+                                cnt.ctypes.data_as(u), start.size, items.ctypes.data_as(u), items.size)
 
 
 def make_settings(overrides):

@@ -11,6 +11,8 @@
 //  - apply's begin/end_motion workgroup flag and reduce_tiles' shared-memory
 //    tree (a max/min) are emulated here around the translated per-cell code;
 //  - nose and strata_fill read `__old` snapshots (Jacobi semantics).
+//  - deposits uploaded by wgr_set_deposits are laid by the translated
+//    deposit entry point at the start of the next frame.
 // One film per process (the translated buffers are module globals).
 #include <algorithm>
 #include <array>
@@ -106,7 +108,11 @@ void run_strata_fill() {
   dispatch_tiles(strata_fill);
 }
 
+bool dep_pending = false;  // deposits uploaded since the last frame
+
 void encode_frame(u32 substeps) {
+  if (dep_pending) dispatch_full(deposit);  // the "pre" pass of Film::encode_frame
+  dep_pending = false;
   active_count[0] = 0;
   run_mark_tiles();
   run_compact_tiles();
@@ -181,6 +187,29 @@ void wgr_after_write_state() {
   for (auto& v : tile_moved.v) v = 1u;
 }
 
+// Deposits for the next frame with their 64x64-cell tile tables, as the
+// host's upload_deposits (src/film/mod.rs:1175-1224) writes them.
+void wgr_set_deposits(const cf_deposit* d, uint32_t n, const uint32_t* start, const uint32_t* count, uint32_t nt,
+                      const uint32_t* items, uint32_t ni) {
+  deposits.v.assign(std::max(n, 1u), Deposit{});
+  for (uint32_t k = 0; k < n; ++k) {
+    Deposit& o = deposits.v[k];
+    o.p0 = vec2<f32>(d[k].p0[0], d[k].p0[1]);
+    o.p1 = vec2<f32>(d[k].p1[0], d[k].p1[1]);
+    o.n0 = vec2<f32>(d[k].n0[0], d[k].n0[1]);
+    o.n1 = vec2<f32>(d[k].n1[0], d[k].n1[1]);
+    o.r0 = d[k].r0; o.r1 = d[k].r1; o.h0 = d[k].h0; o.vol = d[k].vol;
+    o.kind = d[k].kind;
+    o.pig0 = vec4<u32>(d[k].pig[0], d[k].pig[1], d[k].pig[2], d[k].pig[3]);
+    o.pig1 = vec4<u32>(d[k].pig[4], d[k].pig[5], d[k].pig[6], d[k].pig[7]);
+  }
+  tile_start.v.assign(start, start + nt);
+  tile_count.v.assign(count, count + nt);
+  tile_items.v.assign(items, items + ni);
+  if (ni == 0) tile_items.v.assign(1, 0u);
+  dep_pending = ni > 0;
+}
+
 int wgr_run(const char* k) {
   std::string s(k);
   if (s == "mark_tiles") { active_count[0] = 0; run_mark_tiles(); }
@@ -200,6 +229,7 @@ int wgr_run(const char* k) {
   else if (s == "strata_copy_back") dispatch_tiles(strata_copy_back);
   else if (s == "strata_fill") run_strata_fill();
   else if (s == "shade_full") dispatch_full(shade_full);
+  else if (s == "deposit") dispatch_full(deposit);
   else return 0;
   return 1;
 }

@@ -1,7 +1,8 @@
 """Mechanical WGSL -> C++ translation of the reference shaders.
 
 TEST INFRASTRUCTURE.  This script reads the reference's own shader sources
-(shaders/common.wgsl, film.wgsl, strata.wgsl, km.wgsl, cure.wgsl, shade.wgsl)
+(shaders/common.wgsl, film.wgsl, strata.wgsl, km.wgsl, cure.wgsl, shade.wgsl,
+deposit.wgsl)
 from the reference checkout and rewrites them token by token into C++ that
 compiles against wgsl_rt.hpp.  The output goes to oracle/_ref/ (git-ignored):
 no reference source is stored in this repository.  The translated shaders,
@@ -23,7 +24,7 @@ Usage: python translate.py <reference_root> <out_file> [real]
 import re
 import sys
 
-MODULES = ["common.wgsl", "film.wgsl", "strata.wgsl", "km.wgsl", "cure.wgsl", "shade.wgsl"]
+MODULES = ["common.wgsl", "film.wgsl", "strata.wgsl", "km.wgsl", "cure.wgsl", "shade.wgsl", "deposit.wgsl"]
 
 
 def split_items(src):

@@ -106,6 +106,17 @@ class SnapshotInfo(C.Structure):
                 ("cure_rate", C.c_float), ("h_max", C.c_float), ("s_max", C.c_float), ("total_deposited", C.c_double)]
 
 
+class Deposit(C.Structure):
+    """cf_deposit: Deposit (src/film/mod.rs:25-39), 96 bytes."""
+    _fields_ = [("p0", C.c_float * 2), ("p1", C.c_float * 2), ("n0", C.c_float * 2), ("n1", C.c_float * 2),
+                ("r0", C.c_float), ("r1", C.c_float), ("h0", C.c_float), ("vol", C.c_float),
+                ("kind", C.c_uint32), ("pad", C.c_uint32 * 3), ("pig", C.c_uint32 * 8)]
+
+
+assert C.sizeof(Deposit) == 96
+CF_MAX_DEPOSITS = 65536
+
+
 class BatchTuning(C.Structure):
     """cf_batch_tuning."""
     _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
@@ -170,6 +181,16 @@ def load_library(path=None):
         "cf_snapshot_load": ([vp, C.c_char_p, C.c_uint64, C.POINTER(SnapshotInfo)], i32),
         "cf_lz4_compress": ([C.c_char_p, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)], i32),
         "cf_lz4_decompress": ([C.c_char_p, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)], i32),
+        "cf_deposit_ribbon": ([C.POINTER(f32), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32), f32, f32, u32, f32,
+                               C.POINTER(u32), f32, C.POINTER(Deposit)], i32),
+        "cf_deposit_capsule": ([C.POINTER(f32), C.POINTER(f32), f32, f32, C.POINTER(u32), f32, C.POINTER(Deposit)],
+                               i32),
+        "cf_deposit_stroke": ([C.POINTER(f32), C.POINTER(f32), f32, f32, C.POINTER(u32), f32, C.POINTER(Deposit)],
+                              i32),
+        "cf_deposit_sampled_volume": ([C.POINTER(Deposit), f32, C.POINTER(f32)], i32),
+        "cf_deposit_height_at": ([C.POINTER(Deposit), C.POINTER(f32), C.POINTER(f32)], i32),
+        "cf_upload_deposits": ([vp, vp, u32, C.POINTER(u32), C.POINTER(C.c_double)], i32),
+        "cf_lay_deposits": ([vp, vp], i32),
         "cf_batch_create": ([C.POINTER(vp)], i32),
         "cf_batch_destroy": ([vp], i32),
         "cf_batch_add": ([vp, vp], i32),

@@ -173,6 +173,24 @@ class Film:
         self._check(self.L.cf_snapshot_load(self.p, data, len(data), C.byref(info)), "cf_snapshot_load")
         return {k: getattr(info, k) for k, _ in SnapshotInfo._fields_}
 
+    total_deposited = 0.0
+
+    def upload_deposits(self, deps):
+        """Film::upload_deposits (cf_upload_deposits): the records (an array of
+        deposit.DEPOSIT_DTYPE) are laid by the next frame.  Returns the number
+        taken (at most CF_MAX_DEPOSITS); the caller keeps the rest."""
+        from .deposit import DEPOSIT_DTYPE
+        a = np.ascontiguousarray(np.asarray(deps, DEPOSIT_DTYPE).reshape(-1))
+        sent, tot = C.c_uint32(), C.c_double()
+        self._check(self.L.cf_upload_deposits(self.p, a.ctypes.data if a.size else None, a.size, C.byref(sent),
+                                              C.byref(tot)), "cf_upload_deposits")
+        self.total_deposited = tot.value
+        return sent.value
+
+    def lay_deposits(self, stream=None):
+        """cf_lay_deposits: lays the uploaded deposits now (asynchronous)."""
+        self._check(self.L.cf_lay_deposits(self.p, stream), "cf_lay_deposits")
+
     def update_params(self, frame_dt, substeps):
         self._check(self.L.cf_update_params(self.p, frame_dt, substeps), "cf_update_params")
 

@@ -348,6 +348,9 @@ cf_status cf_destroy(cf_film* f) {
   if (f->params_ev) cudaEventDestroy(f->params_ev);
   if (f->d_recs) cudaFree(f->d_recs);
   if (f->d_tiles) cudaFree(f->d_tiles);
+  if (f->d_deps) cudaFree(f->d_deps);
+  if (f->d_dep_tiles) cudaFree(f->d_dep_tiles);
+  if (f->d_dep_items) cudaFree(f->d_dep_items);
   delete f;
   return CF_OK;
 }
@@ -423,6 +426,7 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   std::memcpy(&mm, &ds.mu_min_bits, 4);
   f->h_max_stat = hm;
   f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
+  if (f->dep_pending == 0u) f->h_max_pending = 0.f;  // stats now include the deposits (poll_stats)
   CUDA_TRY(f, cudaDeviceSynchronize());
   return CF_OK;
 }
@@ -446,6 +450,8 @@ cf_status cf_clone_state(cf_film* dst, const cf_film* src, void* stream) {
   dst->mu_min_stat = src->mu_min_stat;
   dst->h_max_pending = src->h_max_pending;
   dst->frames = src->frames;
+  dst->total_deposited = src->total_deposited;
+  dst->dep_pending = 0u;  // deposits uploaded to dst before the clone are dropped
   const bool src_swapped = src->F.sh != src->sh_created, dst_swapped = dst->F.sh != dst->sh_created;
   if (src_swapped != dst_swapped) swap_generations(dst);
   return CF_OK;
@@ -496,6 +502,7 @@ static cf_status post_frame_stats(cf_film* f, cudaStream_t st, bool sync_host) {
   std::memcpy(&mm, &ds.mu_min_bits, 4);
   f->h_max_stat = hm;
   f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
+  if (f->dep_pending == 0u) f->h_max_pending = 0.f;  // stats now include the deposits (poll_stats)
   return CF_OK;
 }
 
@@ -536,6 +543,7 @@ cf_status cf_encode_frame(cf_film* f, uint32_t substeps, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
+  f->launches += launch_pending_deposits(f, st);
   f->launches += cfk::launch_frame_packed(solo_view(f), f->prec, substeps, 0, st);
   swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
@@ -550,6 +558,7 @@ cf_status cf_step_adaptive(cf_film* f, float dt_max, void* stream) {
   if (f->h_params->dt_max != dt_max) f->params_dirty = true;
   cf_status s = upload_params(f, st, dt_max);
   if (s != CF_OK) return s;
+  f->launches += launch_pending_deposits(f, st);
   f->launches += cfk::launch_frame_packed(solo_view(f), f->prec, 1, 1, st);
   swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
@@ -599,6 +608,7 @@ cf_status cf_get_stats(cf_film* f, cf_stats* out) {
   std::memcpy(&mm, &ds.mu_min_bits, 4);
   f->h_max_stat = hm;
   f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
+  if (f->dep_pending == 0u) f->h_max_pending = 0.f;  // stats now include the deposits (poll_stats)
   double dx = (double)f->S.width_m / (double)f->w;
   out->h_max = hm;
   out->mu_min = f->mu_min_stat;
@@ -742,7 +752,8 @@ cf_status cf_debug_run(cf_film* f, const char* kernel, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
-  const int r = cfk::launch_one(solo_view(f), f->prec, kernel, st);
+  const int r = std::strcmp(kernel, "deposit") == 0 ? (launch_pending_deposits(f, st), 1)
+                                                    : cfk::launch_one(solo_view(f), f->prec, kernel, st);
   if (!r) return fail(f, CF_ERR_INVALID_ARG, "unknown kernel");
   if (r == 2) swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;

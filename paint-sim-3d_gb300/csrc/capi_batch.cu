@@ -186,6 +186,7 @@ cf_status step(cf_batch* b, uint32_t frames, uint32_t substeps, float dt_max, cu
     if (adaptive && f->h_params->dt_max != dt_max) f->params_dirty = true;
     cf_status s = upload_params(f, st, adaptive ? dt_max : 0.f);
     if (s != CF_OK) return bfail(b, s, f->err);
+    b->launches += launch_pending_deposits(f, st);  // before the first frame, as alone
   }
   uint32_t done = 0;
   if (b->tune.use_graph) {

@@ -40,6 +40,13 @@ struct cf_film {
   cfk::Film* d_recs = nullptr;
   uint2* d_tiles = nullptr;
   float4* sh_created = nullptr;  // F.sh at create: tells which record is current
+  // deposits for the next frame (cf_upload_deposits)
+  cf_deposit* d_deps = nullptr;
+  uint32_t* d_dep_tiles = nullptr;  // start[nt64], count[nt64]
+  uint32_t* d_dep_items = nullptr;
+  size_t dep_cap = 0, dep_items_cap = 0;
+  uint32_t dep_nt = 0, dep_pending = 0;
+  double total_deposited = 0.0;  // volume laid inside the canvas (upload_deposits)
 };
 
 // The view that steps this film alone (same kernels as a batch).
@@ -77,3 +84,6 @@ inline cf_status fail(cf_film* f, cf_status s, const char* msg) {
 cf_status upload_params(cf_film* f, cudaStream_t st, float dt_max = 0.f);
 // Removes a film from its batch (when the film is destroyed).
 void batch_forget(cf_film* f);
+// Enqueues the film's pending deposits (deposit.wgsl, before the frame's
+// mark_tiles) and clears them; returns the number of launches.
+uint32_t launch_pending_deposits(cf_film* f, cudaStream_t st);

@@ -111,11 +111,6 @@ __device__ __forceinline__ void compact_tile(const Film& F, uint32_t t, int all_
   }
 }
 
-__device__ __forceinline__ void lnmu_table(const float* pigtab, float out[12]) {
-#pragma unroll
-  for (int q = 0; q < 12; ++q) out[q] = logf(fmaxf(pigtab[q * 40 + 32], 1e-3f));
-}
-
 // The commit of the bottom stratum into the relief (cure.wgsl:119-159), the
 // rare branch of cure_tile: out of line so that the common path keeps few
 // registers.

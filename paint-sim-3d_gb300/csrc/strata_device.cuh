@@ -311,6 +311,12 @@ __device__ __forceinline__ void rheo_from_parts(const cf_params& P, float4 agg, 
   n_o = agg.w;
 }
 
+// ln of each pigment's table viscosity (cure.wgsl:3-48 reads it per stratum).
+__device__ __forceinline__ void lnmu_table(const float* pigtab, float out[12]) {
+#pragma unroll
+  for (int q = 0; q < 12; ++q) out[q] = logf(fmaxf(pigtab[q * 40 + 32], 1e-3f));
+}
+
 // Aggregates and colour of a whole in-register stack.
 __device__ inline void finish_stack(const cf_params& P, const float* lnmu_tab, const float* tab, const float* cm,
                                     const uint16_t* rf, float hv, float mv, const Stack& s, float4& agg,

@@ -26,7 +26,7 @@ sys.path.insert(0, str(ROOT / "oracle"))
 sys.path.insert(0, str(ROOT / "paint-sim-3d_gb300"))
 
 OUT_FIELDS = ["h", "m", "rheo", "strata_h", "strata_pig", "strata_cure", "sub_refl", "delta", "fnorm",
-              "color", "acc", "tile_flags", "pres", "flux", "alpha", "tmp", "acc_s", "alpha_s"]
+              "color", "acc", "tile_flags", "pres", "flux", "alpha", "tmp", "acc_s", "alpha_s", "lay"]
 
 
 def mixed_canvas(seed):
@@ -84,7 +84,54 @@ def cases():
     cv = synth.blob_canvas(48, 40, 13, n_blobs=5, sigma=(3, 8), per_cell_n=False, tau=(0, 0.5), mu=(0.05, 0.3),
                            peak_mm=(1.0, 3.0))
     out.append(("spreading_front", cv, dict(frame_dt=1 / 60, frames=10, adaptive_substeps=True)))
+    cv = synth.blob_canvas(48, 48, 17, n_blobs=4, sigma=(3, 8), per_cell_n=False, tables="reference",
+                           tau=(0.0, 1.0), mu=(0.05, 0.5))
+    out.append(("deposit_strokes", cv, dict(frame_dt=1 / 60, frames=5, adaptive_substeps=True,
+                                            deposits={0: deposit_set(cv, 5), 2: deposit_set(cv, 6)})))
+    cv = synth.blob_canvas(48, 48, 17, n_blobs=1, sigma=(2, 5), per_cell_n=False, tables="reference",
+                           tau=(0.0, 1.0), mu=(0.05, 0.5))
+    out.append(("deposit_fresh", cv, dict(frame_dt=1 / 60, frames=4, adaptive_substeps=True,
+                                          deposits={0: deposit_set(cv, 100), 2: deposit_set(cv, 102)})))
     return out
+
+
+def deposit_set(cv, seed):
+    """Strokes, capsules, a dot, an angled ribbon, a recycled deposit and one
+    that crosses the canvas edge, built by the Deposit constructors."""
+    import deposit_ref as dr
+    w = np.float32(cv.settings["width_m"])
+    dx = w / np.float32(cv.w)
+    rng = np.random.Generator(np.random.PCG64(seed))
+
+    def pig():
+        v = np.zeros(16)
+        v[:12] = rng.dirichlet(np.full(12, 0.5))
+        v[13] = rng.uniform(0.5, 2.0)
+        v[14] = rng.uniform(9.0, 11.0) if rng.random() < 0.5 else 0.0
+        return dr.pack_pig(v)
+
+    def pt():
+        return (float(rng.uniform(0.1, 0.9) * w), float(rng.uniform(0.1, 0.9) * w))
+
+    deps = []
+    for _ in range(3):
+        a = pt()
+        b = (a[0] + float(rng.uniform(-0.3, 0.3) * w), a[1] + float(rng.uniform(-0.3, 0.3) * w))
+        deps.append(dr.stroke(a, b, float(rng.uniform(1.5, 4) * dx), float(rng.uniform(0.5, 3) * 1e-9), pig(), dx))
+    a = pt()
+    deps.append(dr.capsule(a, (a[0] + float(2 * dx), a[1] - float(3 * dx)), float(2.5 * dx), 1e-9, pig(), dx))
+    deps.append(dr.capsule(pt(), pt(), float(1.2 * dx), 0.7e-9, pig(), dx))
+    a = pt()
+    deps.append(dr.capsule(a, a, float(3 * dx), 1.5e-9, pig(), dx))
+    a = pt()
+    deps.append(dr.ribbon(a, (a[0] + float(6 * dx), a[1] + float(2 * dx)), (np.cos(0.3), -np.sin(0.3)),
+                          (np.cos(0.4), np.sin(0.4)), float(2 * dx), float(3.5 * dx), 0, 1.2e-9, pig(), dx))
+    d = dr.stroke((float(-2 * dx), float(0.5 * w)), (float(5 * dx), float(0.55 * w)), float(2 * dx), 1e-9, pig(), dx)
+    d["kind"] |= dr.RECYCLED
+    deps.append(d)
+    for k, d in enumerate(deps):
+        d["kind"] |= ((k % 6) + 1) << dr.METHOD_SHIFT
+    return np.array(deps)
 
 
 def main():
@@ -100,9 +147,17 @@ def main():
         r = po.RefShaders(cv.w, cv.h)
         r.set_tables(cv.pigtab, cv.cmf)
         r.write_state(cv.planes)
-        schedule, params = [], []
+        schedule, params, dep_frames = [], [], {}
         for f in range(sched["frames"]):
             fdt = sched["frame_dt"]
+            if f in sched.get("deposits", {}):
+                import deposit_ref as dr
+                deps = sched["deposits"][f]
+                hm, hp = o.host_stats()
+                _, start, cnt, items, _, _ = dr.bin_deposits(deps, cv.w, cv.h, st.width_m, st.height_m, hm, hp)
+                o.upload_deposits(deps)
+                r.set_deposits(deps, start, cnt, items)
+                dep_frames["deposits_%d" % f] = deps.view(np.uint8).reshape(len(deps), 96)
             n = o.choose_substeps(fdt) if sched.get("adaptive_substeps") else sched["substeps"]
             o.update_params(fdt, n)
             p = o.params()
@@ -112,11 +167,12 @@ def main():
             schedule.append((fdt, n))
             params.append(np.frombuffer(bytes(p), np.uint8))
         outs = {"out_" + k: r.buf(k) for k in OUT_FIELDS}
-        worst = max(float(np.abs(o.buf(k) - outs["out_" + k]).max()) for k in OUT_FIELDS if k != "rheo")
+        worst = max(float(np.abs(o.buf(k) - outs["out_" + k]).max()) for k in OUT_FIELDS if k not in ("rheo", "lay"))
+        assert np.array_equal(o.buf("lay"), outs["out_lay"]), "lay differs"
         ins = {"in_" + k: np.asarray(v) for k, v in cv.planes.items()}
         np.savez_compressed(HERE / ("%s.npz" % name), w=cv.w, h=cv.h, settings=json.dumps(cv.settings),
                             pigtab=cv.pigtab, cmf=cv.cmf, schedule=np.array(schedule),
-                            params=np.stack(params), **ins, **outs)
+                            params=np.stack(params), **ins, **outs, **dep_frames)
         print("%-16s %dx%d frames %d substeps %s  oracle-vs-ref max |d| %.3e" % (
             name, cv.w, cv.h, len(schedule), [s[1] for s in schedule], worst))
 

@@ -10,6 +10,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import deposit_ref as dr
 import pyoracle as po
 
 GOLDEN = sorted((Path(__file__).resolve().parent / "golden").glob("*.npz"))
@@ -24,7 +25,9 @@ def replay(d, bits=64):
     o.set_tables(d["pigtab"], d["cmf"])
     planes = {k[3:]: d[k] for k in d.files if k.startswith("in_")}
     o.write_state(planes)
-    for (fdt, n), praw in zip(d["schedule"], d["params"]):
+    for f, ((fdt, n), praw) in enumerate(zip(d["schedule"], d["params"])):
+        if "deposits_%d" % f in d.files:  # upload_deposits before choose_substeps (src/main.rs:1881-1892)
+            o.upload_deposits(d["deposits_%d" % f].reshape(-1).view(dr.DEPOSIT_DTYPE))
         o.update_params(float(fdt), int(n))
         assert bytes(o.params()) == praw.tobytes(), "update_params drifted from the fixture"
         o.encode_frame(int(n))
@@ -43,13 +46,16 @@ def test_oracle_matches_reference_fixture(path):
         scale = max(float(np.abs(want).max()), 1e-30)
         err = float(np.abs(got - want).max()) / scale
         assert err <= 1e-12, (f, err)
+    if "out_lay" in d.files:
+        assert np.array_equal(o.buf("lay").astype(np.uint64), d["out_lay"].astype(np.uint64))
     rheo = o.buf("rheo").reshape(-1, 3)[:, :2].reshape(-1)
     want = d["out_rheo"].reshape(-1, 3)[:, :2].reshape(-1)
     assert np.allclose(rheo, want, rtol=1e-12, atol=0)
 
 
 def test_fixtures_exist():
-    assert len(GOLDEN) >= 6
+    assert len(GOLDEN) >= 8
+    assert any("deposits_0" in np.load(p).files for p in GOLDEN)
 
 
 @pytest.mark.parametrize("path", GOLDEN[:3], ids=[p.stem for p in GOLDEN[:3]])

@@ -18,6 +18,7 @@ import pytest
 import parity
 import pyoracle as po
 from canvaz_film import capi, synth
+from canvaz_film.deposit import DEPOSIT_DTYPE
 
 pytestmark = pytest.mark.gpu
 
@@ -162,7 +163,9 @@ def replay_cuda(d, precision=capi.CF_PREC_REFERENCE):
     f = Film(st, w, h, precision)
     f.set_tables(d["pigtab"], d["cmf"])
     f.write_state({k[3:]: d[k] for k in d.files if k.startswith("in_")})
-    for (fdt, n), praw in zip(d["schedule"], d["params"]):
+    for fr, ((fdt, n), praw) in enumerate(zip(d["schedule"], d["params"])):
+        if "deposits_%d" % fr in d.files:
+            f.upload_deposits(d["deposits_%d" % fr].reshape(-1).view(DEPOSIT_DTYPE))
         f.update_params(float(fdt), int(n))
         got, want = bytes(f.params()), praw.tobytes()
         # front.zw and front3.xyz feed only the implicit CG solve and depend on
@@ -174,6 +177,15 @@ def replay_cuda(d, precision=capi.CF_PREC_REFERENCE):
     return f
 
 
+# deposit_strokes lays a second set of strokes onto paint that is spreading at
+# its yield threshold; the frames after it amplify single-cell branch flips.
+# Perturbing the input heights by 1e-7 (relative) moves the oracle's FP32
+# mirror of the reference arithmetic between 2e-7 and 4e-6 from FP64 on this
+# fixture, and the CUDA path between 1.5e-7 and 2.3e-5; deposit_fresh (strokes
+# on bare canvas) holds the usual 1e-5.
+H_REL_BRANCHY = {"deposit_strokes": 5e-5}
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=[p.stem for p in GOLDEN])
 def test_frames_vs_reference_fixture(built, path):
     d = np.load(path)
@@ -183,7 +195,7 @@ def test_frames_vs_reference_fixture(built, path):
     want = {k: d["out_" + k] for k in got}
     m = parity.metrics(got, want)
     print(path.stem, m)
-    parity.check(m)
+    parity.check(m, h_rel=H_REL_BRANCHY.get(path.stem, parity.H_REL_L2))
     tf = f.plane("tile_flags").astype(np.uint64)
     assert (tf == d["out_tile_flags"].astype(np.uint64)).mean() >= 0.95
 
