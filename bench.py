@@ -65,7 +65,9 @@ PREC_NAME = {capi.CF_PREC_FP32: "f32", capi.CF_PREC_REFERENCE: "f32+f16pig", cap
 # and config 4, the Poisson-served stream.
 BATCH_WORKLOAD = "batch64_dt1e-3_fp32"
 SERVE_WORKLOAD = "serve_poisson20_fp32bf16"
-# The deposit rasteriser alone: 4096 strokes per step onto a 4096^2 FP32 film.
+# The deposit rasteriser alone: 4096 strokes per step onto a 4096^2 FP32 film
+# (and the same density at 2048^2, the small case for kernel captures).
+DEPOSIT_WORKLOADS = {"deposit4096_strokes4096_fp32": (4096, 4096), "deposit2048_strokes1024_fp32": (2048, 1024)}
 DEPOSIT_WORKLOAD = "deposit4096_strokes4096_fp32"
 # Compulsory bytes per cell that receives paint (FP32 storage): reads h, m,
 # strata_h, strata_cure, 64 f32 pigment slots, 16 f16 substrate bands;
@@ -81,7 +83,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, DEPOSIT_WORKLOAD])
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD] + sorted(DEPOSIT_WORKLOADS))
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="arrival window of the served workload")
     ap.add_argument("--serve-wall", type=float, default=60.0, help="wall-clock cut-off of the served run")
     ap.add_argument("--serve-steps-scale", type=float, default=1.0, help="scales the served 100-3000 step range")
@@ -234,13 +236,14 @@ def tiles_touched(deps, side, dx):
     return int(np.prod(hi - lo + 1, axis=1).sum())
 
 
-DEPOSIT_SIDE, DEPOSIT_COUNT, DEPOSIT_SETS = 4096, 4096, 4
+DEPOSIT_SETS = 4
 DEPOSIT_CPU_SIDE = 1024  # CPU sample: the same stroke density on a 1024^2 film
 
 
-def deposit_cpu(budget_s, threads_note=True):
+def deposit_cpu(workload, budget_s):
     """The oracle's FP32 deposit pass (run_deposit, OpenMP over rows) on a
-    1024^2 film with 256 strokes per launch (the workload's density)."""
+    1024^2 film with the workload's stroke density (256 strokes per launch)."""
+    side_w, count_w = DEPOSIT_WORKLOADS[workload]
     import pyoracle as po
     po.build()
     side = DEPOSIT_CPU_SIDE
@@ -248,7 +251,7 @@ def deposit_cpu(budget_s, threads_note=True):
     cv = synth.blob_canvas(16, 16, 1, n_blobs=1, tables="reference")
     o = po.Oracle(side, side, st, capi.CF_PIG_F32, 32)
     o.set_tables(cv.pigtab, cv.cmf)
-    n = DEPOSIT_COUNT * side * side // (DEPOSIT_SIDE * DEPOSIT_SIDE)
+    n = count_w * side * side // (side_w * side_w)
     sets = [deposit_strokes(n, side * 1e-3, np.float32(1e-3), 100 + k) for k in range(2)]
     el, launches = 0.0, 0
     while True:
@@ -261,12 +264,12 @@ def deposit_cpu(budget_s, threads_note=True):
             break
     return {"value": n * launches / el / 1e6, "unit": "Mdeposits/s", "cores": os.cpu_count(), "kind": "port",
             "sample": "%d launches of %d strokes on a %dx%d FP32 film (the %dx%d workload's stroke density), "
-                      "oracle run_deposit, OpenMP %d threads, %.1f s" % (launches, n, side, side, DEPOSIT_SIDE,
-                                                                          DEPOSIT_SIDE, os.cpu_count(), el)}
+                      "oracle run_deposit, OpenMP %d threads, %.1f s" % (launches, n, side, side, side_w,
+                                                                          side_w, os.cpu_count(), el)}
 
 
 def deposit_arm(args):
-    """The deposit rasteriser on one GPU: every step uploads one set of 4096
+    """The deposit rasteriser on one GPU: every step uploads one set of
     strokes (cf_upload_deposits: host binning + copies) and lays it
     (cf_lay_deposits).  `value` = strokes per second of device time (CUDA
     events around each launch); `e2e` = strokes per second of the whole
@@ -278,13 +281,13 @@ def deposit_arm(args):
     if not capi.LIB_PATH.exists():
         import __graft_entry__ as g
         g.build()
-    side = DEPOSIT_SIDE
+    side, count = DEPOSIT_WORKLOADS[args.workload]
     dx = np.float32(1e-3)
     st = capi.Settings.default(width_m=side * 1e-3, height_m=side * 1e-3)
     cv = synth.blob_canvas(16, 16, 1, n_blobs=1, tables="reference")
     film = Film(st, side, side, capi.CF_PREC_FP32)
     film.set_tables(cv.pigtab, cv.cmf)
-    sets = [deposit_strokes(DEPOSIT_COUNT, side * 1e-3, dx, 10 * rank + k) for k in range(DEPOSIT_SETS)]
+    sets = [deposit_strokes(count, side * 1e-3, dx, 10 * rank + k) for k in range(DEPOSIT_SETS)]
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
     # cells one launch paints (first set on the bare film)
@@ -307,7 +310,7 @@ def deposit_arm(args):
         torch.cuda.synchronize()
     t = sum(a.elapsed_time(b) for a, b in evs) / 1e3
     launches = film.stats()["launches"] - l0
-    value = DEPOSIT_COUNT * args.steps / t / 1e6
+    value = count * args.steps / t / 1e6
     peak, peak_kind = peaks()
     achieved = DEPOSIT_BYTES_PER_CELL * covered * args.steps / t / 1e9
     e2e = None
@@ -321,18 +324,19 @@ def deposit_arm(args):
             film.stats()
         te = time.perf_counter() - t0
         items = float(np.mean([tiles_touched(s_, side, dx) for s_ in sets]))
-        e2e = {"value": DEPOSIT_COUNT * args.e2e_steps / te / 1e6, "unit": "Mdeposits/s",
-               "h2d_bytes_per_step": int(96 * DEPOSIT_COUNT + 8 * (side // 64) ** 2 + 4 * items),
+        e2e = {"value": count * args.e2e_steps / te / 1e6, "unit": "Mdeposits/s",
+               "h2d_bytes_per_step": int(96 * count + 8 * (side // 64) ** 2 + 4 * items),
                "d2h_bytes_per_step": int(ctypes.sizeof(capi.Stats)),
                "steps": args.e2e_steps, "path": "cf_upload_deposits(host records) + cf_lay_deposits + cf_get_stats"}
-    cb = None if args.no_cpu_baseline else deposit_cpu(args.cpu_seconds)
+    cb = None if args.no_cpu_baseline else deposit_cpu(args.workload, args.cpu_seconds)
     line = {
         "metric": "Mdeposits/s", "value": value, "unit": "Mdeposits/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded strokes and capsules)",
-        "config": {"workload": DEPOSIT_WORKLOAD, "w": side, "h": side, "strokes_per_step": DEPOSIT_COUNT,
+        "config": {"workload": args.workload, "w": side, "h": side, "strokes_per_step": count,
                    "cells_painted_per_step": covered, "precision": "f32",
-                   "l2": "each step paints new cells of a 4096^2 film (9.9 GB of state): no flush"},
+                   "l2": "each step paints new cells of a %d^2 film (%.1f GB of state): no flush"
+                         % (side, film_bytes(side * side, capi.CF_PREC_FP32) / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "alg_bytes_per_painted_cell": DEPOSIT_BYTES_PER_CELL,
                      "scope": "k_deposit", "traffic": None},
@@ -346,8 +350,8 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    if args.workload == DEPOSIT_WORKLOAD:
-        cb = deposit_cpu(min(150.0, 10.0 * (args.steps + args.warmup)))
+    if args.workload in DEPOSIT_WORKLOADS:
+        cb = deposit_cpu(args.workload, min(150.0, 10.0 * (args.steps + args.warmup)))
         print(json.dumps({"impl": "reference", "metric": "Mdeposits/s", "value": cb["value"], "unit": "Mdeposits/s",
                           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -647,7 +651,7 @@ def main():
         batch_arm(args)
     elif args.workload == SERVE_WORKLOAD:
         serve_arm(args)
-    elif args.workload == DEPOSIT_WORKLOAD:
+    elif args.workload in DEPOSIT_WORKLOADS:
         deposit_arm(args)
     else:
         gpu_arm(args)

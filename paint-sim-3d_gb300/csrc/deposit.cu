@@ -120,41 +120,87 @@ __device__ uint32_t lay_pack(uint32_t method, float dx, float dy) {
   return (method & 0xffu) | ((uint32_t)(fminf(fmaxf(turn, 0.f), 1.f) * 65535.0f) << 8);
 }
 
-// deposit.wgsl:31-75 for every cell of the grid (the stack of a cell that
-// receives paint gets each deposit's volume as a new top stratum)
-template <int MODE>
-__global__ void __launch_bounds__(256) k_deposit(cfk::Film F, const cf_deposit* __restrict__ deps,
-                                                 const uint32_t* __restrict__ tile_start,
-                                                 const uint32_t* __restrict__ tile_count,
-                                                 const uint32_t* __restrict__ tile_items) {
-  using namespace cfk;
-  const int i = (int)(blockIdx.x * 16 + threadIdx.x), j = (int)(blockIdx.y * 16 + threadIdx.y);
-  if (i >= (int)F.w || j >= (int)F.h) return;
-  const cf_params& P = F.P->p;
+// The deposits of the cell (i, j)'s 64x64-cell tile that pass the reach test
+// of deposit.wgsl:44-47 (centre within 1.415 r + 0.6 dx of the segment), in
+// list order; with SAMPLE, only those whose 4x4-supersampled height add
+// (deposit.wgsl:48-54) is > 0, with the add.
+struct DepTables {
+  const cf_deposit* deps;
+  const uint32_t* tile_start;
+  const uint32_t* tile_count;
+  const uint32_t* tile_items;
+};
+template <bool SAMPLE, class Fn>
+__device__ __forceinline__ void for_each_add(const cfk::Film& F, const cf_params& P, const DepTables& D, int i,
+                                             int j, Fn fn) {
   const uint32_t tile = (uint32_t)(i / 64) + (uint32_t)(j / 64) * P.tiles[0];
-  const uint32_t n = tile_count[tile];
+  const uint32_t n = D.tile_count[tile];
   if (n == 0u) return;
-  const uint32_t start = tile_start[tile];
-  const uint32_t c = idx(F, i, j);
+  const uint32_t start = D.tile_start[tile];
   const float px = ((float)i + 0.5f) * P.dx, py = ((float)j + 0.5f) * P.dx;
-  Stack s;  // loaded when the first deposit reaches the cell
-  float added = 0.f, top_add = 0.f;
-  uint32_t top_lay = 0u;
   for (uint32_t q = 0; q < n; ++q) {
-    const cf_deposit& d = deps[tile_items[start + q]];
+    const cf_deposit& d = D.deps[D.tile_items[start + q]];
     const float abx = d.p1[0] - d.p0[0], aby = d.p1[1] - d.p0[1];
     const float along = fminf(fmaxf(((px - d.p0[0]) * abx + (py - d.p0[1]) * aby) / fmaxf(abx * abx + aby * aby, 1e-30f),
                                     0.f), 1.f);
     const float reach = 1.415f * fmaxf(d.r0, d.r1) + 0.6f * P.dx;
     const float ox = px - d.p0[0] - along * abx, oy = py - d.p0[1] - along * aby;
     if (ox * ox + oy * oy > reach * reach) continue;
+    if (!SAMPLE) {
+      fn(d, 0.f, abx, aby);
+      continue;
+    }
     float add = 0.f;
     for (int sy = 0; sy < 4; ++sy)
       for (int sx = 0; sx < 4; ++sx) {
         const float sxf = ((float)sx - 1.5f) * (0.25f * P.dx), syf = ((float)sy - 1.5f) * (0.25f * P.dx);
         add += 0.0625f * ribbon_height(px + sxf, py + syf, d);
       }
-    if (add > 0.f) {
+    if (add > 0.f) fn(d, add, abx, aby);
+  }
+}
+
+// Pass 1 of deposit.wgsl:31-75, over the 64x64 tiles that list deposits (the
+// reference dispatches the whole grid; cells of other tiles return at once):
+// lists the cells that some deposit reaches, a superset of the cells that
+// receive paint.  No sampling and no stack, so the pass is light.
+__global__ void __launch_bounds__(256) k_deposit_mark(cfk::Film F, DepTables D, const uint32_t* __restrict__ tiles64,
+                                                      uint32_t* __restrict__ painted,
+                                                      uint32_t* __restrict__ painted_count) {
+  using namespace cfk;
+  // block b: 16x16 sub-tile (b % 16) of the b / 16-th 64x64 tile that lists deposits
+  const uint32_t t = tiles64[blockIdx.x >> 4], sub = blockIdx.x & 15u;
+  const uint32_t t64w = (F.w + 63u) / 64u;
+  const int i = (int)((t % t64w) * 64u + (sub & 3u) * 16u + threadIdx.x);
+  const int j = (int)((t / t64w) * 64u + (sub >> 2) * 16u + threadIdx.y);
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const cf_params& P = F.P->p;
+  bool any = false;
+  for_each_add<false>(F, P, D, i, j, [&](const cf_deposit&, float, float, float) { any = true; });
+  if (any) list_append(painted, painted_count, idx(F, i, j));
+}
+
+// Pass 2, one thread per listed cell: the cell's stack gets each deposit's
+// add > 0 as a new top stratum (stack_push_top, strata.wgsl:105-130), then h,
+// lay (the largest add's method and direction) and the tile's moved flag, as
+// deposit.wgsl:59-74 writes them; a listed cell that gets no paint is left
+// untouched.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_deposit_lay(cfk::Film F, DepTables D, const uint32_t* __restrict__ painted,
+                                                     const uint32_t* __restrict__ painted_count) {
+  using namespace cfk;
+  const cf_params& P = F.P->p;
+  __shared__ float lt[12];  // ln of the pigments' table viscosities, for the aggregates
+  if (threadIdx.x < 12) lt[threadIdx.x] = logf(fmaxf(F.pigtab[threadIdx.x * 40 + 32], 1e-3f));
+  __syncthreads();
+  const uint32_t count = *painted_count;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const uint32_t c = painted[e];
+    const int i = (int)(c % F.w), j = (int)(c / F.w);
+    Stack s;  // loaded when the first add arrives
+    float added = 0.f, top_add = 0.f;
+    uint32_t top_lay = 0u;
+    for_each_add<true>(F, P, D, i, j, [&](const cf_deposit& d, float add, float abx, float aby) {
       if (added == 0.f) stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
       float pig[16];
 #pragma unroll
@@ -170,9 +216,8 @@ __global__ void __launch_bounds__(256) k_deposit(cfk::Film F, const cf_deposit* 
         const float el = sqrtf(ex * ex + ey * ey);
         top_lay = lay_pack(d.kind >> METHOD_SHIFT, ex / el, ey / el);
       }
-    }
-  }
-  if (added > 0.f) {
+    });
+    if (!(added > 0.f)) continue;
     F.hh[c] = F.hh[c] + added;
     F.lay[c] = top_lay;
     F.tile_moved[(uint32_t)(i >> 4) + (uint32_t)(j >> 4) * F.tw] = 1u;  // mark_moved
@@ -180,15 +225,13 @@ __global__ void __launch_bounds__(256) k_deposit(cfk::Film F, const cf_deposit* 
     stack_store<MODE>(F, F.sh, F.scu, F.pig, c, s);
     F.dry_shaded[c] = 0u;
     // The next cure reads the composition aggregates of the stack instead of
-    // the stack itself: refresh them from the stored (rounded) strata, as the
-    // strata pass does for the cells it writes.
-    stack_load<MODE>(F, F.sh, F.scu, F.pig, c, s);
-    float lt[12];
-    lnmu_table(F.pigtab, lt);
-    float4 agg;
-    ushort4 col_unused;
-    finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, F.hh[c], F.m[c], s, agg, col_unused);
-    F.agg[c] = agg;
+    // the stack itself: refresh them from the strata as stored (rounded), as
+    // the strata pass does for the cells it writes.
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int q = 0; q < 16; ++q) s.pg[k][q] = PigIO<MODE>::round(s.pg[k][q]);
+    F.agg[c] = stack_agg(P, lt, s);
   }
 }
 
@@ -198,18 +241,24 @@ __global__ void __launch_bounds__(256) k_deposit(cfk::Film F, const cf_deposit* 
 // clears them; returns the number of launches.
 uint32_t launch_pending_deposits(cf_film* f, cudaStream_t st) {
   if (f->dep_pending == 0u) return 0u;
-  const dim3 g(f->tw, f->th), b(16, 16);
+  const DepTables D{f->d_deps, f->d_dep_tiles, f->d_dep_tiles + f->dep_nt, f->d_dep_items};
+  uint32_t* count = f->d_dep_tiles + 2 * f->dep_nt;
+  const uint32_t* tiles64 = f->d_dep_tiles + 2 * f->dep_nt + 1;  // the 64x64 tiles that list deposits
+  uint32_t* painted = f->F.fill_list;  // frame scratch: the frame's strata pass rebuilds it
+  if (cudaMemsetAsync(count, 0, sizeof(uint32_t), st) != cudaSuccess) return 0u;  // deposits stay pending
+  k_deposit_mark<<<f->dep_tiles_listed * 16u, dim3(16, 16), 0, st>>>(f->F, D, tiles64, painted, count);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const dim3 g((unsigned)std::max(sms, 1) * 4u), b(256);
   if (f->prec == CF_PREC_REFERENCE)
-    k_deposit<CF_PREC_REFERENCE><<<g, b, 0, st>>>(f->F, f->d_deps, f->d_dep_tiles, f->d_dep_tiles + f->dep_nt,
-                                                  f->d_dep_items);
+    k_deposit_lay<CF_PREC_REFERENCE><<<g, b, 0, st>>>(f->F, D, painted, count);
   else if (f->prec == CF_PREC_FP32)
-    k_deposit<CF_PREC_FP32><<<g, b, 0, st>>>(f->F, f->d_deps, f->d_dep_tiles, f->d_dep_tiles + f->dep_nt,
-                                             f->d_dep_items);
+    k_deposit_lay<CF_PREC_FP32><<<g, b, 0, st>>>(f->F, D, painted, count);
   else
-    k_deposit<CF_PREC_BF16><<<g, b, 0, st>>>(f->F, f->d_deps, f->d_dep_tiles, f->d_dep_tiles + f->dep_nt,
-                                             f->d_dep_items);
+    k_deposit_lay<CF_PREC_BF16><<<g, b, 0, st>>>(f->F, D, painted, count);
   f->dep_pending = 0u;
-  return 1u;
+  return 2u;
 }
 
 extern "C" {
@@ -315,13 +364,14 @@ cf_status cf_upload_deposits(cf_film* f, const cf_deposit* deps, uint32_t count,
     for (int64_t ty = ty0; ty <= ty1; ++ty)
       for (int64_t tx = tx0; tx <= tx1; ++tx) lists[(size_t)(ty * tx_n + tx)].push_back(di);
   }
-  std::vector<uint32_t> start(nt), cnt(nt), items;
+  std::vector<uint32_t> start(nt), cnt(nt), items, listed;
   const size_t cap = (size_t)CF_MAX_DEPOSITS * 16;  // tile_items holds 16 entries per deposit
   for (uint32_t t = 0; t < nt; ++t) {
     const size_t take = std::min(lists[t].size(), cap - items.size());
     start[t] = (uint32_t)items.size();
     cnt[t] = (uint32_t)take;
     items.insert(items.end(), lists[t].begin(), lists[t].begin() + (ptrdiff_t)take);
+    if (take) listed.push_back(t);
   }
   // device copies (grown as needed; the previous frame's are no longer read
   // once the stream has passed them)
@@ -338,15 +388,19 @@ cf_status cf_upload_deposits(cf_film* f, const cf_deposit* deps, uint32_t count,
     CUDA_TRY(f, cudaMalloc(&f->d_dep_items, sizeof(uint32_t) * std::max<size_t>(items.size(), 1)));
     f->dep_items_cap = items.size();
   }
-  if (!f->d_dep_tiles) {
-    CUDA_TRY(f, cudaMalloc(&f->d_dep_tiles, sizeof(uint32_t) * 2 * nt));
+  if (!f->d_dep_tiles) {  // start[nt], count[nt], the painted-cell counter, the listed tiles[<= nt]
+    CUDA_TRY(f, cudaMalloc(&f->d_dep_tiles, sizeof(uint32_t) * (3 * nt + 1)));
     f->dep_nt = nt;
   }
   if (count) CUDA_TRY(f, cudaMemcpy(f->d_deps, deps, sizeof(cf_deposit) * count, cudaMemcpyHostToDevice));
   CUDA_TRY(f, cudaMemcpy(f->d_dep_tiles, start.data(), sizeof(uint32_t) * nt, cudaMemcpyHostToDevice));
   CUDA_TRY(f, cudaMemcpy(f->d_dep_tiles + nt, cnt.data(), sizeof(uint32_t) * nt, cudaMemcpyHostToDevice));
-  if (!items.empty())
+  if (!items.empty()) {
     CUDA_TRY(f, cudaMemcpy(f->d_dep_items, items.data(), sizeof(uint32_t) * items.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(f, cudaMemcpy(f->d_dep_tiles + 2 * nt + 1, listed.data(), sizeof(uint32_t) * listed.size(),
+                           cudaMemcpyHostToDevice));
+  }
+  f->dep_tiles_listed = (uint32_t)listed.size();
   f->dep_pending = items.empty() ? 0u : count;
   if (sent) *sent = count;
   if (total_deposited) *total_deposited = f->total_deposited;

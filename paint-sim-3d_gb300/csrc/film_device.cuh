@@ -128,6 +128,18 @@ __device__ __forceinline__ uint32_t idx(const Film& F, int i, int j) { return (u
 __device__ __forceinline__ bool in_grid(const Film& F, int i, int j) {
   return i >= 0 && j >= 0 && i < (int)F.w && j < (int)F.h;
 }
+// Appends v to a device list; one atomic per warp (the threads of the warp
+// that append at this point).
+__device__ __forceinline__ void list_append(uint32_t* list, uint32_t* count, uint32_t v) {
+  const unsigned m = __activemask();
+  const int lane = (int)((threadIdx.y * blockDim.x + threadIdx.x) & 31u);
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  list[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
 __device__ __forceinline__ bool cell_active(const Film& F, int i, int j) {  // film.wgsl:128-131
   return (F.tile_flags[(uint32_t)(i >> 4) + (uint32_t)(j >> 4) * F.tw] & ACTIVE) != 0u;
 }
@@ -218,6 +230,12 @@ struct PigIO {
       }
       base[at(F, c, k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
     }
+  }
+  // a slot value as the store above keeps it
+  __device__ static __forceinline__ float round(float v) {
+    if constexpr (MODE == CF_PREC_FP32) return v;
+    else if constexpr (MODE == CF_PREC_REFERENCE) return h16_to_f(f_to_h16(v));
+    else return b16_to_f(f_to_b16(v));
   }
   // bit-exact copy of stratum ks of cell cs (in src) to stratum kd of cell cd (in dst)
   __device__ static __forceinline__ void copy(const Film& F, uint4* dst, uint32_t cd, int kd, const uint4* src,

@@ -45,7 +45,7 @@ struct cf_film {
   uint32_t* d_dep_tiles = nullptr;  // start[nt64], count[nt64]
   uint32_t* d_dep_items = nullptr;
   size_t dep_cap = 0, dep_items_cap = 0;
-  uint32_t dep_nt = 0, dep_pending = 0;
+  uint32_t dep_nt = 0, dep_pending = 0, dep_tiles_listed = 0;
   double total_deposited = 0.0;  // volume laid inside the canvas (upload_deposits)
 };
 

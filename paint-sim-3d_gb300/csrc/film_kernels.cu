@@ -545,18 +545,6 @@ __device__ __forceinline__ bool not_compact(const cf_params& P, float hc, float4
   return false;
 }
 
-// Appends v to a device list; one atomic per warp (the threads of the warp
-// that append at this point).
-__device__ __forceinline__ void list_append(uint32_t* list, uint32_t* count, uint32_t v) {
-  const unsigned m = __activemask();
-  const int lane = (int)((threadIdx.y * blockDim.x + threadIdx.x) & 31u);
-  const int leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-  base = __shfl_sync(m, base, leader);
-  list[base + __popc(m & ((1u << lane) - 1u))] = v;
-}
-
 // ---- face passes: fluxes and strata_split over the live faces of a tile ----
 // Face k of cell (i, j) joins cell (i + FACE_DI[k], j + FACE_DJ[k]).
 __device__ __constant__ int FACE_DI[4] = {1, 0, 1, 1};

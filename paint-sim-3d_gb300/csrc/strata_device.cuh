@@ -203,30 +203,34 @@ struct CellAcc {
       r[2 * k + 1] = h16_to_f(wv[k] >> 16);
     }
   }
+  // the composition part of a stratum of thickness t > 0 (cure.wgsl:3-48)
+  __device__ __forceinline__ void add_comp(float t, const float* pg, const float* lnmu_tab) {
+    total += t;
+    float csum = 0.f, lm = 0.f, ty = 0.f;
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+      float cc = pg[q];
+      if (cc > 0.f) {
+        csum += cc;
+        lm += cc * lnmu_tab[q];
+        ty += cc * pg[13];
+      }
+    }
+    if (pg[14] > 0.f) lm = csum * (pg[14] - 10.0f);
+    if (csum > 0.f) {
+      lnmu += t * lm / csum;
+      tau += t * ty / csum;
+      wsum += t;
+      if (pg[15] > 0.f) { nsum += t * pg[15]; nw += t; }
+    }
+    thin += t * pg[12];
+  }
   // stratum k (in order 0..3) of thickness t, cure u and slots pg
   __device__ __forceinline__ void add(int k, float t, float u, const float* pg, float hv, const float* lnmu_tab,
                                       const float* tab, bool debug) {
     ssum += t;
     if (t > 0.f) {
-      total += t;
-      float csum = 0.f, lm = 0.f, ty = 0.f;
-#pragma unroll
-      for (int q = 0; q < 12; ++q) {
-        float cc = pg[q];
-        if (cc > 0.f) {
-          csum += cc;
-          lm += cc * lnmu_tab[q];
-          ty += cc * pg[13];
-        }
-      }
-      if (pg[14] > 0.f) lm = csum * (pg[14] - 10.0f);
-      if (csum > 0.f) {
-        lnmu += t * lm / csum;
-        tau += t * ty / csum;
-        wsum += t;
-        if (pg[15] > 0.f) { nsum += t * pg[15]; nw += t; }
-      }
-      thin += t * pg[12];
+      add_comp(t, pg, lnmu_tab);
       if (hv > 0.f) {
         float w[12], sc;
         layer_weights(pg, tab, w, sc);
@@ -315,6 +319,17 @@ __device__ __forceinline__ void rheo_from_parts(const cf_params& P, float4 agg, 
 __device__ __forceinline__ void lnmu_table(const float* pigtab, float out[12]) {
 #pragma unroll
   for (int q = 0; q < 12; ++q) out[q] = logf(fmaxf(pigtab[q * 40 + 32], 1e-3f));
+}
+
+// The composition aggregates alone of a whole in-register stack (bitwise the
+// ones finish_stack gives), for passes that change a stack but not its colour.
+__device__ inline float4 stack_agg(const cf_params& P, const float* lnmu_tab, const Stack& s) {
+  CellAcc a;
+  a.total = a.lnmu = a.tau = a.thin = a.wsum = a.nsum = a.nw = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (s.th[k] > 0.f) a.add_comp(s.th[k], s.pg[k], lnmu_tab);
+  return a.agg(P);
 }
 
 // Aggregates and colour of a whole in-register stack.
