@@ -1494,6 +1494,369 @@ struct Film {
     for (long c = 0; c < (long)N; ++c) k_shade_cell((size_t)c);
   }
 
+  // ---- implicit hydrostatic CG steps (film.wgsl:895-1207; dispatched by
+  // Film::encode_frame, src/film/mod.rs:1373-1408) ----
+  // The system and the flux of each step live on the active tiles; planes
+  // of inactive tiles keep the values of the last step that covered them,
+  // and the reference reads those (cg_m, cg_p of a neighbour) as they are.
+  std::vector<R> cg_m /*4N*/, cg_d, cg_x, cg_r, cg_p, cg_q, cg_t, cg_t2;
+  std::vector<R> cg_part, cg_part2;  // per active tile (list position)
+  R cg_s[2][4] = {};
+  std::vector<uint32_t> cg_tiles;  // active tiles in compact_tiles' order
+
+  void cg_alloc() {
+    if (cg_d.size() == N) return;
+    cg_m.assign(4 * N, 0);
+    for (auto* v : {&cg_d, &cg_x, &cg_r, &cg_p, &cg_q, &cg_t, &cg_t2}) v->assign(N, 0);
+    cg_part.assign((size_t)TW * TH, 0);
+    cg_part2.assign((size_t)TW * TH, 0);
+  }
+  // film.wgsl:895-923 (the mobility of a face; the flow index of the face as
+  // in face(): the per-cell extension reduces to phys.z)
+  R face_mob(size_t ca, size_t cb, V gcap, V ghyd, V gtilt, bool diag) const {
+    R ha = h[ca], hb = h[cb];
+    if (std::min(ha, hb) <= 0) return 0;
+    R hf = F(0.5f) * (ha + hb);
+    R rax = rheo[3 * ca], ray = rheo[3 * ca + 1], rbx = rheo[3 * cb], rby = rheo[3 * cb + 1];
+    R wa = ha / (ha + hb);
+    R wb = R(1) - wa;
+    R mu = std::exp(wa * std::log(std::max(rax, F(1e-4f))) + wb * std::log(std::max(rbx, F(1e-4f))));
+    R ty = wa * ray + wb * rby;
+    R na = cell_n(ca), nb = cell_n(cb);
+    R nf = na == nb ? na : wa * na + wb * nb;
+    R thin = std::min(ha, hb) / hf;
+    R fcap = thin * thin * thin;
+    V yc = yield_cap(V{gcap.x * fcap, gcap.y * fcap}, ty);
+    V gg{yc.x + ghyd.x + gtilt.x, yc.y + ghyd.y + gtilt.y};
+    R gmag = len(gg.x, gg.y);
+    R qy[3];
+    hb_flux(gmag, yield_depth(ca, cb, hf, ty, gg), mu, ty, nf, qy);
+    if (qy[0] <= 0) return 0;
+    R mob = std::min(std::max(qy[0] / gmag - misc[3], R(0)), front[2]);
+    if (std::min(ha, hb) < F(0.5f) * std::max(ha, hb)) {
+      if (diag) return 0;
+      size_t tgt = hb > ha ? ca : cb;
+      mob = mob / std::pow((R)std::max(feeders(tgt), 1u), F(0.7f));
+    }
+    return mob;
+  }
+  R kappa() const { return front[3] * phys[0] * g[2] * inv_dx * inv_dx; }  // film.wgsl:925-927
+  R hold_u(size_t c) const {  // film.wgsl:929-933
+    R hold = 0;
+    if (h[c] > 0) hold = hold_level(nose_dist(c));
+    return m[c] - hold;
+  }
+  // film.wgsl:935-987
+  void k_cg_setup_cell(int i, int j) {
+    size_t c = idx(i, j);
+    R mob[4] = {0, 0, 0, 0};
+    V p00 = pressure_at(i, j);
+    V gxy{phys[0] * g[0], phys[0] * g[1]};
+    const R s2 = F(0.70710678f);
+    if (i + 1 < (int)W && cell_active(i + 1, j)) {
+      size_t cb = idx(i + 1, j);
+      V p10 = pressure_at(i + 1, j);
+      V gm{-(p10.x - p00.x) * inv_dx, -(p10.y - p00.y) * inv_dx};
+      V a = pressure_wet(i, j + 1, p00), b = pressure_wet(i + 1, j + 1, p10);
+      V cc = pressure_wet(i, j - 1, p00), d = pressure_wet(i + 1, j - 1, p10);
+      V pt{a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y};
+      V gt{-pt.x * F(0.25f) * inv_dx, -pt.y * F(0.25f) * inv_dx};
+      mob[0] = face_mob(c, cb, V{gm.x, gt.x}, V{gm.y, gt.y}, gxy, false);
+    }
+    if (j + 1 < (int)H && cell_active(i, j + 1)) {
+      size_t cb = idx(i, j + 1);
+      V p01 = pressure_at(i, j + 1);
+      V gm{-(p01.x - p00.x) * inv_dx, -(p01.y - p00.y) * inv_dx};
+      V a = pressure_wet(i + 1, j, p00), b = pressure_wet(i + 1, j + 1, p01);
+      V cc = pressure_wet(i - 1, j, p00), d = pressure_wet(i - 1, j + 1, p01);
+      V pt{a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y};
+      V gt{-pt.x * F(0.25f) * inv_dx, -pt.y * F(0.25f) * inv_dx};
+      mob[1] = face_mob(c, cb, V{gm.x, gt.x}, V{gm.y, gt.y}, V{gxy.y, gxy.x}, false);
+    }
+    if (i + 1 < (int)W && j + 1 < (int)H && cell_active(i + 1, j + 1)) {
+      size_t cb = idx(i + 1, j + 1);
+      V p11 = pressure_at(i + 1, j + 1);
+      V ga{-(p11.x - p00.x) * inv_dx * s2, -(p11.y - p00.y) * inv_dx * s2};
+      V pa = pressure_wet(i + 1, j, p00), pb = pressure_wet(i, j + 1, p11);
+      V gp{-(pa.x - pb.x) * inv_dx * s2, -(pa.y - pb.y) * inv_dx * s2};
+      V gt{(gxy.x + gxy.y) * s2, (gxy.x - gxy.y) * s2};
+      mob[2] = face_mob(c, cb, V{ga.x, gp.x}, V{ga.y, gp.y}, gt, true);
+    }
+    if (i + 1 < (int)W && j > 0 && cell_active(i + 1, j - 1)) {
+      size_t cb = idx(i + 1, j - 1);
+      V p1m = pressure_at(i + 1, j - 1);
+      V ga{-(p1m.x - p00.x) * inv_dx * s2, -(p1m.y - p00.y) * inv_dx * s2};
+      V pa = pressure_wet(i + 1, j, p00), pb = pressure_wet(i, j - 1, p1m);
+      V gp{-(pa.x - pb.x) * inv_dx * s2, -(pa.y - pb.y) * inv_dx * s2};
+      V gt{(gxy.x - gxy.y) * s2, (gxy.x + gxy.y) * s2};
+      mob[3] = face_mob(c, cb, V{ga.x, gp.x}, V{ga.y, gp.y}, gt, true);
+    }
+    for (int k = 0; k < 4; ++k) cg_m[4 * c + k] = mob[k];
+  }
+  // film.wgsl:994-1010: neighbour k of (i, j) and the weighted mobility of
+  // the face to it (the faces of the lower-left neighbours are theirs)
+  bool cg_nb(int k, int i, int j, size_t& nc, R& mw) const {
+    size_t c = idx(i, j);
+    nc = 0;
+    mw = 0;
+    const R wa = F(0.6666667f), wd = F(0.16666667f);
+    switch (k) {
+      case 0: if (i + 1 < (int)W) { nc = idx(i + 1, j); mw = wa * cg_m[4 * c]; } break;
+      case 1: if (j + 1 < (int)H) { nc = idx(i, j + 1); mw = wa * cg_m[4 * c + 1]; } break;
+      case 2: if (i + 1 < (int)W && j + 1 < (int)H) { nc = idx(i + 1, j + 1); mw = wd * cg_m[4 * c + 2]; } break;
+      case 3: if (i + 1 < (int)W && j > 0) { nc = idx(i + 1, j - 1); mw = wd * cg_m[4 * c + 3]; } break;
+      case 4: if (i > 0) { nc = idx(i - 1, j); mw = wa * cg_m[4 * nc]; } break;
+      case 5: if (j > 0) { nc = idx(i, j - 1); mw = wa * cg_m[4 * nc + 1]; } break;
+      case 6: if (i > 0 && j > 0) { nc = idx(i - 1, j - 1); mw = wd * cg_m[4 * nc + 2]; } break;
+      default: if (i > 0 && j + 1 < (int)H) { nc = idx(i - 1, j + 1); mw = wd * cg_m[4 * nc + 3]; } break;
+    }
+    return mw > 0;
+  }
+  // film.wgsl:1012-1021
+  R lap_src(size_t c, int which) const {
+    switch (which) {
+      case 0: return cg_p[c];
+      case 1: return h[c];
+      case 2: return cg_t2[c];
+      case 3: return cg_t[c];
+      case 4: return cg_x[c] + hold_u(c);
+      default: return hold_u(c);
+    }
+  }
+  // film.wgsl:1023-1043
+  R lap_w(int i, int j, size_t c, int which) const {
+    R vc = lap_src(c, which), acc_v = 0;
+    for (int dj = -1; dj <= 1; ++dj)
+      for (int di = -1; di <= 1; ++di) {
+        if (di == 0 && dj == 0) continue;
+        int x = i + di, y = j + dj;
+        if (x < 0 || y < 0 || x >= (int)W || y >= (int)H) continue;
+        if (!cell_active(x, y)) continue;
+        size_t n = idx(x, y);
+        if (h[n] <= 0) continue;
+        R w = (di != 0 && dj != 0) ? F(0.16666667f) : F(0.6666667f);
+        acc_v += w * (lap_src(n, which) - vc);
+      }
+    return acc_v;
+  }
+  // film.wgsl:1045-1064
+  R lap_diag(int i, int j) const {
+    R s1 = 0, s2 = 0;
+    for (int dj = -1; dj <= 1; ++dj)
+      for (int di = -1; di <= 1; ++di) {
+        if (di == 0 && dj == 0) continue;
+        int x = i + di, y = j + dj;
+        if (x < 0 || y < 0 || x >= (int)W || y >= (int)H) continue;
+        if (!cell_active(x, y)) continue;
+        if (h[idx(x, y)] <= 0) continue;
+        R w = (di != 0 && dj != 0) ? F(0.16666667f) : F(0.6666667f);
+        s1 += w;
+        s2 += w * w;
+      }
+    return s1 * s1 + s2;
+  }
+  // film.wgsl:1085-1095
+  R apply_a(int i, int j, size_t c) const {
+    R k = kappa(), pc = cg_p[c], acc_v = pc;
+    for (int f = 0; f < 8; ++f) {
+      size_t nc;
+      R mw;
+      if (cg_nb(f, i, j, nc, mw)) acc_v += k * mw * (pc - cg_p[nc]);
+    }
+    if (h[c] > 0) acc_v += front3[0] * lap_w(i, j, c, 3);
+    return acc_v;
+  }
+  // film.wgsl:1110-1141
+  R k_cg_init_cell(int i, int j) {
+    size_t c = idx(i, j);
+    R k = kappa(), hc = h[c], uc = hold_u(c);
+    R diag = 1, b = hc, ax = hc;
+    for (int f = 0; f < 8; ++f) {
+      size_t nc;
+      R mw;
+      if (cg_nb(f, i, j, nc, mw)) {
+        diag += k * mw;
+        b += k * mw * (hold_u(nc) - uc);
+        ax += k * mw * (hc - h[nc]);
+      }
+    }
+    if (hc > 0) {
+      R cc = front3[0];
+      diag += cc * lap_diag(i, j);
+      b -= cc * lap_w(i, j, c, 2);
+      ax += cc * lap_w(i, j, c, 3);
+    }
+    R r = b - ax;
+    cg_d[c] = diag;
+    cg_x[c] = hc;
+    cg_r[c] = r;
+    cg_p[c] = r / diag;
+    return r * r / diag;
+  }
+  R pot(size_t c, const std::vector<R>& hh) const {  // film.wgsl:1227-1229, h as of before cg_finish
+    R hold = 0;
+    if (hh[c] > 0) hold = hold_level(nose_dist(c));
+    return cg_x[c] + (m[c] - hold);
+  }
+  // film.wgsl:1232-1274 (reads h as of before the dispatch: Jacobi)
+  void k_cg_finish_cell(int i, int j, const std::vector<R>& h_old, R& dv, R& tv, bool& moved) {
+    size_t c = idx(i, j);
+    R h0 = h_old[c], hn = std::max(cg_x[c], R(0));
+    R rg = phys[0] * g[2] * inv_dx, pc = pot(c, h_old);
+    const R wa = F(0.6666667f), wdf = F(0.23570226f), s2 = F(0.70710678f);
+    R f[4] = {0, 0, 0, 0};
+    const R* mob = &cg_m[4 * c];
+    if (mob[0] > 0) f[0] = wa * mob[0] * rg * (pc - pot(idx(i + 1, j), h_old));
+    if (mob[1] > 0) f[1] = wa * mob[1] * rg * (pc - pot(idx(i, j + 1), h_old));
+    if (mob[2] > 0) f[2] = wdf * mob[2] * rg * (pc - pot(idx(i + 1, j + 1), h_old)) * s2;
+    if (mob[3] > 0) f[3] = wdf * mob[3] * rg * (pc - pot(idx(i + 1, j - 1), h_old)) * s2;
+    if (h0 > 0) {
+      R kc = front3[1], tc = cg_t[c];
+      if (i + 1 < (int)W) { size_t n = idx(i + 1, j); if (h_old[n] > 0 && cell_active(i + 1, j)) f[0] += wa * kc * (cg_t[n] - tc); }
+      if (j + 1 < (int)H) { size_t n = idx(i, j + 1); if (h_old[n] > 0 && cell_active(i, j + 1)) f[1] += wa * kc * (cg_t[n] - tc); }
+      if (i + 1 < (int)W && j + 1 < (int)H) { size_t n = idx(i + 1, j + 1); if (h_old[n] > 0 && cell_active(i + 1, j + 1)) f[2] += wdf * kc * (cg_t[n] - tc) * s2; }
+      if (i + 1 < (int)W && j > 0) { size_t n = idx(i + 1, j - 1); if (h_old[n] > 0 && cell_active(i + 1, j - 1)) f[3] += wdf * kc * (cg_t[n] - tc) * s2; }
+    }
+    for (int k = 0; k < 4; ++k) acc[4 * c + k] += f[k] * front[3];
+    h[c] = hn;
+    moved = std::fabs(hn - h0) > F(1e-6f);
+    dv = hn - h0;
+    tv = hn;
+  }
+  // the shader's workgroup tree: for s = 128 .. 1, a[li] += a[li + s]
+  static R tree256(R* a) {
+    for (int st = 128; st > 0; st >>= 1)
+      for (int li = 0; li < st; ++li) a[li] += a[li + st];
+    return a[0];
+  }
+  // total_parts (film.wgsl:1157-1168): strided sums of the tile partials, then the tree
+  R total_parts(const std::vector<R>& part) const {
+    R a[256];
+    for (size_t l = 0; l < 256; ++l) {
+      R v = 0;
+      for (size_t t = l; t < cg_tiles.size(); t += 256) v += part[t];
+      a[l] = v;
+    }
+    return tree256(a);
+  }
+  // a tile-list dispatch whose invocations each give one value v (0 outside
+  // the grid) summed per tile by the workgroup tree into part[w]
+  template <class Fn>
+  void cg_tiles_sum(std::vector<R>& part, Fn fn) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long w = 0; w < (long)cg_tiles.size(); ++w) {
+      uint32_t t = cg_tiles[w];
+      R a[256];
+      for (int li = 0; li < 256; ++li) {
+        int i = (int)(t % TW) * 16 + li % 16, j = (int)(t / TW) * 16 + li / 16;
+        a[li] = in_grid(i, j) ? fn(i, j) : R(0);
+      }
+      part[w] = tree256(a);
+    }
+  }
+  template <class Fn>
+  void cg_tiles_each(Fn fn) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long w = 0; w < (long)cg_tiles.size(); ++w) {
+      uint32_t t = cg_tiles[w];
+      for (int li = 0; li < 256; ++li) {
+        int i = (int)(t % TW) * 16 + li % 16, j = (int)(t / TW) * 16 + li / 16;
+        if (in_grid(i, j)) fn(i, j);
+      }
+    }
+  }
+  // one implicit step (src/film/mod.rs:1374-1407)
+  void run_implicit_step(uint32_t iters) {
+    cg_alloc();
+    cg_tiles.clear();
+    for (uint32_t t = 0; t < TW * TH; ++t)
+      if (tile_flags[t] & 32u) cg_tiles.push_back(t);
+    run_laplacian();
+    cg_tiles_each([&](int i, int j) { k_cg_setup_cell(i, j); });
+    cg_tiles_each([&](int i, int j) {  // cg_lap_h
+      size_t c = idx(i, j);
+      cg_t[c] = lap_w(i, j, c, 1);
+      cg_t2[c] = lap_w(i, j, c, 5);
+    });
+    cg_tiles_sum(cg_part, [&](int i, int j) { return k_cg_init_cell(i, j); });
+    R rz = total_parts(cg_part);  // cg_reduce_init
+    for (int k = 0; k < 4; ++k) cg_s[0][k] = cg_s[1][k] = 0;
+    cg_s[0][0] = cg_s[1][0] = rz;
+    for (uint32_t it = 0; it < iters; ++it) {
+      cg_tiles_each([&](int i, int j) { size_t c = idx(i, j); cg_t[c] = lap_w(i, j, c, 0); });  // cg_lap_p
+      cg_tiles_sum(cg_part, [&](int i, int j) {  // cg_iter_a
+        size_t c = idx(i, j);
+        R q = apply_a(i, j, c);
+        cg_q[c] = q;
+        return cg_p[c] * q;
+      });
+      {  // cg_reduce_a
+        R pq = total_parts(cg_part), alpha = 0;
+        if (pq > 0) alpha = cg_s[0][0] / pq;
+        cg_s[0][1] = pq;
+        cg_s[0][2] = alpha;
+        cg_s[0][3] = 0;
+      }
+      R alpha = cg_s[0][2];
+      cg_tiles_sum(cg_part, [&](int i, int j) {  // cg_iter_b
+        size_t c = idx(i, j);
+        R r = cg_r[c] - alpha * cg_q[c];
+        cg_x[c] = cg_x[c] + alpha * cg_p[c];
+        cg_r[c] = r;
+        return r * r / cg_d[c];
+      });
+      {  // cg_reduce_b
+        R rz2 = total_parts(cg_part), beta = 0;
+        if (cg_s[0][0] > 0) beta = rz2 / cg_s[0][0];
+        cg_s[0][0] = rz2;
+        cg_s[0][3] = beta;
+      }
+      R beta = cg_s[0][3];
+      cg_tiles_each([&](int i, int j) { size_t c = idx(i, j); cg_p[c] = cg_r[c] / cg_d[c] + beta * cg_p[c]; });
+    }
+    cg_tiles_each([&](int i, int j) { size_t c = idx(i, j); cg_t[c] = lap_w(i, j, c, 4); });  // cg_lap_u
+    {  // cg_finish
+      std::vector<R> h_old = h;
+#pragma omp parallel for schedule(dynamic, 1)
+      for (long w = 0; w < (long)cg_tiles.size(); ++w) {
+        uint32_t t = cg_tiles[w];
+        R a[256], tv_sum = 0;
+        bool any = false;
+        R tvs[256];
+        for (int li = 0; li < 256; ++li) {
+          int i = (int)(t % TW) * 16 + li % 16, j = (int)(t / TW) * 16 + li / 16;
+          R dv = 0, tv = 0;
+          bool mv = false;
+          if (in_grid(i, j)) k_cg_finish_cell(i, j, h_old, dv, tv, mv);
+          a[li] = dv;
+          tvs[li] = tv;
+          any = any || mv;
+        }
+        cg_part[w] = tree256(a);
+        for (int li = 0; li < 256; ++li) tv_sum += tvs[li];
+        cg_part2[w] = tv_sum;
+        if (any) tile_moved[t] = 1u;
+      }
+    }
+    {  // cg_reduce_mass
+      R a[256], b[256];
+      for (size_t l = 0; l < 256; ++l) {
+        R d = 0, tot = 0;
+        for (size_t t = l; t < cg_tiles.size(); t += 256) { d += cg_part[t]; tot += cg_part2[t]; }
+        a[l] = d;
+        b[l] = tot;
+      }
+      for (int st = 128; st > 0; st >>= 1)
+        for (int li = 0; li < st; ++li) { a[li] += a[li + st]; b[li] += b[li + st]; }
+      R x1 = cg_s[1][0], s0x = cg_s[0][0];
+      cg_s[1][0] = x1; cg_s[1][1] = a[0]; cg_s[1][2] = b[0]; cg_s[1][3] = s0x;
+    }
+    if (cg_s[1][2] > 0) {  // cg_rescale
+      R fr = R(1) - cg_s[1][1] / cg_s[1][2];
+      cg_tiles_each([&](int i, int j) { size_t c = idx(i, j); h[c] = std::max(h[c] * fr, R(0)); });
+    }
+  }
+
   // ---- deposits (shaders/deposit.wgsl; tables binned by upload_deposits,
   // src/film/mod.rs:1175-1224, on the host) ----
   std::vector<cf_deposit> deps;
@@ -1591,8 +1954,9 @@ struct Film {
   }
 
   // Film::encode_frame, src/film/mod.rs:1322-1462 (simulation portion;
-  // journal / brush / knife / CG / slump / pool8 are not on the path).  The
-  // deposits uploaded since the last frame are laid first, then dropped.
+  // journal / brush / knife / slump / pool8 are not on the path).  The
+  // deposits uploaded since the last frame are laid first, then dropped; the
+  // implicit hydrostatic steps run after clear_acc.
   void encode_frame(uint32_t substeps) {
     if (!dep_items.empty()) run_deposit();
     dep_items.clear();
@@ -1600,6 +1964,7 @@ struct Film {
     k_compact_tiles();
     run_cure();
     run_clear_acc();
+    for (uint32_t s = 0; s < PF.implicit_steps; ++s) run_implicit_step(S.implicit_iters);
     for (uint32_t s = 0; s < substeps; ++s) {
       run_laplacian();
       run_plug();

@@ -146,6 +146,12 @@ class Oracle:
     def set_params(self, p):
         self.L.cfo_set_params(self.p, C.byref(p))
 
+    def implicit_steps(self):
+        """Film::implicit_steps of the last update_params (0 with implicit_hydro off)."""
+        p, n = Params(), C.c_uint32()
+        self.L.cfo_get_params(self.p, C.byref(p), C.byref(n))
+        return n.value
+
     def choose_substeps(self, frame_dt):
         return self.L.cfo_choose_substeps(self.p, frame_dt)
 
@@ -206,6 +212,7 @@ def ref_lib():
         L.wgr_run.restype = C.c_int
         u32p = C.POINTER(C.c_uint32)
         L.wgr_set_deposits.argtypes = [C.c_void_p, C.c_uint32, u32p, u32p, C.c_uint32, u32p, C.c_uint32]
+        L.wgr_set_implicit.argtypes = [C.c_uint32, C.c_uint32]
         L.wgr_buffer.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_int]
         L.wgr_buffer.restype = C.c_int
         L.wgr_active_count.restype = C.c_uint32
@@ -263,6 +270,10 @@ class RefShaders:
 
     def run(self, kernel):
         assert self.L.wgr_run(kernel.encode()), kernel
+
+    def set_implicit(self, steps, iters):
+        """Film::implicit_steps and FilmSettings::implicit_iters for the next frames."""
+        self.L.wgr_set_implicit(steps, iters)
 
     def set_deposits(self, deps, start, cnt, items):
         """Deposits for the next frame with tile tables from the

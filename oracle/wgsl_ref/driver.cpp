@@ -12,7 +12,10 @@
 //    tree (a max/min) are emulated here around the translated per-cell code;
 //  - nose and strata_fill read `__old` snapshots (Jacobi semantics).
 //  - deposits uploaded by wgr_set_deposits are laid by the translated
-//    deposit entry point at the start of the next frame.
+//    deposit entry point at the start of the next frame;
+//  - the implicit hydrostatic CG steps (wgr_set_implicit) run after
+//    clear_acc; their workgroup and single-workgroup sums are completed in the
+//    shader's tree order, and cg_finish reads h as of before the dispatch.
 // One film per process (the translated buffers are module globals).
 #include <algorithm>
 #include <array>
@@ -25,6 +28,40 @@
 
 #include "../film_oracle.hpp"
 #include "ref_shaders.inc"
+
+// Workgroup-at-a-time definitions of the helpers whose barriers sit inside
+// them (common.wgsl:112-120, film.wgsl:1099-1107 and 1157-1168): the driver
+// runs a workgroup's 256 invocations one after the other, then finishes the
+// barrier's work in the shader's order.
+namespace wg {
+u32 wg_flag = 0u, wg_slot = 0u;
+bool wg_reduced = false;
+void begin_motion(u32) {}
+void end_motion(bool moved, vec3<u32>, u32) {
+  if (moved) wg_flag = 1u;
+}
+void wg_reduce(u32 li, f32 v, u32 slot) {
+  wg_sum[li] = v;
+  wg_slot = slot;
+  wg_reduced = true;
+}
+// the shader's tree: for s = 128, 64, .., 1: a[li] += a[li + s] for li < s
+f32 tree_sum(array<f32, 256>& a) {
+  for (u32 st = 128u; st > 0u; st >>= 1u)
+    for (u32 li = 0; li < st; ++li) a[li] += a[li + st];
+  return a[0];
+}
+// each invocation's strided sum of the tile partials, then the tree
+f32 total_parts(u32) {
+  const u32 n = active_count[0];
+  for (u32 l = 0; l < 256u; ++l) {
+    f32 v = f32(0);
+    for (u32 t = l; t < n; t += 256u) v += cg_part[t];
+    wg_sum[l] = v;
+  }
+  return tree_sum(wg_sum);
+}
+}  // namespace wg
 
 using namespace wg;
 
@@ -109,6 +146,90 @@ void run_strata_fill() {
 }
 
 bool dep_pending = false;  // deposits uploaded since the last frame
+u32 impl_steps = 0u, impl_iters = 40u;  // Film::implicit_steps, FilmSettings::implicit_iters
+
+// A tile-list dispatch of an entry with workgroup sums: invocations run in
+// descending local index, so the li == 0 code after a barrier sees every
+// invocation's workgroup writes; the partial of wg_reduce and the moved flag
+// of end_motion are completed after each workgroup.
+void dispatch_tiles_wg(void (*fn)(vec3<u32>, vec3<u32>, u32)) {
+  u32 n = active_count[0];
+  for (u32 w = 0; w < n; ++w) {
+    wg_flag = 0u;
+    wg_reduced = false;
+    for (int li = 255; li >= 0; --li) fn(vec3<u32>(w, 0, 0), vec3<u32>((u32)li % 16u, (u32)li / 16u, 0), (u32)li);
+    if (wg_reduced) cg_part[wg_slot] = tree_sum(wg_sum);
+    if (wg_flag) tile_moved[tile_list[w]] = 1u;
+  }
+}
+
+// single-workgroup reductions: invocation 0 writes
+void dispatch_one(void (*fn)(u32)) {
+  for (int li = 255; li >= 0; --li) fn((u32)li);
+}
+
+// cg_reduce_mass (film.wgsl:1190-1207): two strided sums and trees
+void run_cg_reduce_mass() {
+  const u32 n = active_count[0];
+  array<f32, 256> a{}, b{};
+  for (u32 l = 0; l < 256u; ++l) {
+    f32 d = f32(0), tot = f32(0);
+    for (u32 t = l; t < n; t += 256u) { d += cg_part[t]; tot += cg_part2[t]; }
+    a[l] = d;
+    b[l] = tot;
+  }
+  for (u32 st = 128u; st > 0u; st >>= 1u)
+    for (u32 li = 0; li < st; ++li) { a[li] += a[li + st]; b[li] += b[li + st]; }
+  const vec4<f32> s1 = cg_s[1];
+  cg_s[1] = vec4<f32>(s1.x, a[0], b[0], cg_s[0].x);
+}
+
+// cg_finish writes h[c] while its neighbours' pot() reads h: the reads see
+// the h of before the dispatch (Jacobi, as in the oracle).
+void run_cg_finish() {
+  std::vector<f32> h_old = h.v, h_new = h.v;
+  u32 n = active_count[0];
+  for (u32 w = 0; w < n; ++w) {
+    wg_flag = 0u;
+    wg_reduced = false;
+    for (int li = 255; li >= 0; --li) {
+      vec3<u32> wid(w, 0, 0), lid((u32)li % 16u, (u32)li / 16u, 0);
+      cg_finish(wid, lid, (u32)li);
+      vec3<u32> id = tile_cell(wid, lid);
+      if (in_grid(id)) {
+        u32 c = idx(id.x, id.y);
+        h_new[c] = h[c];
+        h[c] = h_old[c];
+      }
+    }
+    if (wg_reduced) cg_part[wg_slot] = tree_sum(wg_sum);
+    if (wg_flag) tile_moved[tile_list[w]] = 1u;
+  }
+  h.v = h_new;
+}
+
+// Film::encode_frame's implicit hydrostatic steps (src/film/mod.rs:1373-1408)
+void run_implicit() {
+  for (u32 s = 0; s < impl_steps; ++s) {
+    dispatch_tiles(laplacian);
+    dispatch_tiles(cg_setup);
+    dispatch_tiles(cg_lap_h);
+    dispatch_tiles_wg(cg_init);
+    dispatch_one(cg_reduce_init);
+    for (u32 it = 0; it < impl_iters; ++it) {
+      dispatch_tiles(cg_lap_p);
+      dispatch_tiles_wg(cg_iter_a);
+      dispatch_one(cg_reduce_a);
+      dispatch_tiles_wg(cg_iter_b);
+      dispatch_one(cg_reduce_b);
+      dispatch_tiles(cg_iter_c);
+    }
+    dispatch_tiles(cg_lap_u);
+    run_cg_finish();
+    run_cg_reduce_mass();
+    dispatch_tiles(cg_rescale);
+  }
+}
 
 void encode_frame(u32 substeps) {
   if (dep_pending) dispatch_full(deposit);  // the "pre" pass of Film::encode_frame
@@ -118,6 +239,7 @@ void encode_frame(u32 substeps) {
   run_compact_tiles();
   dispatch_full(cure_step);
   dispatch_tiles(clear_acc);
+  run_implicit();
   for (u32 s = 0; s < substeps; ++s) {
     dispatch_tiles(laplacian);
     dispatch_tiles(plug);
@@ -151,6 +273,8 @@ void wgr_create(uint32_t w, uint32_t h_) {
   sz(alpha_s, N); sz(strata_cure2, N); sz(tile_flags, TW * TH); sz(tile_list, TW * TH);
   sz(active_count, 4); sz(tile_moved, TW * TH); sz(lay, N);
   sz(stats_out, ((w + 63) / 64) * ((h_ + 63) / 64)); sz(h_frame, N); sz(fnorm, N);
+  sz(cg_m, N); sz(cg_d, N); sz(cg_x, N); sz(cg_r, N); sz(cg_p, N); sz(cg_q, N); sz(cg_t, N); sz(cg_t2, N);
+  sz(cg_part, TW * TH); sz(cg_part2, TW * TH); sz(cg_s, 2);
   color_out.w = w; color_out.v.assign(N, vec4<f32>(f32(0)));
   detail_out.w = w; detail_out.v.assign(N, vec4<f32>(f32(0)));
 }
@@ -171,6 +295,12 @@ void wgr_set_tables(const float* pt, const float* cm) {
 }
 
 void wgr_encode_frame(uint32_t substeps) { encode_frame(substeps); }
+
+// Film::implicit_steps (update_params) and FilmSettings::implicit_iters
+void wgr_set_implicit(uint32_t steps, uint32_t iters) {
+  impl_steps = steps;
+  impl_iters = iters;
+}
 
 // write_state scratch clearing (src/film/mod.rs:1307-1317)
 void wgr_after_write_state() {

@@ -15,8 +15,8 @@ Only the subset of WGSL that these shaders use is handled: structs, module
 constants and bindings, functions, let/var, if/else/for/while, vector and
 array constructors, swizzles, pointers to function variables, atomics and
 barriers (the driver emulates workgroup phases where a barrier matters).
-Top-level items that use `switch` (the implicit CG solve, which is not on the
-path) are dropped together with everything that references them.
+`switch` becomes an if / else-if chain.  Helpers whose workgroup barriers
+sit inside them are left to driver.cpp (DRIVER_PROVIDED).
 
 Usage: python translate.py <reference_root> <out_file> [real]
   real = double (default) or float: the C++ type that WGSL f32 maps to.
@@ -120,7 +120,36 @@ def conv_array_ctor(code):
     return re.sub(r"(?<![\w:<])array<([^()]*?)>\(", r"make_array<\1>(", code)
 
 
+def conv_switch(code):
+    """switch e { case a, b: {..} default: {..} } -> an if / else-if chain."""
+    while True:
+        m = re.search(r"\bswitch\s+(.+?)\s*\{", code)
+        if not m:
+            return code
+        end = match_bracket(code, m.end() - 1)
+        inner = code[m.end():end - 1]
+        arms, i = [], 0
+        while True:
+            c = re.compile(r"\s*(case\s+(.+?)|default)\s*:\s*\{", re.S).match(inner, i)
+            if not c:
+                assert not inner[i:].strip(), inner[i:][:60]
+                break
+            close = match_bracket(inner, c.end() - 1)
+            arms.append((None if c.group(1) == "default" else split_top(c.group(2)), inner[c.end():close - 1]))
+            i = close
+        parts = []
+        for k, (labels, body) in enumerate(arms):
+            if labels is None:
+                parts.append("{" + body + "}")
+            else:
+                cond = " || ".join("__sw == (%s)" % lab for lab in labels)
+                parts.append("if (%s) {%s}" % (cond, body))
+        chain = " else ".join(parts)
+        code = code[:m.start()] + "{ const auto __sw = (%s); %s }" % (m.group(1), chain) + code[end:]
+
+
 def conv_body(body):
+    body = conv_switch(body)
     out = []
     for line in body.split("\n"):
         s = line
@@ -184,6 +213,18 @@ JACOBI = {"nose": ["delta"], "strata_fill": ["strata_h", "strata_pig", "strata_c
 # barrier-separated phase (`<name>__p0`, `__p1`, ...).
 PHASED = ["mark_tiles"]
 
+# Helpers with workgroup barriers inside them: only their prototypes are
+# emitted; driver.cpp gives them workgroup-at-a-time definitions (the driver
+# runs a workgroup's invocations one after the other, then completes the
+# barrier's work: the tile's moved flag, the tree sums of wg_reduce and
+# total_parts in the shader's order).
+DRIVER_PROVIDED = {"begin_motion", "end_motion", "wg_reduce", "total_parts"}
+
+# Entry points not translated: cg_reduce_mass keeps its barriers inline
+# (driver.cpp restates its two tree sums); pool8 and the slump pass are not
+# on the path.
+DROPPED = {"cg_reduce_mass"}
+
 
 def match_bracket(s, i):
     """Index just past the bracket group that opens at s[i]."""
@@ -243,7 +284,7 @@ def translate(ref_root, real="double"):
             src += "\n" + f.read() + "\n"
     items = split_items(src)
     named = [(it,) + item_name(it) for it in items]
-    dropped = {nm for it, kind, nm in named if kind == "fn" and "switch" in it}
+    dropped = set(DROPPED)
     changed = True
     while changed:
         changed = False
@@ -272,6 +313,8 @@ def translate(ref_root, real="double"):
                 it = alias_reads(it, JACOBI[nm])
             proto, text = conv_fn(it, nm)
             protos.append(proto + ";")
+            if nm in DRIVER_PROVIDED:
+                continue
             fns.append(text)
             if nm in PHASED:
                 fns.extend(phase_split(proto, text))

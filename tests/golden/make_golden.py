@@ -92,6 +92,10 @@ def cases():
                            tau=(0.0, 1.0), mu=(0.05, 0.5))
     out.append(("deposit_fresh", cv, dict(frame_dt=1 / 60, frames=4, adaptive_substeps=True,
                                           deposits={0: deposit_set(cv, 100), 2: deposit_set(cv, 102)})))
+    cv = synth.blob_canvas(48, 48, 29, n_blobs=4, sigma=(4, 9), per_cell_n=False, tables="reference",
+                           tau=(0.0, 0.3), mu=(0.05, 0.2), peak_mm=(3.0, 5.0))
+    cv.settings.update(implicit_hydro=1)
+    out.append(("implicit_pour", cv, dict(frame_dt=1 / 60, frames=4, adaptive_substeps=True)))
     return out
 
 
@@ -147,7 +151,7 @@ def main():
         r = po.RefShaders(cv.w, cv.h)
         r.set_tables(cv.pigtab, cv.cmf)
         r.write_state(cv.planes)
-        schedule, params, dep_frames = [], [], {}
+        schedule, params, dep_frames, implicit = [], [], {}, []
         for f in range(sched["frames"]):
             fdt = sched["frame_dt"]
             if f in sched.get("deposits", {}):
@@ -162,6 +166,8 @@ def main():
             o.update_params(fdt, n)
             p = o.params()
             r.set_params(p)
+            r.set_implicit(o.implicit_steps(), st.implicit_iters)
+            implicit.append(o.implicit_steps())
             r.encode_frame(n)
             o.encode_frame(n)
             schedule.append((fdt, n))
@@ -172,9 +178,10 @@ def main():
         ins = {"in_" + k: np.asarray(v) for k, v in cv.planes.items()}
         np.savez_compressed(HERE / ("%s.npz" % name), w=cv.w, h=cv.h, settings=json.dumps(cv.settings),
                             pigtab=cv.pigtab, cmf=cv.cmf, schedule=np.array(schedule),
-                            params=np.stack(params), **ins, **outs, **dep_frames)
-        print("%-16s %dx%d frames %d substeps %s  oracle-vs-ref max |d| %.3e" % (
-            name, cv.w, cv.h, len(schedule), [s[1] for s in schedule], worst))
+                            params=np.stack(params), implicit_steps=np.array(implicit), **ins, **outs,
+                            **dep_frames)
+        print("%-16s %dx%d frames %d substeps %s implicit %s  oracle-vs-ref max |d| %.3e" % (
+            name, cv.w, cv.h, len(schedule), [s[1] for s in schedule], implicit, worst))
 
 
 if __name__ == "__main__":
