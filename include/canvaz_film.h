@@ -91,7 +91,7 @@ typedef struct cf_settings {
     uint32_t max_substeps;
     uint32_t min_substeps;
     uint32_t implicit_iters;
-    int32_t implicit_hydro;   /* implicit CG hydrostatic solve: only 0 is supported */
+    int32_t implicit_hydro;   /* implicit hydrostatic CG steps (film.wgsl:895-1302); fixed at cf_create */
     int32_t slump;            /* slump pass: only 0 is supported (reference default) */
     int32_t capillary;
     int32_t capillary_implicit;
@@ -202,16 +202,20 @@ cf_status cf_pack_params(const cf_settings* settings, uint32_t w, uint32_t h, fl
 cf_status cf_choose_substeps(cf_film* film, float frame_dt, uint32_t* substeps);
 
 /* Film::encode_frame (src/film/mod.rs:1322-1462), simulation portion: tile
- * activity, cure, `substeps` x {laplacian, plug, fluxes, limiter, apply, nose},
- * strata split/limit/update/copy/fill x 6, tile stats and the full KM shade.
- * Uses the params of the last cf_update_params. */
+ * activity, cure, the implicit hydrostatic steps that update_params chose
+ * (each a CG solve of implicit_iters iterations), `substeps` x {laplacian,
+ * plug, fluxes, limiter, apply, nose}, strata split/limit/update/copy/fill x 6,
+ * tile stats and the full KM shade.  Uses the params of the last
+ * cf_update_params. */
 cf_status cf_encode_frame(cf_film* film, uint32_t substeps, void* stream);
 
 /* One adaptive step: the substep dt is derived on the device from the
  * h_max / mu_min of the previous frame with the formulas of choose_substeps
- * (dt = min(dt_max, dt_cfl, dt_hyd, dt_cap)), the dt-dependent params are
- * re-derived on the device, and one frame with one substep is run.  No host
- * round trip; graph-capturable. */
+ * (dt = min(dt_max, dt_cfl, dt_hyd, dt_cap)), the dt-dependent params (and
+ * the implicit step count) are re-derived on the device, and one frame with
+ * one substep is run.  No host round trip; graph-capturable.  With
+ * implicit_hydro on, the launches cover 4 implicit steps and the film skips
+ * the ones it does not take. */
 cf_status cf_step_adaptive(cf_film* film, float dt_max, void* stream);
 
 /* Film::dry_now (src/film/mod.rs:1230-1244): one cure pass with rate
@@ -234,8 +238,8 @@ cf_status cf_get_stats(cf_film* film, cf_stats* out);
  * (Film::read_state / write_state, src/film/mod.rs:1281-1320): copies src's
  * whole device state (every plane with both strata generations, tables,
  * params, stats) into dst on `stream`, so dst steps exactly as src would.
- * dst and src have the same size, precision and device.  A serving loop
- * admits a job by cloning a resident template canvas. */
+ * dst and src have the same size, precision, device and implicit_hydro.  A
+ * serving loop admits a job by cloning a resident template canvas. */
 cf_status cf_clone_state(cf_film* dst, const cf_film* src, void* stream);
 
 /* Params of the last update (for parity checks of update_params). */
@@ -250,7 +254,8 @@ const char* cf_last_error(const cf_film* film);
 
 /* Device bytes a film of w x h cells in `precision` holds (its arena, params,
  * stats, tables and tile table): what an admission policy budgets.  Pure host
- * function. */
+ * function.  A film created with implicit_hydro holds 52 B per cell and 8 B
+ * per 16x16 tile more (the CG planes). */
 cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* bytes);
 
 /* --- deposits: paint laid on the film ------------------------------------------ */

@@ -107,6 +107,7 @@ static void fill_devparams(cf_film* f, DevParams& D, float dt_max) {
   D.s_implicit = f->S.implicit_hydro;
   D.dt_max = dt_max;
   D.implicit_steps = f->implicit_steps;
+  D.implicit_iters = f->S.implicit_iters;
   D.frames = f->frames;
   const cf_params& P = f->P;
   D.hold1 = P.front[0] * (1.0f - std::exp(-0.5f * P.front[1]));
@@ -168,7 +169,7 @@ cf_status cf_pack_params(const cf_settings* s, uint32_t w, uint32_t h, float fra
 // The device planes of a film (n cells, nt tiles) in arena order; add(p, bytes)
 // receives each plane's pointer slot and size.
 template <class Add>
-static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, Add add) {
+static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, bool cg, Add add) {
   const size_t pig_b = precision == CF_PREC_FP32 ? 4 : 2, rh_b = precision == CF_PREC_BF16 ? 2 : 4;
   add((void**)&F.hh, 4 * n); add((void**)&F.m, 4 * n); add(&F.mu, rh_b * n); add(&F.tau, rh_b * n);
   add(&F.nn, rh_b * n); add((void**)&F.delta, 4 * n); add((void**)&F.delta_old, 4 * n);
@@ -181,6 +182,12 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, Add a
   add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
   add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n); add((void**)&F.dry_shaded, n);
   add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
+  if (cg) {  // implicit hydrostatic step (settings.implicit_hydro)
+    add((void**)&F.cg_m, 16 * n);
+    for (float** p : {&F.cg_d, &F.cg_x, &F.cg_r, &F.cg_p, &F.cg_pa, &F.cg_pb, &F.cg_q, &F.cg_t, &F.cg_t2})
+      add((void**)p, 4 * n);
+    add((void**)&F.cg_part, 4 * nt); add((void**)&F.cg_part2, 4 * nt); add((void**)&F.cg, sizeof(cfk::CgState));
+  }
 }
 
 extern "C" {
@@ -191,7 +198,7 @@ cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* byt
   const size_t n = (size_t)w * h, nt = (size_t)((w + 15) / 16) * ((h + 15) / 16);
   cfk::Film F{};
   size_t total = 0;
-  carve_planes(F, n, nt, precision, [&](void**, size_t b) { total += (b + 255) & ~(size_t)255; });
+  carve_planes(F, n, nt, precision, false, [&](void**, size_t b) { total += (b + 255) & ~(size_t)255; });
   total += sizeof(DevParams) + sizeof(DevStats) + sizeof(float) * 528 + 2 * sizeof(cfk::Film) + sizeof(uint2) * nt;
   *bytes = total;
   return CF_OK;
@@ -225,7 +232,7 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
   struct Slot { void** p; size_t bytes; };
   std::vector<Slot> slots;
   cfk::Film& F = f->F;
-  carve_planes(F, n, nt, precision, [&](void** p, size_t b) { slots.push_back({p, b}); });
+  carve_planes(F, n, nt, precision, s->implicit_hydro != 0, [&](void** p, size_t b) { slots.push_back({p, b}); });
   size_t total = 0;
   for (auto& sl : slots) total += (sl.bytes + 255) & ~(size_t)255;
   cudaError_t e = cudaMalloc(&f->arena, total);
@@ -435,6 +442,8 @@ cf_status cf_clone_state(cf_film* dst, const cf_film* src, void* stream) {
   if (!dst || !src || dst == src) return fail(dst, CF_ERR_INVALID_ARG, "cf_clone_state: null or same film");
   if (dst->w != src->w || dst->h != src->h || dst->prec != src->prec || dst->device != src->device)
     return fail(dst, CF_ERR_INVALID_ARG, "cf_clone_state: size, precision or device differ");
+  if (dst->arena_bytes != src->arena_bytes)  // one has the implicit CG planes, the other not
+    return fail(dst, CF_ERR_INVALID_ARG, "cf_clone_state: implicit_hydro differs");
   cudaStream_t st = (cudaStream_t)stream;
   // identical (w, h, precision) give identical arena layouts: one copy moves
   // every plane, both strata generations included
@@ -537,14 +546,14 @@ cf_status cf_choose_substeps(cf_film* f, float frame_dt, uint32_t* out) {  // sr
 
 cf_status cf_encode_frame(cf_film* f, uint32_t substeps, void* stream) {
   if (!f || substeps == 0 || substeps > 4096) return fail(f, CF_ERR_INVALID_ARG, "cf_encode_frame");
-  if (f->S.implicit_hydro && f->implicit_steps > 0)
-    return fail(f, CF_ERR_UNSUPPORTED, "implicit hydrostatic CG solve is not implemented (set implicit_hydro = 0)");
   if (f->S.slump) return fail(f, CF_ERR_UNSUPPORTED, "slump pass is not implemented (reference default is off)");
   cudaStream_t st = (cudaStream_t)stream;
   cf_status s = upload_params(f, st);
   if (s != CF_OK) return s;
   f->launches += launch_pending_deposits(f, st);
-  f->launches += cfk::launch_frame_packed(solo_view(f), f->prec, substeps, 0, st);
+  cfk::PackedFrame V = solo_view(f);
+  V.implicit_steps = f->S.implicit_hydro ? f->implicit_steps : 0u;
+  f->launches += cfk::launch_frame_packed(V, f->prec, substeps, 0, st);
   swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
   f->frames++;
@@ -559,7 +568,11 @@ cf_status cf_step_adaptive(cf_film* f, float dt_max, void* stream) {
   cf_status s = upload_params(f, st, dt_max);
   if (s != CF_OK) return s;
   f->launches += launch_pending_deposits(f, st);
-  f->launches += cfk::launch_frame_packed(solo_view(f), f->prec, 1, 1, st);
+  cfk::PackedFrame V = solo_view(f);
+  // the device picks dt and with it the implicit step count (0..4): the
+  // launches cover 4 steps and the film's kernels skip the ones it does not take
+  V.implicit_steps = f->S.implicit_hydro ? 4u : 0u;
+  f->launches += cfk::launch_frame_packed(V, f->prec, 1, 1, st);
   swap_generations(f);
   if ((s = check_launch(f)) != CF_OK) return s;
   f->frames++;

@@ -112,14 +112,34 @@ cf_status build(cf_batch* b) {
   return CF_OK;
 }
 
+// Implicit hydrostatic steps to launch for a group: each film's own count
+// when the host knows it, else (dt chosen on the device, or a graph replayed
+// over frames whose counts differ) the most a frame takes, 4; the films'
+// kernels skip the steps beyond their own count.
+void implicit_view(const cf_batch::Group& g, bool fixed_count, cfk::PackedFrame& V) {
+  uint32_t steps = 0, iters = 0;
+  bool on = false, cap = false;
+  for (const cf_film* f : g.films) {
+    if (!f->S.implicit_hydro) continue;
+    on = true;
+    steps = std::max(steps, f->implicit_steps);
+    iters = std::max(iters, f->S.implicit_iters);
+    cap = cap || f->S.capillary_implicit;
+  }
+  V.implicit_steps = on ? (fixed_count ? steps : 4u) : 0u;
+  V.implicit_iters = iters;
+  V.cap_implicit = cap;
+}
+
 // Enqueues `frames` frames starting at parity p; no host bookkeeping.
-uint64_t enqueue(cf_batch* b, int p, uint32_t frames, uint32_t substeps, int adaptive, cudaStream_t st) {
+uint64_t enqueue(cf_batch* b, int p, uint32_t frames, uint32_t substeps, int adaptive, bool graph, cudaStream_t st) {
   uint64_t n = 0;
   const uint32_t blocks = (uint32_t)b->sms * std::max(b->tune.list_blocks_per_sm, 1u);
   for (uint32_t r = 0; r < frames; ++r) {
     for (auto& g : b->groups) {
       const uint32_t nf = (uint32_t)g.films.size();
       cfk::PackedFrame V;
+      implicit_view(g, !adaptive && !graph, V);
       V.films = g.d_films + (size_t)p * nf;
       V.films_next = g.d_films + (size_t)(1 - p) * nf;
       V.tiles = g.d_tiles;
@@ -147,7 +167,7 @@ cf_status capture(cf_batch* b, int p, uint32_t frames, uint32_t substeps, int ad
   if (!b->cap) BATCH_TRY(b, cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
   cudaGraph_t graph = nullptr;
   BATCH_TRY(b, cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
-  b->g_launches = enqueue(b, p, frames, substeps, adaptive, b->cap);
+  b->g_launches = enqueue(b, p, frames, substeps, adaptive, true, b->cap);
   cudaError_t e = cudaStreamEndCapture(b->cap, &graph);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -169,8 +189,6 @@ cf_status step(cf_batch* b, uint32_t frames, uint32_t substeps, float dt_max, cu
   if (b->films.empty() || frames == 0) return CF_OK;
   for (cf_film* f : b->films) {
     if (f->S.slump) return bfail(b, CF_ERR_UNSUPPORTED, "slump pass is not implemented");
-    if (!adaptive && f->S.implicit_hydro && f->implicit_steps > 0)
-      return bfail(b, CF_ERR_UNSUPPORTED, "implicit hydrostatic CG solve is not implemented (set implicit_hydro = 0)");
   }
   // a film stepped on its own since the build is in the other generation
   // than the batch's records say: rebuild them
@@ -212,7 +230,7 @@ cf_status step(cf_batch* b, uint32_t frames, uint32_t substeps, float dt_max, cu
   }
   if (done < frames) {
     const uint32_t rest = frames - done;
-    const uint64_t n = enqueue(b, b->parity, rest, substeps, adaptive, st);
+    const uint64_t n = enqueue(b, b->parity, rest, substeps, adaptive, false, st);
     BATCH_TRY(b, cudaGetLastError());
     advance(b, rest, n);
   }

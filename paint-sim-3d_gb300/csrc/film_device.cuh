@@ -36,12 +36,22 @@ struct DevParams {
   int32_t s_implicit;
   float dt_max;         // adaptive step upper bound
   uint32_t implicit_steps;
+  uint32_t implicit_iters;  // FilmSettings::implicit_iters
   uint32_t frames;
   // per-film constants of the front terms (settings only, never dt):
   float hold1;          // hold_level(1) (film.wgsl:153-156)
   float cox_theta;      // atan(tan theta) (film.wgsl:236-244)
   float cox_span;       // max(front.x - hold_level(1), 1e-6)
   float cox_adv;        // min(theta + front2.x, 3.1)
+};
+
+// Scalars of a film's implicit CG solve (film.wgsl cg_s[0], cg_s[1]) and the
+// count of blocks that have written their tile partial in the current launch.
+struct CgState {
+  float rz, pq, alpha, beta;  // cg_s[0]
+  float s1x, dv, tv, s0x;     // cg_s[1]: rz of the init, sum of h changes, sum of h, last rz
+  uint32_t blocks_done;
+  uint32_t pad[7];
 };
 
 // Global reductions written by the stats kernels.
@@ -118,6 +128,13 @@ struct Film {
   uint8_t* dry_shaded;  // 1: color holds the colour of a dry cell for the current sub_refl, m and cmf
   uint32_t* full_list;  // cells of the strata full path (DevStats::full_count)
   uint32_t* fill_list;  // strata fill candidates (DevStats::fill_count)
+  // implicit CG planes (null when the film's settings turn the implicit
+  // hydrostatic step off): face mobilities, diagonal, solution, residual,
+  // direction (cg_p as the last step left it; cg_pa / cg_pb alternate during
+  // a solve), A p (then the new h), weighted Laplacians, tile partials
+  float4* cg_m;
+  float *cg_d, *cg_x, *cg_r, *cg_p, *cg_pa, *cg_pb, *cg_q, *cg_t, *cg_t2, *cg_part, *cg_part2;
+  CgState* cg;
   uint32_t persist_blocks;  // grid of the list kernels: a few blocks per SM
   uint32_t all_active;      // keep every tile active (settings.all_active)
   const float* pigtab;  // 12 x 40

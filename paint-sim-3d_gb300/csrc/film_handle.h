@@ -59,6 +59,8 @@ inline cfk::PackedFrame solo_view(const cf_film* f) {
   V.ntiles = f->tw * f->th;
   V.nfilms = 1;
   V.persist_blocks = f->F.persist_blocks;
+  V.implicit_iters = f->S.implicit_iters;
+  V.cap_implicit = f->S.implicit_hydro && f->S.capillary_implicit;
   return V;
 }
 inline void swap_generations(cf_film* f) {

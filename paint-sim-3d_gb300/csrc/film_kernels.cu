@@ -1330,9 +1330,17 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
   kp_compact_tiles<<<(nt + 255u) / 256u, 256, 0, st>>>(A, T, nt);
   kp_cure<MODE><<<nt, b, 0, st>>>(A, T, nt);
   n += 4;
-  if (substeps == 0) { kp_clear_acc<<<nt, b, 0, st>>>(A, T, nt); ++n; }
-  for (uint32_t s = 0; s < substeps; ++s) {
+  // clear_acc runs with the first laplacian of the frame: the first implicit
+  // step's (src/film/mod.rs:1371-1376) or the first substep's
+  const uint32_t isteps = V.implicit_steps;
+  if (substeps == 0 && isteps == 0) { kp_clear_acc<<<nt, b, 0, st>>>(A, T, nt); ++n; }
+  for (uint32_t s = 0; s < isteps; ++s) {
     if (s == 0) kp_laplacian<true><<<nt, b, 0, st>>>(A, T, nt);
+    else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+    n += 1 + launch_cg_step(V, MODE, s, V.implicit_iters, V.cap_implicit, st);
+  }
+  for (uint32_t s = 0; s < substeps; ++s) {
+    if (s == 0 && isteps == 0) kp_laplacian<true><<<nt, b, 0, st>>>(A, T, nt);
     else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
     kp_plug<MODE><<<nt, b, 0, st>>>(A, T, nt);
     kp_fluxes<MODE><<<nt, b, 0, st>>>(A, T, nt);

@@ -19,7 +19,17 @@ struct PackedFrame {
   uint32_t ntiles;
   uint32_t nfilms;
   uint32_t persist_blocks; // grid of the strata list kernels
+  // implicit hydrostatic steps launched (each film's kernels skip the steps
+  // beyond its own count), CG iterations per step (each film stops at its
+  // own), and whether any film has the implicit capillary term
+  uint32_t implicit_steps = 0;
+  uint32_t implicit_iters = 40;
+  bool cap_implicit = false;
 };
+
+// The kernels of implicit step `step` (cg.cu); returns the launch count.
+uint32_t launch_cg_step(const PackedFrame& V, int mode, uint32_t step, uint32_t iters, bool cap_implicit,
+                        cudaStream_t st);
 
 // One frame of Film::encode_frame for every film of V with `substeps`
 // substeps (adaptive: each film's dt chosen on the device first, one
