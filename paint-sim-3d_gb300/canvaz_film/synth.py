@@ -222,9 +222,20 @@ def drip_canvas(w, h, seed, n_lines=200, segs=(2, 6), width_cells=(2, 8), height
     return Canvas(w, h, planes, pigtab, cmf, settings, "drips%d_s%d" % (n_lines, seed))
 
 
+def pour_canvas(w, h, seed, n_blobs=300):
+    """Thick, runny pours (3-5 mm, mu 0.05-0.2 Pa s, tau_y <= 0.3 Pa) with the
+    reference's implicit hydrostatic step on, as its defaults have it: the
+    frames take 1-4 implicit CG steps."""
+    cv = blob_canvas(w, h, seed, n_blobs=n_blobs, sigma=(8.0, 40.0), per_cell_n=False, tables="reference",
+                     tau=(0.0, 0.3), mu=(0.05, 0.2), peak_mm=(3.0, 5.0))
+    cv.settings.update(implicit_hydro=1)
+    return cv
+
+
 def config(k, seed=0, scale=1):
     """The workloads: 0 = 512^2 blobs (K, S over 8 bands), 1 = 2048^2 tilted
-    drips, 2 = 4096^2 blobs over a cured ground.  `scale` divides the side."""
+    drips, 2 = 4096^2 blobs over a cured ground, 5 = 2048^2 thick pours with
+    the implicit hydrostatic step.  `scale` divides the side."""
     if k == 0:
         s = 512 // scale
         return blob_canvas(s, s, seed, n_blobs=20, nband=8)
@@ -234,4 +245,7 @@ def config(k, seed=0, scale=1):
     if k == 2:
         s = 4096 // scale
         return blob_canvas(s, s, seed, n_blobs=max(500 // (scale * scale), 8), ground=5e-5, raw=False)
+    if k == 5:
+        s = 2048 // scale
+        return pour_canvas(s, s, seed, n_blobs=max(300 // (scale * scale), 4))
     raise ValueError(k)

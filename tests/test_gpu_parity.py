@@ -182,8 +182,10 @@ def replay_cuda(d, precision=capi.CF_PREC_REFERENCE):
 # Perturbing the input heights by 1e-7 (relative) moves the oracle's FP32
 # mirror of the reference arithmetic between 2e-7 and 4e-6 from FP64 on this
 # fixture, and the CUDA path between 1.5e-7 and 2.3e-5; deposit_fresh (strokes
-# on bare canvas) holds the usual 1e-5.
-H_REL_BRANCHY = {"deposit_strokes": 5e-5}
+# on bare canvas) holds the usual 1e-5.  implicit_pour runs 8 CG solves of 40
+# iterations in f32: the FP32 mirror lands 2.4e-5 to 4.8e-5 from FP64 under
+# the same perturbations, the CUDA path 2.4e-5.
+H_REL_BRANCHY = {"deposit_strokes": 5e-5, "implicit_pour": 1e-4}
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[p.stem for p in GOLDEN])
