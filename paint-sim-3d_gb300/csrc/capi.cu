@@ -376,32 +376,59 @@ static cf_status copy_plane(cf_film* f, void* dst, const void* src, size_t bytes
   return CF_OK;
 }
 
+// The address a kernel reads a host buffer at, when the buffer is page-locked
+// CUDA host memory (else null: the buffer is staged through a copy).
+static const void* kernel_readable_host(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: null");
   if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: pig_format");
   cfk::Film& F = f->F;
   size_t n = f->n;
   CUDA_TRY(f, cudaDeviceSynchronize());
+  // Everything is enqueued on the legacy stream and waited for once at the
+  // end.  Planes from device or page-locked host memory are copied
+  // asynchronously; the pigment and rheology planes, which change layout, are
+  // converted by kernels that read such sources in place (no staging).
+  const cudaMemcpyKind h2d = v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  auto put = [&](void* dst, const void* src, size_t bytes) -> cf_status {
+    if (!src) return CF_OK;
+    const bool async_ok = v->device || kernel_readable_host(src) != nullptr;
+    if (async_ok) CUDA_TRY(f, cudaMemcpyAsync(dst, src, bytes, h2d, 0));
+    else CUDA_TRY(f, cudaMemcpy(dst, src, bytes, h2d));
+    return CF_OK;
+  };
   cf_status st;
-  if (v->h && (st = copy_plane(f, F.hh, v->h, 4 * n, v->device, true)) != CF_OK) return st;
-  if (v->m && (st = copy_plane(f, F.m, v->m, 4 * n, v->device, true)) != CF_OK) return st;
-  if (v->strata_h && (st = copy_plane(f, F.sh, v->strata_h, 16 * n, v->device, true)) != CF_OK) return st;
-  if (v->strata_cure && (st = copy_plane(f, F.scu, v->strata_cure, 16 * n, v->device, true)) != CF_OK) return st;
-  if (v->sub_refl && (st = copy_plane(f, F.refl, v->sub_refl, 32 * n, v->device, true)) != CF_OK) return st;
-  if (v->lay && (st = copy_plane(f, F.lay, v->lay, 4 * n, v->device, true)) != CF_OK) return st;
-  size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2;
-  if (v->rheo || v->strata_pig) {
+  if ((st = put(F.hh, v->h, 4 * n)) != CF_OK) return st;
+  if ((st = put(F.m, v->m, 4 * n)) != CF_OK) return st;
+  if ((st = put(F.sh, v->strata_h, 16 * n)) != CF_OK) return st;
+  if ((st = put(F.scu, v->strata_cure, 16 * n)) != CF_OK) return st;
+  if ((st = put(F.refl, v->sub_refl, 32 * n)) != CF_OK) return st;
+  if ((st = put(F.lay, v->lay, 4 * n)) != CF_OK) return st;
+  const size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2;
+  const void* pig_src = v->strata_pig ? (v->device ? v->strata_pig : kernel_readable_host(v->strata_pig)) : nullptr;
+  const void* rheo_src = v->rheo ? (v->device ? v->rheo : kernel_readable_host(v->rheo)) : nullptr;
+  if (pig_src) cfk::launch_pig_import(F, f->prec, F.pig, pig_src, v->pig_format, 0);
+  if (rheo_src) cfk::launch_rheo_import(F, f->prec, (const float2*)rheo_src, f->S.n_index, n, 0);
+  if ((v->strata_pig && !pig_src) || (v->rheo && !rheo_src)) {  // pageable host memory: stage it
     void* tmp = nullptr;
-    size_t need = std::max(v->strata_pig ? 64 * esz * n : 0, v->rheo ? 8 * n : 0);
+    size_t need = std::max(v->strata_pig && !pig_src ? 64 * esz * n : 0, v->rheo && !rheo_src ? 8 * n : 0);
     CUDA_TRY(f, cudaMalloc(&tmp, need));
-    if (v->strata_pig) {
-      cudaError_t e = cudaMemcpy(tmp, v->strata_pig, 64 * esz * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+    if (v->strata_pig && !pig_src) {
+      cudaError_t e = cudaMemcpy(tmp, v->strata_pig, 64 * esz * n, cudaMemcpyHostToDevice);
       if (e == cudaSuccess) cfk::launch_pig_import(F, f->prec, F.pig, tmp, v->pig_format, 0);
       if (e == cudaSuccess) e = cudaDeviceSynchronize();
       if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
     }
-    if (v->rheo) {
-      cudaError_t e = cudaMemcpy(tmp, v->rheo, 8 * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+    if (v->rheo && !rheo_src) {
+      cudaError_t e = cudaMemcpy(tmp, v->rheo, 8 * n, cudaMemcpyHostToDevice);
       if (e == cudaSuccess) cfk::launch_rheo_import(F, f->prec, (const float2*)tmp, f->S.n_index, n, 0);
       if (e == cudaSuccess) e = cudaDeviceSynchronize();
       if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
@@ -410,16 +437,16 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   }
   // write_state :1307-1317 — clear scratch, mark every tile moved
   size_t pig_b = f->prec == CF_PREC_FP32 ? 4 : 2;
-  CUDA_TRY(f, cudaMemset(F.pres, 0, 8 * n));
-  CUDA_TRY(f, cudaMemset(F.flux, 0, 16 * n));
-  CUDA_TRY(f, cudaMemset(F.acc, 0, 16 * n));
-  CUDA_TRY(f, cudaMemset(F.alpha, 0, 4 * n));
-  CUDA_TRY(f, cudaMemset(F.delta, 0, 4 * n));
-  CUDA_TRY(f, cudaMemset(F.tmp, 0, 4 * n));
-  CUDA_TRY(f, cudaMemset(F.acc_s, 0, 64 * n));
-  CUDA_TRY(f, cudaMemset(F.sh2, 0, 16 * n));
-  CUDA_TRY(f, cudaMemset(F.pig2, 0, 64 * pig_b * n));
-  CUDA_TRY(f, cudaMemset(F.alpha_s, 0, 16 * n));
+  CUDA_TRY(f, cudaMemsetAsync(F.pres, 0, 8 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.flux, 0, 16 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.acc, 0, 16 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.alpha, 0, 4 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.delta, 0, 4 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.tmp, 0, 4 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.acc_s, 0, 64 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.sh2, 0, 16 * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.pig2, 0, 64 * pig_b * n, 0));
+  CUDA_TRY(f, cudaMemsetAsync(F.alpha_s, 0, 16 * n, 0));
   cfk::launch_fill_u32(F.tile_moved, 1u, (size_t)f->tw * f->th, 0);
   // aggregates of the uploaded strata for the first cure, and its colour
   cfk::launch_compose(solo_view(f), f->prec, 1, 0);

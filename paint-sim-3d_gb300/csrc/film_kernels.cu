@@ -1134,31 +1134,37 @@ __device__ __forceinline__ void adaptive_params_film(DevParams* Dp, DevStats* S)
 }
 
 // ---- state I/O: reference pigment layout [cell][stratum][slot] <-> chunks ----
-// one thread per (cell, stratum, chunk)
+// A block transposes 32 cells through shared memory: it reads their 64 slots
+// as one contiguous run (the source may be pinned host memory read over the
+// link), then writes each chunk plane's 32 cells as one contiguous run.
 template <int MODE>
-__global__ void k_pig_import(Film F, uint4* dst, const void* src, int fmt) {
-  constexpr int QN = PigIO<MODE>::QN, PER = 16 / QN;  // slots per chunk
-  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= (size_t)F.n * 4 * QN) return;
-  uint32_t c = (uint32_t)(t / (4 * QN));
-  int k = (int)((t / QN) % 4), q = (int)(t % QN);
-  float v[16] = {};
-  for (int e = 0; e < PER; ++e) {
-    size_t s = (size_t)c * 64 + 16 * k + q * PER + e;
+__global__ void __launch_bounds__(256) k_pig_import_t(Film F, uint4* dst, const void* src, int fmt) {
+  constexpr int QN = PigIO<MODE>::QN, PER = 16 / QN, CB = 32;
+  __shared__ float sv[CB][65];
+  const size_t c0 = (size_t)blockIdx.x * CB;
+  const int ncell = (int)min((size_t)CB, (size_t)F.n - c0);
+  for (int e = threadIdx.x; e < ncell * 64; e += blockDim.x) {
+    const size_t s = c0 * 64 + (size_t)e;
     float x;
     if (fmt == CF_PIG_F32) x = ((const float*)src)[s];
     else if (fmt == CF_PIG_F16) x = h16_to_f(((const uint16_t*)src)[s]);
     else x = b16_to_f(((const uint16_t*)src)[s]);
-    v[q * PER + e] = x;
+    sv[e / 64][e % 64] = x;
   }
-  // pack this chunk only
-  uint32_t wv[4];
-  for (int e = 0; e < 4; ++e) {
-    if (MODE == CF_PREC_FP32) wv[e] = __float_as_uint(v[q * PER + e]);
-    else if (MODE == CF_PREC_REFERENCE) wv[e] = f_to_h16(v[q * PER + 2 * e]) | (f_to_h16(v[q * PER + 2 * e + 1]) << 16);
-    else wv[e] = f_to_b16(v[q * PER + 2 * e]) | (f_to_b16(v[q * PER + 2 * e + 1]) << 16);
+  __syncthreads();
+  for (int e = threadIdx.x; e < 4 * QN * CB; e += blockDim.x) {
+    const int cl = e % CB, plane = e / CB;
+    if (cl >= ncell) continue;
+    const int k = plane / QN, q = plane % QN;
+    const float* v = &sv[cl][16 * k + q * PER];
+    uint32_t wv[4];
+    for (int w = 0; w < 4; ++w) {
+      if (MODE == CF_PREC_FP32) wv[w] = __float_as_uint(v[w]);
+      else if (MODE == CF_PREC_REFERENCE) wv[w] = f_to_h16(v[2 * w]) | (f_to_h16(v[2 * w + 1]) << 16);
+      else wv[w] = f_to_b16(v[2 * w]) | (f_to_b16(v[2 * w + 1]) << 16);
+    }
+    dst[PigIO<MODE>::at(F, (uint32_t)(c0 + cl), k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
   }
-  dst[PigIO<MODE>::at(F, c, k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
 }
 template <int MODE>
 __global__ void k_pig_export(Film F, const uint4* srcp, void* dst, int fmt) {
@@ -1387,11 +1393,10 @@ void launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st) {
 }
 
 void launch_pig_import(const Film& F, int mode, uint4* dst, const void* src, int fmt, cudaStream_t st) {
-  size_t qn = mode == CF_PREC_FP32 ? 4 : 2;
-  unsigned g = (unsigned)(((size_t)F.n * 4 * qn + 255) / 256);
-  if (mode == CF_PREC_REFERENCE) k_pig_import<CF_PREC_REFERENCE><<<g, 256, 0, st>>>(F, dst, src, fmt);
-  else if (mode == CF_PREC_FP32) k_pig_import<CF_PREC_FP32><<<g, 256, 0, st>>>(F, dst, src, fmt);
-  else k_pig_import<CF_PREC_BF16><<<g, 256, 0, st>>>(F, dst, src, fmt);
+  const unsigned g = (unsigned)(((size_t)F.n + 31) / 32);
+  if (mode == CF_PREC_REFERENCE) k_pig_import_t<CF_PREC_REFERENCE><<<g, 256, 0, st>>>(F, dst, src, fmt);
+  else if (mode == CF_PREC_FP32) k_pig_import_t<CF_PREC_FP32><<<g, 256, 0, st>>>(F, dst, src, fmt);
+  else k_pig_import_t<CF_PREC_BF16><<<g, 256, 0, st>>>(F, dst, src, fmt);
 }
 void launch_pig_export(const Film& F, int mode, const uint4* srcp, void* dst, int fmt, cudaStream_t st) {
   size_t qn = mode == CF_PREC_FP32 ? 4 : 2;
