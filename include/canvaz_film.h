@@ -231,6 +231,17 @@ cf_status cf_color_device_ptr(cf_film* film, void** ptr);
 /* Copies the colour plane (4 x IEEE half per cell) to host memory. Synchronous. */
 cf_status cf_read_color(cf_film* film, uint16_t* rgba16f_host);
 
+/* Asynchronous forms for pipelines that keep the host link busy while
+ * another film computes.  Every plane of the view must be device memory or
+ * page-locked host memory (CF_ERR_INVALID_ARG otherwise); the work is
+ * enqueued on `stream` and the caller waits on it.  After
+ * cf_write_state_async the host's copy of the tile stats is refreshed by the
+ * next cf_update_params, cf_choose_substeps, cf_get_stats or cf_sync.
+ * cf_read_color_async takes a device or page-locked destination. */
+cf_status cf_write_state_async(cf_film* film, const cf_state_view* view, void* stream);
+cf_status cf_read_state_async(cf_film* film, const cf_state_view* view, void* stream);
+cf_status cf_read_color_async(cf_film* film, uint16_t* rgba16f, void* stream);
+
 /* Statistics of the last frame; synchronous. */
 cf_status cf_get_stats(cf_film* film, cf_stats* out);
 

@@ -168,6 +168,9 @@ def load_library(path=None):
         "cf_dry_now": ([vp, vp], i32),
         "cf_color_device_ptr": ([vp, C.POINTER(vp)], i32),
         "cf_read_color": ([vp, C.POINTER(C.c_uint16)], i32),
+        "cf_write_state_async": ([vp, C.POINTER(StateView), vp], i32),
+        "cf_read_state_async": ([vp, C.POINTER(StateView), vp], i32),
+        "cf_read_color_async": ([vp, C.POINTER(C.c_uint16), vp], i32),
         "cf_get_stats": ([vp, C.POINTER(Stats)], i32),
         "cf_get_params": ([vp, C.POINTER(Params)], i32),
         "cf_sync": ([vp], i32),

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -387,72 +388,95 @@ static const void* kernel_readable_host(const void* p) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
-  if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: null");
-  if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: pig_format");
+// Where a kernel or an asynchronous copy can take a state plane from: device
+// memory as it is, page-locked host memory at its device-side address; null
+// for pageable host memory.
+static const void* async_src(const cf_state_view* v, const void* p) {
+  if (!p) return nullptr;
+  return v->device ? p : kernel_readable_host(p);
+}
+
+// Everything of write_state after the planes are in place (src/film/mod.rs:
+// 1307-1317): scratch cleared, every tile marked moved, the aggregates and
+// colour of the uploaded strata, the tile stats.  Enqueued on `st`.
+static cf_status write_state_tail(cf_film* f, cudaStream_t st) {
   cfk::Film& F = f->F;
-  size_t n = f->n;
-  CUDA_TRY(f, cudaDeviceSynchronize());
-  // Everything is enqueued on the legacy stream and waited for once at the
-  // end.  Planes from device or page-locked host memory are copied
-  // asynchronously; the pigment and rheology planes, which change layout, are
-  // converted by kernels that read such sources in place (no staging).
-  const cudaMemcpyKind h2d = v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  auto put = [&](void* dst, const void* src, size_t bytes) -> cf_status {
-    if (!src) return CF_OK;
-    const bool async_ok = v->device || kernel_readable_host(src) != nullptr;
-    if (async_ok) CUDA_TRY(f, cudaMemcpyAsync(dst, src, bytes, h2d, 0));
-    else CUDA_TRY(f, cudaMemcpy(dst, src, bytes, h2d));
-    return CF_OK;
-  };
-  cf_status st;
-  if ((st = put(F.hh, v->h, 4 * n)) != CF_OK) return st;
-  if ((st = put(F.m, v->m, 4 * n)) != CF_OK) return st;
-  if ((st = put(F.sh, v->strata_h, 16 * n)) != CF_OK) return st;
-  if ((st = put(F.scu, v->strata_cure, 16 * n)) != CF_OK) return st;
-  if ((st = put(F.refl, v->sub_refl, 32 * n)) != CF_OK) return st;
-  if ((st = put(F.lay, v->lay, 4 * n)) != CF_OK) return st;
-  const size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2;
-  const void* pig_src = v->strata_pig ? (v->device ? v->strata_pig : kernel_readable_host(v->strata_pig)) : nullptr;
-  const void* rheo_src = v->rheo ? (v->device ? v->rheo : kernel_readable_host(v->rheo)) : nullptr;
-  if (pig_src) cfk::launch_pig_import(F, f->prec, F.pig, pig_src, v->pig_format, 0);
-  if (rheo_src) cfk::launch_rheo_import(F, f->prec, (const float2*)rheo_src, f->S.n_index, n, 0);
-  if ((v->strata_pig && !pig_src) || (v->rheo && !rheo_src)) {  // pageable host memory: stage it
-    void* tmp = nullptr;
-    size_t need = std::max(v->strata_pig && !pig_src ? 64 * esz * n : 0, v->rheo && !rheo_src ? 8 * n : 0);
-    CUDA_TRY(f, cudaMalloc(&tmp, need));
-    if (v->strata_pig && !pig_src) {
-      cudaError_t e = cudaMemcpy(tmp, v->strata_pig, 64 * esz * n, cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) cfk::launch_pig_import(F, f->prec, F.pig, tmp, v->pig_format, 0);
-      if (e == cudaSuccess) e = cudaDeviceSynchronize();
-      if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
-    }
-    if (v->rheo && !rheo_src) {
-      cudaError_t e = cudaMemcpy(tmp, v->rheo, 8 * n, cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) cfk::launch_rheo_import(F, f->prec, (const float2*)tmp, f->S.n_index, n, 0);
-      if (e == cudaSuccess) e = cudaDeviceSynchronize();
-      if (e != cudaSuccess) { cudaFree(tmp); f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
-    }
-    cudaFree(tmp);
-  }
-  // write_state :1307-1317 — clear scratch, mark every tile moved
-  size_t pig_b = f->prec == CF_PREC_FP32 ? 4 : 2;
-  CUDA_TRY(f, cudaMemsetAsync(F.pres, 0, 8 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.flux, 0, 16 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.acc, 0, 16 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.alpha, 0, 4 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.delta, 0, 4 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.tmp, 0, 4 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.acc_s, 0, 64 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.sh2, 0, 16 * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.pig2, 0, 64 * pig_b * n, 0));
-  CUDA_TRY(f, cudaMemsetAsync(F.alpha_s, 0, 16 * n, 0));
-  cfk::launch_fill_u32(F.tile_moved, 1u, (size_t)f->tw * f->th, 0);
-  // aggregates of the uploaded strata for the first cure, and its colour
-  cfk::launch_compose(solo_view(f), f->prec, 1, 0);
-  // current stats so that the first adaptive step sees this state
-  cfk::launch_reduce(solo_view(f), f->prec, 0);
+  const size_t n = f->n, pig_b = f->prec == CF_PREC_FP32 ? 4 : 2;
+  CUDA_TRY(f, cudaMemsetAsync(F.pres, 0, 8 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.flux, 0, 16 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.acc, 0, 16 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.alpha, 0, 4 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.delta, 0, 4 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.tmp, 0, 4 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.acc_s, 0, 64 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.sh2, 0, 16 * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.pig2, 0, 64 * pig_b * n, st));
+  CUDA_TRY(f, cudaMemsetAsync(F.alpha_s, 0, 16 * n, st));
+  cfk::launch_fill_u32(F.tile_moved, 1u, (size_t)f->tw * f->th, st);
+  cfk::launch_compose(solo_view(f), f->prec, 1, st);
+  cfk::launch_reduce(solo_view(f), f->prec, st);
   CUDA_TRY(f, cudaGetLastError());
+  return CF_OK;
+}
+
+// The planes of a view whose sources are device or page-locked host memory,
+// enqueued on `st`.  Host planes move by the copy engines, so the SMs stay
+// free for work on other streams: plain planes straight into place, the
+// pigment and rheology planes (which change layout) into scratch planes that
+// write_state clears anyway (pig2, acc_s), from which kernels convert them.
+// A pigment source wider than the film's storage is converted by a kernel
+// reading it in place.
+// Uploads from host memory queue on the host link in call order, whatever
+// stream they are on: each waits for the previous one's copies (not for its
+// conversion kernels), so with several films in flight the link stays busy
+// while the others compute, instead of the uploads sharing it and finishing
+// together.
+static std::mutex g_link_mu;
+static cudaEvent_t g_link_ev[64] = {};  // per device: the last upload's copies
+
+static cf_status write_planes_async(cf_film* f, const cf_state_view* v, cudaStream_t st) {
+  cfk::Film& F = f->F;
+  const size_t n = f->n;
+  const cudaMemcpyKind k = v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  std::unique_lock<std::mutex> link(g_link_mu, std::defer_lock);
+  cudaEvent_t* link_ev = nullptr;
+  if (!v->device && f->device >= 0 && f->device < 64) {
+    link.lock();
+    link_ev = &g_link_ev[f->device];
+    if (*link_ev) CUDA_TRY(f, cudaStreamWaitEvent(st, *link_ev, 0));
+    else CUDA_TRY(f, cudaEventCreateWithFlags(link_ev, cudaEventDisableTiming));
+  }
+  const struct { void* dst; const void* src; size_t bytes; } plain[] = {
+      {F.hh, v->h, 4 * n}, {F.m, v->m, 4 * n}, {F.sh, v->strata_h, 16 * n}, {F.scu, v->strata_cure, 16 * n},
+      {F.refl, v->sub_refl, 32 * n}, {F.lay, v->lay, 4 * n}};
+  for (const auto& p : plain)
+    if (p.src) CUDA_TRY(f, cudaMemcpyAsync(p.dst, p.src, p.bytes, k, st));
+  const size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2, pig_b = f->prec == CF_PREC_FP32 ? 4 : 2;
+  const bool pig_staged = v->strata_pig && !v->device && esz <= pig_b;
+  if (pig_staged) CUDA_TRY(f, cudaMemcpyAsync(F.pig2, v->strata_pig, 64 * esz * n, cudaMemcpyHostToDevice, st));
+  if (v->rheo && !v->device) CUDA_TRY(f, cudaMemcpyAsync(F.acc_s, v->rheo, 8 * n, cudaMemcpyHostToDevice, st));
+  if (link_ev) {
+    CUDA_TRY(f, cudaEventRecord(*link_ev, st));
+    link.unlock();
+  }
+  if (v->strata_pig)
+    cfk::launch_pig_import(F, f->prec, F.pig, pig_staged ? (const void*)F.pig2 : async_src(v, v->strata_pig),
+                           v->pig_format, st);
+  if (v->rheo)
+    cfk::launch_rheo_import(F, f->prec, (const float2*)(v->device ? v->rheo : (const void*)F.acc_s), f->S.n_index,
+                            n, st);
+  return CF_OK;
+}
+
+static bool all_async(const cf_state_view* v) {
+  for (const void* p : {v->h, v->m, v->rheo, v->strata_h, v->strata_pig, v->strata_cure, v->sub_refl, v->lay})
+    if (p && !async_src(v, p)) return false;
+  return true;
+}
+
+// Host-side copy of the tile stats after a write (the first adaptive step and
+// update_params read them).
+static cf_status refresh_host_stats(cf_film* f) {
   DevStats ds;
   CUDA_TRY(f, cudaMemcpy(&ds, f->d_stats, sizeof(ds), cudaMemcpyDeviceToHost));
   float hm, mm;
@@ -461,7 +485,60 @@ cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
   f->h_max_stat = hm;
   f->mu_min_stat = mm > 1e8f ? 1.0f : mm;
   if (f->dep_pending == 0u) f->h_max_pending = 0.f;  // stats now include the deposits (poll_stats)
+  return CF_OK;
+}
+
+cf_status cf_write_state(cf_film* f, const cf_state_view* v) {
+  if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: null");
+  if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state: pig_format");
+  cfk::Film& F = f->F;
+  size_t n = f->n;
   CUDA_TRY(f, cudaDeviceSynchronize());
+  cf_status st;
+  if (all_async(v)) {  // everything enqueued, one wait
+    if ((st = write_planes_async(f, v, 0)) != CF_OK) return st;
+  } else {  // pageable host memory: plain copies, pigments and rheology staged
+    if (v->h && (st = copy_plane(f, F.hh, v->h, 4 * n, v->device, true)) != CF_OK) return st;
+    if (v->m && (st = copy_plane(f, F.m, v->m, 4 * n, v->device, true)) != CF_OK) return st;
+    if (v->strata_h && (st = copy_plane(f, F.sh, v->strata_h, 16 * n, v->device, true)) != CF_OK) return st;
+    if (v->strata_cure && (st = copy_plane(f, F.scu, v->strata_cure, 16 * n, v->device, true)) != CF_OK) return st;
+    if (v->sub_refl && (st = copy_plane(f, F.refl, v->sub_refl, 32 * n, v->device, true)) != CF_OK) return st;
+    if (v->lay && (st = copy_plane(f, F.lay, v->lay, 4 * n, v->device, true)) != CF_OK) return st;
+    const size_t esz = v->pig_format == CF_PIG_F32 ? 4 : 2;
+    if (v->rheo || v->strata_pig) {
+      void* tmp = nullptr;
+      size_t need = std::max(v->strata_pig ? 64 * esz * n : 0, v->rheo ? 8 * n : 0);
+      CUDA_TRY(f, cudaMalloc(&tmp, need));
+      cudaError_t e = cudaSuccess;
+      if (v->strata_pig) {
+        e = cudaMemcpy(tmp, v->strata_pig, 64 * esz * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) cfk::launch_pig_import(F, f->prec, F.pig, tmp, v->pig_format, 0);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      }
+      if (e == cudaSuccess && v->rheo) {
+        e = cudaMemcpy(tmp, v->rheo, 8 * n, v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) cfk::launch_rheo_import(F, f->prec, (const float2*)tmp, f->S.n_index, n, 0);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      }
+      cudaFree(tmp);
+      if (e != cudaSuccess) { f->err = cudaGetErrorString(e); return CF_ERR_CUDA; }
+    }
+  }
+  if ((st = write_state_tail(f, 0)) != CF_OK) return st;
+  if ((st = refresh_host_stats(f)) != CF_OK) return st;
+  CUDA_TRY(f, cudaDeviceSynchronize());
+  return CF_OK;
+}
+
+cf_status cf_write_state_async(cf_film* f, const cf_state_view* v, void* stream) {
+  if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state_async: null");
+  if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state_async: pig_format");
+  if (!all_async(v)) return fail(f, CF_ERR_INVALID_ARG, "cf_write_state_async: a plane is in pageable host memory");
+  cudaStream_t st = (cudaStream_t)stream;
+  cf_status s;
+  if ((s = write_planes_async(f, v, st)) != CF_OK) return s;
+  if ((s = write_state_tail(f, st)) != CF_OK) return s;
+  f->stats_stale = true;  // the host copy of the tile stats refreshes at the next stats read
   return CF_OK;
 }
 
@@ -493,6 +570,22 @@ cf_status cf_clone_state(cf_film* dst, const cf_film* src, void* stream) {
   return CF_OK;
 }
 
+// The planes of a view into device or page-locked host memory, enqueued on `st`.
+static cf_status read_planes_async(cf_film* f, const cf_state_view* v, cudaStream_t st) {
+  cfk::Film& F = f->F;
+  const size_t n = f->n;
+  const cudaMemcpyKind k = v->device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  const struct { void* dst; const void* src; size_t bytes; } plain[] = {
+      {v->h, F.hh, 4 * n}, {v->m, F.m, 4 * n}, {v->strata_h, F.sh, 16 * n}, {v->strata_cure, F.scu, 16 * n},
+      {v->sub_refl, F.refl, 32 * n}, {v->lay, F.lay, 4 * n}};
+  for (const auto& p : plain)
+    if (p.dst) CUDA_TRY(f, cudaMemcpyAsync(p.dst, p.src, p.bytes, k, st));
+  if (const void* d = async_src(v, v->strata_pig)) cfk::launch_pig_export(F, f->prec, F.pig, (void*)d, v->pig_format, st);
+  if (const void* d = async_src(v, v->rheo)) cfk::launch_rheo_export(F, f->prec, (float2*)d, n, st);
+  CUDA_TRY(f, cudaGetLastError());
+  return CF_OK;
+}
+
 cf_status cf_read_state(cf_film* f, const cf_state_view* v) {
   if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state: null");
   if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state: pig_format");
@@ -500,6 +593,11 @@ cf_status cf_read_state(cf_film* f, const cf_state_view* v) {
   size_t n = f->n;
   CUDA_TRY(f, cudaDeviceSynchronize());
   cf_status st;
+  if (all_async(v)) {
+    if ((st = read_planes_async(f, v, 0)) != CF_OK) return st;
+    CUDA_TRY(f, cudaDeviceSynchronize());
+    return CF_OK;
+  }
   if (v->h && (st = copy_plane(f, v->h, F.hh, 4 * n, v->device, false)) != CF_OK) return st;
   if (v->m && (st = copy_plane(f, v->m, F.m, 4 * n, v->device, false)) != CF_OK) return st;
   if (v->strata_h && (st = copy_plane(f, v->strata_h, F.sh, 16 * n, v->device, false)) != CF_OK) return st;
@@ -528,8 +626,16 @@ cf_status cf_read_state(cf_film* f, const cf_state_view* v) {
   return CF_OK;
 }
 
+cf_status cf_read_state_async(cf_film* f, const cf_state_view* v, void* stream) {
+  if (!f || !v) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state_async: null");
+  if (v->pig_format < 0 || v->pig_format > 2) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state_async: pig_format");
+  if (!all_async(v)) return fail(f, CF_ERR_INVALID_ARG, "cf_read_state_async: a plane is in pageable host memory");
+  return read_planes_async(f, v, (cudaStream_t)stream);
+}
+
 static cf_status post_frame_stats(cf_film* f, cudaStream_t st, bool sync_host) {
   if (!sync_host) return CF_OK;
+  f->stats_stale = false;
   DevStats ds;
   CUDA_TRY(f, cudaMemcpyAsync(&ds, f->d_stats, sizeof(ds), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(f, cudaStreamSynchronize(st));
@@ -544,6 +650,12 @@ static cf_status post_frame_stats(cf_film* f, cudaStream_t st, bool sync_host) {
 
 cf_status cf_update_params(cf_film* f, float frame_dt, uint32_t substeps) {
   if (!f || !(frame_dt > 0.f) || substeps == 0) return fail(f, CF_ERR_INVALID_ARG, "cf_update_params");
+  if (f->stats_stale) {  // the stats of an asynchronously written state
+    CUDA_TRY(f, cudaDeviceSynchronize());
+    cf_status s = refresh_host_stats(f);
+    if (s != CF_OK) return s;
+    f->stats_stale = false;
+  }
   pack_params(f, frame_dt, substeps);
   return CF_OK;
 }
@@ -632,6 +744,19 @@ cf_status cf_read_color(cf_film* f, uint16_t* out) {
   if (!f || !out) return fail(f, CF_ERR_INVALID_ARG, "cf_read_color");
   CUDA_TRY(f, cudaDeviceSynchronize());
   CUDA_TRY(f, cudaMemcpy(out, f->F.color, 8 * f->n, cudaMemcpyDeviceToHost));
+  return CF_OK;
+}
+
+cf_status cf_read_color_async(cf_film* f, uint16_t* out, void* stream) {
+  if (!f || !out) return fail(f, CF_ERR_INVALID_ARG, "cf_read_color_async");
+  if (!kernel_readable_host(out)) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, out) != cudaSuccess || a.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      return fail(f, CF_ERR_INVALID_ARG, "cf_read_color_async: destination is pageable host memory");
+    }
+  }
+  CUDA_TRY(f, cudaMemcpyAsync(out, f->F.color, 8 * f->n, cudaMemcpyDefault, (cudaStream_t)stream));
   return CF_OK;
 }
 

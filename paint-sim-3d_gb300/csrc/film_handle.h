@@ -47,6 +47,7 @@ struct cf_film {
   size_t dep_cap = 0, dep_items_cap = 0;
   uint32_t dep_nt = 0, dep_pending = 0, dep_tiles_listed = 0;
   double total_deposited = 0.0;  // volume laid inside the canvas (upload_deposits)
+  bool stats_stale = false;      // an asynchronous write changed the state since the host read the stats
 };
 
 // The view that steps this film alone (same kernels as a batch).

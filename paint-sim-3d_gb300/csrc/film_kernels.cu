@@ -1166,23 +1166,34 @@ __global__ void __launch_bounds__(256) k_pig_import_t(Film F, uint4* dst, const 
     dst[PigIO<MODE>::at(F, (uint32_t)(c0 + cl), k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
   }
 }
+// The inverse transpose: a block reads each chunk plane's run of 32 cells,
+// then writes the 32 cells' 64 slots as one contiguous run (the destination
+// may be page-locked host memory written over the link).
 template <int MODE>
-__global__ void k_pig_export(Film F, const uint4* srcp, void* dst, int fmt) {
-  constexpr int QN = PigIO<MODE>::QN, PER = 16 / QN;
-  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= (size_t)F.n * 4 * QN) return;
-  uint32_t c = (uint32_t)(t / (4 * QN));
-  int k = (int)((t / QN) % 4), q = (int)(t % QN);
-  uint4 u = srcp[PigIO<MODE>::at(F, c, k, q)];
-  uint32_t wv[4] = {u.x, u.y, u.z, u.w};
-  for (int e = 0; e < PER; ++e) {
-    float x;
-    if (MODE == CF_PREC_FP32) x = __uint_as_float(wv[e]);
-    else {
-      uint32_t bits = (e & 1) ? (wv[e / 2] >> 16) : (wv[e / 2] & 0xffffu);
-      x = MODE == CF_PREC_REFERENCE ? h16_to_f(bits) : b16_to_f(bits);
+__global__ void __launch_bounds__(256) k_pig_export_t(Film F, const uint4* srcp, void* dst, int fmt) {
+  constexpr int QN = PigIO<MODE>::QN, PER = 16 / QN, CB = 32;
+  __shared__ float sv[CB][65];
+  const size_t c0 = (size_t)blockIdx.x * CB;
+  const int ncell = (int)min((size_t)CB, (size_t)F.n - c0);
+  for (int e = threadIdx.x; e < 4 * QN * CB; e += blockDim.x) {
+    const int cl = e % CB, plane = e / CB;
+    if (cl >= ncell) continue;
+    const int k = plane / QN, q = plane % QN;
+    const uint4 u = srcp[PigIO<MODE>::at(F, (uint32_t)(c0 + cl), k, q)];
+    const uint32_t wv[4] = {u.x, u.y, u.z, u.w};
+    float* v = &sv[cl][16 * k + q * PER];
+    for (int x = 0; x < PER; ++x) {
+      if (MODE == CF_PREC_FP32) v[x] = __uint_as_float(wv[x]);
+      else {
+        const uint32_t bits = (x & 1) ? (wv[x / 2] >> 16) : (wv[x / 2] & 0xffffu);
+        v[x] = MODE == CF_PREC_REFERENCE ? h16_to_f(bits) : b16_to_f(bits);
+      }
     }
-    size_t s = (size_t)c * 64 + 16 * k + q * PER + e;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < ncell * 64; e += blockDim.x) {
+    const size_t s = c0 * 64 + (size_t)e;
+    const float x = sv[e / 64][e % 64];
     if (fmt == CF_PIG_F32) ((float*)dst)[s] = x;
     else if (fmt == CF_PIG_F16) ((uint16_t*)dst)[s] = (uint16_t)f_to_h16(x);
     else ((uint16_t*)dst)[s] = (uint16_t)f_to_b16(x);
@@ -1399,11 +1410,10 @@ void launch_pig_import(const Film& F, int mode, uint4* dst, const void* src, int
   else k_pig_import_t<CF_PREC_BF16><<<g, 256, 0, st>>>(F, dst, src, fmt);
 }
 void launch_pig_export(const Film& F, int mode, const uint4* srcp, void* dst, int fmt, cudaStream_t st) {
-  size_t qn = mode == CF_PREC_FP32 ? 4 : 2;
-  unsigned g = (unsigned)(((size_t)F.n * 4 * qn + 255) / 256);
-  if (mode == CF_PREC_REFERENCE) k_pig_export<CF_PREC_REFERENCE><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
-  else if (mode == CF_PREC_FP32) k_pig_export<CF_PREC_FP32><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
-  else k_pig_export<CF_PREC_BF16><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
+  const unsigned g = (unsigned)(((size_t)F.n + 31) / 32);
+  if (mode == CF_PREC_REFERENCE) k_pig_export_t<CF_PREC_REFERENCE><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
+  else if (mode == CF_PREC_FP32) k_pig_export_t<CF_PREC_FP32><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
+  else k_pig_export_t<CF_PREC_BF16><<<g, 256, 0, st>>>(F, srcp, dst, fmt);
 }
 void launch_rheo_import(const Film& F, int mode, const float2* src, float n_global, size_t n, cudaStream_t st) {
   unsigned g = (unsigned)((n + 255) / 256);
