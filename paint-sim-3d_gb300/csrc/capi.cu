@@ -188,6 +188,7 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, bool 
     for (float** p : {&F.cg_d, &F.cg_x, &F.cg_r, &F.cg_p, &F.cg_pa, &F.cg_pb, &F.cg_q, &F.cg_t, &F.cg_t2})
       add((void**)p, 4 * n);
     add((void**)&F.cg_part, 4 * nt); add((void**)&F.cg_part2, 4 * nt); add((void**)&F.cg, sizeof(cfk::CgState));
+    add((void**)&F.cg_cnt, 4 * ((nt + 31) / 32));
   }
 }
 

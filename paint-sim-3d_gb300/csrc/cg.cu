@@ -135,28 +135,42 @@ __device__ __forceinline__ float lap_diag(const Film& F, int i, int j) {
   return s1 * s1 + s2;
 }
 
-// The shader's workgroup tree over 256 values (film.wgsl:1099-1107), in place.
+// The sum of a 256-thread block's values (the shader sums its workgroup
+// with a tree, film.wgsl:1099-1107; this is a tree too, by warp shuffles, then
+// over the 8 warps): every thread gets the total.
 __device__ __forceinline__ float block_tree(float* sv, float v) {
   const uint32_t li = threadIdx.y * 16u + threadIdx.x;
-  sv[li] = v;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();  // sv may still be read by a previous call
+  if ((li & 31u) == 0u) sv[li >> 5] = v;
   __syncthreads();
-  for (uint32_t s = 128u; s > 0u; s >>= 1u) {
-    if (li < s) sv[li] += sv[li + s];
-    __syncthreads();
-  }
-  return sv[0];
+  float t = sv[0];
+#pragma unroll
+  for (int w = 1; w < 8; ++w) t += sv[w];
+  return t;
 }
 
 // Writes this block's tile partial(s), then reports whether it is the last
-// block of the film to do so (the caller then sums the film's partials).
+// block of the film to do so (the caller then sums the film's partials).  The
+// count is two-level: a counter per group of 32 tiles, and the film's counter
+// taken only by each group's last block, so no address takes more than a few
+// hundred atomics per launch (one counter per film serialised 16 k atomics at
+// 2048^2, tens of microseconds per launch).
 __device__ __forceinline__ bool last_block(const Film& F, uint32_t t, float part, float part2, bool two) {
   __shared__ uint32_t s_last;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     F.cg_part[t] = part;
     if (two) F.cg_part2[t] = part2;
     __threadfence();
-    const uint32_t done = atomicAdd(&F.cg->blocks_done, 1u);
-    s_last = done == F.tw * F.th - 1u ? 1u : 0u;
+    const uint32_t nt = F.tw * F.th, g = t >> 5, ng = (nt + 31u) >> 5;
+    const uint32_t in_group = min(32u, nt - (g << 5));
+    s_last = 0u;
+    if (atomicAdd(&F.cg_cnt[g], 1u) == in_group - 1u) {
+      F.cg_cnt[g] = 0u;  // every block of the group has counted
+      __threadfence();
+      s_last = atomicAdd(&F.cg->blocks_done, 1u) == ng - 1u ? 1u : 0u;
+    }
   }
   __syncthreads();
   if (s_last) __threadfence();
@@ -312,18 +326,65 @@ __global__ void __launch_bounds__(256) kp_cg_lap_p(CG_ARGS, uint32_t step, uint3
 
 // cg_iter_a (film.wgsl:1109-1120, apply_a :1083-1094) and cg_reduce_a
 // (film.wgsl:1214-1222); with the fused cg_iter_c of the previous iteration.
+// Without the implicit capillary term, the block first stages the directions
+// of its tile and a one-cell halo, and the mobilities of the tile and of its
+// lower-left halo, in shared memory (coalesced loads; each cell then reads
+// its 8 neighbours there).
 __global__ void __launch_bounds__(256) kp_cg_iter_a(CG_ARGS, uint32_t step, uint32_t it, int from_lap) {
   CG_TILE
   if (step >= D.implicit_steps || it >= D.implicit_iters) return;
   __shared__ float sv[256];
+  __shared__ float sp[18][18];
+  __shared__ float4 sm[18][17];
   // p_it goes to cg_pa for even it, cg_pb for odd; p_{it-1} is in the other
   // (for it = 0 the init's direction, in cg_pa)
   const float* prev = (it & 1u) || it == 0u ? F.cg_pa : F.cg_pb;
   float* cur = (it & 1u) ? F.cg_pb : F.cg_pa;
   const float beta = F.cg->beta;
   float v = 0.f;
-  if (cell_on) {
-    const float pc = from_lap ? F.cg_q[c] : dir_at(F, c, true, it, beta, prev);
+  if (!from_lap) {
+    const int x0 = (int)(t % F.tw) * 16 - 1, y0 = (int)(t / F.tw) * 16 - 1;
+    const int li = (int)(threadIdx.y * 16u + threadIdx.x);
+    if (tile_on) {
+      for (int e = li; e < 18 * 18; e += 256) {
+        const int x = x0 + e % 18, y = y0 + e / 18;
+        float pv = 0.f;
+        float4 mv = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (x >= 0 && y >= 0 && x < (int)F.w && y < (int)F.h) {
+          const uint32_t n = idx(F, x, y);
+          pv = dir_at(F, n, cell_active(F, x, y), it, beta, prev);
+          if (e % 18 < 17) mv = F.cg_m[n];
+        }
+        sp[e / 18][e % 18] = pv;
+        if (e % 18 < 17) sm[e / 18][e % 18] = mv;
+      }
+    }
+    __syncthreads();
+    if (cell_on) {
+      const int lx = (int)threadIdx.x + 1, ly = (int)threadIdx.y + 1;
+      const float pc = sp[ly][lx];
+      const float k = kappa(P);
+      const int W = (int)F.w, H = (int)F.h;
+      const float4 m0 = sm[ly][lx];
+      float acc_v = pc;
+      // the order of cg_nb (film.wgsl:994-1010)
+      if (i + 1 < W && W_AXIS * m0.x > 0.f) acc_v += k * (W_AXIS * m0.x) * (pc - sp[ly][lx + 1]);
+      if (j + 1 < H && W_AXIS * m0.y > 0.f) acc_v += k * (W_AXIS * m0.y) * (pc - sp[ly + 1][lx]);
+      if (i + 1 < W && j + 1 < H && W_DIAG_LAP * m0.z > 0.f)
+        acc_v += k * (W_DIAG_LAP * m0.z) * (pc - sp[ly + 1][lx + 1]);
+      if (i + 1 < W && j > 0 && W_DIAG_LAP * m0.w > 0.f) acc_v += k * (W_DIAG_LAP * m0.w) * (pc - sp[ly - 1][lx + 1]);
+      if (i > 0 && W_AXIS * sm[ly][lx - 1].x > 0.f) acc_v += k * (W_AXIS * sm[ly][lx - 1].x) * (pc - sp[ly][lx - 1]);
+      if (j > 0 && W_AXIS * sm[ly - 1][lx].y > 0.f) acc_v += k * (W_AXIS * sm[ly - 1][lx].y) * (pc - sp[ly - 1][lx]);
+      if (i > 0 && j > 0 && W_DIAG_LAP * sm[ly - 1][lx - 1].z > 0.f)
+        acc_v += k * (W_DIAG_LAP * sm[ly - 1][lx - 1].z) * (pc - sp[ly - 1][lx - 1]);
+      if (i > 0 && j + 1 < H && W_DIAG_LAP * sm[ly + 1][lx - 1].w > 0.f)
+        acc_v += k * (W_DIAG_LAP * sm[ly + 1][lx - 1].w) * (pc - sp[ly + 1][lx - 1]);
+      v = pc * acc_v;
+      cur[c] = pc;  // other blocks read p_{it-1} from the other plane
+      F.cg_q[c] = acc_v;
+    }
+  } else if (cell_on) {
+    const float pc = F.cg_q[c];
     const float k = kappa(P);
     float acc_v = pc;
     for (int f = 0; f < 8; ++f) {

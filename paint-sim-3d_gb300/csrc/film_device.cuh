@@ -135,6 +135,7 @@ struct Film {
   float4* cg_m;
   float *cg_d, *cg_x, *cg_r, *cg_p, *cg_pa, *cg_pb, *cg_q, *cg_t, *cg_t2, *cg_part, *cg_part2;
   CgState* cg;
+  uint32_t* cg_cnt;  // per group of 32 tiles: blocks that have written their partial
   uint32_t persist_blocks;  // grid of the list kernels: a few blocks per SM
   uint32_t all_active;      // keep every tile active (settings.all_active)
   const float* pigtab;  // 12 x 40
