@@ -21,6 +21,11 @@ HEADERS = ["film_device.cuh", "strata_device.cuh", "strata_lane.cuh", "film_kern
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr"]
+# Per-file device flags.  The deposit pass decides sample by sample whether a
+# lattice point is inside a ribbon (cut planes, x < 1): it keeps one rounding
+# per operation, as the reference's f32 host code and the oracle do, so no
+# fused multiply-add moves a sample across those edges.
+FILE_FLAGS = {"deposit.cu": ["--fmad=false"]}
 
 
 def nvcc():
@@ -46,7 +51,7 @@ def build(force=False, verbose=False, extra=()):
         obj = OUT / (Path(s).stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+            cmd = [nvcc(), *ARCH, *FLAGS, *FILE_FLAGS.get(s, []), *extra, "-c", str(src), "-o", str(obj)]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

@@ -39,11 +39,13 @@ def state_of(f):
     return {"h": s["h"], "m": s["m"], "strata_h": s["strata_h"], "strata_pig": s["strata_pig"], "color": f.color()}
 
 
-@pytest.mark.parametrize("prec", [capi.CF_PREC_REFERENCE, capi.CF_PREC_FP32])
-def test_implicit_frames_vs_fp64_oracle(built, prec):
-    """Bound on h: 1e-5, or 1.5x the FP32 mirror's own distance from FP64."""
+@pytest.mark.parametrize("prec,size", [(capi.CF_PREC_REFERENCE, (96, 80)), (capi.CF_PREC_FP32, (96, 80)),
+                                       (capi.CF_PREC_FP32, (70, 45))])
+def test_implicit_frames_vs_fp64_oracle(built, prec, size):
+    """Bound on h: 1e-5, or 1.5x the FP32 mirror's own distance from FP64.
+    70 x 45 leaves partial tiles on the right and top edges."""
     from canvaz_film.film import Film
-    cv = pour()
+    cv = pour(*size)
     st = po.make_settings(cv.settings)
     pig_mode = capi.PREC_TO_PIG[prec]
     o = po.Oracle(cv.w, cv.h, st, pig_mode, 64)
@@ -108,6 +110,35 @@ def test_implicit_batch_equals_alone(built, graph):
         for f in alone:
             f.encode_frame(8)
         b.step(1, 8)
+    for fa, fb in zip(alone, batched):
+        fa.sync()
+        fb.sync()
+        sa, sb = fa.read_state(), fb.read_state()
+        for k in sa:
+            assert np.array_equal(np.asarray(sa[k]).view(np.uint8), np.asarray(sb[k]).view(np.uint8)), k
+
+
+def test_implicit_adaptive_batch_equals_alone(built):
+    """dt chosen on the device: the launches cover 4 implicit steps and each
+    film skips the ones it does not take; batched equals alone, bit for bit."""
+    from canvaz_film.film import Batch, Film
+    cvs = [pour(64, 48, 21), pour(50, 37, 22)]
+    alone, batched = [], []
+    for cv in cvs:
+        for lst in (alone, batched):
+            f = Film(po.make_settings(cv.settings), cv.w, cv.h, capi.CF_PREC_FP32)
+            f.set_tables(cv.pigtab, cv.cmf)
+            f.write_state(cv.planes)
+            lst.append(f)
+    b = Batch()
+    for f in batched:
+        b.add(f)
+    b.tuning = {"list_blocks_per_sm": 8, "use_graph": 1, "frames_per_graph": 2}
+    for _ in range(3):
+        for f in alone:
+            f.step_adaptive(1 / 60)
+            f.step_adaptive(1 / 60)
+        b.step(2, 1, 1 / 60)
     for fa, fb in zip(alone, batched):
         fa.sync()
         fb.sync()
