@@ -88,7 +88,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD] + sorted(DEPOSIT_WORKLOADS))
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, RELIEF_WORKLOAD]
+                    + sorted(DEPOSIT_WORKLOADS))
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="arrival window of the served workload")
     ap.add_argument("--serve-wall", type=float, default=60.0, help="wall-clock cut-off of the served run")
     ap.add_argument("--serve-steps-scale", type=float, default=1.0, help="scales the served 100-3000 step range")
@@ -239,6 +240,95 @@ def tiles_touched(deps, side, dx):
     lo = np.floor((np.minimum(deps["p0"], deps["p1"]) - rb[:, None]) / tile).clip(0, side // 64 - 1)
     hi = np.floor((np.maximum(deps["p0"], deps["p1"]) + rb[:, None]) / tile).clip(0, side // 64 - 1)
     return int(np.prod(hi - lo + 1, axis=1).sum())
+
+
+RELIEF_WORKLOAD = "relief2048_view3840x2160_fp32"
+
+
+def relief_arm(args):
+    """The render pass's reading of the film: cf_render_relief of a 3840 x 2160
+    top-down view of the default 2048^2 drip canvas (after 5 adaptive steps),
+    4 pixels per 3 cells, the view panned every step.  `value` = output
+    Mpixel/s of device time; `e2e` adds the read-back of each image."""
+    import torch
+    from canvaz_film.film import Film
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    cv = synth.config(1, 0)
+    st = settings_for(cv)
+    film = Film(st, cv.w, cv.h, capi.CF_PREC_FP32)
+    film.set_tables(cv.pigtab, cv.cmf)
+    film.write_state(cv.planes)
+    for _ in range(5):
+        film.step_adaptive(1.0 / 60.0)
+    W, H = 3840, 2160
+    pm = 0.75 * float(st.width_m) / cv.w
+    img = torch.empty(W * H * 4, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def view(k):
+        return 0.02 * (k % 7) * float(st.width_m), 0.03 * (k % 5) * float(st.height_m)
+
+    for k in range(args.warmup):
+        film.render_relief(img.data_ptr(), *view(k), pm, W, H, stream=sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for k in range(args.steps):
+            film.render_relief(img.data_ptr(), *view(k), pm, W, H, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    value = W * H * args.steps / t / 1e6
+    host = torch.empty(W * H * 4, dtype=torch.uint8).pin_memory()
+    t0 = time.perf_counter()
+    for k in range(max(args.e2e_steps, 1)):
+        film.render_relief(img.data_ptr(), *view(k), pm, W, H, stream=sh)
+        with torch.cuda.stream(stream):
+            host.copy_(img, non_blocking=True)
+        stream.synchronize()
+    te = time.perf_counter() - t0
+    peak, peak_kind = peaks()
+    # compulsory bytes per output pixel: the 4 colour texels and 4 x 4 relief
+    # cells it reads are shared by about 0.56 pixels per cell (4/3 px per
+    # cell), so per pixel about (8 B colour + 8 B h, m) x 0.5625 read + 4 B written
+    alg = 16 * 0.5625 + 4
+    cb = None
+    if not args.no_cpu_baseline:
+        import relief_ref as rr
+        fs = film.read_state()
+        col = film.color()
+        R = rr.Relief(cv.w, cv.h, float(st.width_m), float(st.height_m), fs["h"], fs["m"], col)
+        rng = np.random.default_rng(0)
+        pts = np.stack([rng.uniform(0, float(st.width_m), 200000), rng.uniform(0, float(st.height_m), 200000)], 1)
+        t0 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t0 < min(args.cpu_seconds, 20.0):
+            R.sample(pts)
+            n += len(pts)
+        el = time.perf_counter() - t0
+        cb = {"value": n / el / 1e6, "unit": "Mpixel/s", "cores": 1, "kind": "port",
+              "sample": "%d points of the same film through oracle/relief_ref.py (numpy, float64), %.1f s" % (n, el)}
+    line = {"metric": "Mpixel/s", "value": value, "unit": "Mpixel/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (the default drip canvas)",
+            "config": {"workload": RELIEF_WORKLOAD, "view": [W, H], "film": [cv.w, cv.h],
+                       "pixel_m": pm, "l2": "the film's h, m and colour planes (67 MB) fit in L2"},
+            "roofline": {"bound": "hbm", "achieved": alg * W * H * args.steps / t / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg * W * H * args.steps / t / 1e9 / peak,
+                         "peak_source": peak_kind, "alg_bytes_per_pixel": alg, "scope": "k_render_relief",
+                         "traffic": None},
+            "gpu_launches": args.steps, "clocks": clk.summary(),
+            "e2e": {"value": W * H * max(args.e2e_steps, 1) / te / 1e6, "unit": "Mpixel/s", "h2d_bytes_per_step": 64,
+                    "d2h_bytes_per_step": W * H * 4, "steps": max(args.e2e_steps, 1),
+                    "path": "cf_render_relief + read back of the RGBA8 image"},
+            "cpu_baseline": cb}
+    print(json.dumps(line), flush=True)
 
 
 DEPOSIT_SETS = 4
@@ -686,6 +776,8 @@ def main():
         serve_arm(args)
     elif args.workload in DEPOSIT_WORKLOADS:
         deposit_arm(args)
+    elif args.workload == RELIEF_WORKLOAD:
+        relief_arm(args)
     else:
         gpu_arm(args)
 

@@ -312,6 +312,30 @@ cf_status cf_upload_deposits(cf_film* film, const cf_deposit* deps, uint32_t cou
  * not stepped).  No-op when none are pending.  Asynchronous. */
 cf_status cf_lay_deposits(cf_film* film, void* stream);
 
+/* --- the render pass's reading of the film (shaders/render.wgsl) --------------- */
+
+/* Relief and colour at canvas points (metres), as the renderer samples them
+ * with its plain camera: per point 8 floats: surf_cubic (height of h + m,
+ * :335-353), base_slope x and y (:628-638), color_sharp r, g, b, a
+ * (:706-750), wet_bilinear (h, :394-406).  `points` (2 floats each) and
+ * `out` are device memory; enqueued on `stream`. */
+cf_status cf_sample_relief(cf_film* film, const float* points, uint32_t n, float* out, void* stream);
+
+/* A top-down view: pixel (x, y) samples the canvas point
+ * (x0 + (x + 0.5) pixel_m, y0 + (y + 0.5) pixel_m), row 0 at the lowest y;
+ * colour = color_sharp x (ambient + (1 - ambient) max(n . light, 0)) with
+ * the normal of base_slope (normal_from_slope, :640-642), written as sRGB
+ * RGBA8 to `rgba8` (device memory, width x height x 4 bytes).  The shading
+ * is this library's, not the renderer's. */
+typedef struct cf_relief_view {
+    float x0, y0, pixel_m;
+    uint32_t width, height;
+    float light[3];
+    float ambient;
+    uint32_t reserved;
+} cf_relief_view;
+cf_status cf_render_relief(cf_film* film, const cf_relief_view* view, uint8_t* rgba8, void* stream);
+
 /* --- painting files (src/session.rs) ----------------------------------------- */
 
 /* The header fields of a Canvaz painting file (src/session.rs:248-310). */

@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE.  Needs the reference checkout (argument or REFERENCE env
 var, default /root/reference); does nothing when it is absent.  Steps:
 translate.py writes oracle/_ref/ref_shaders.inc (FP64), then g++ compiles
-driver.cpp against it.  Everything it writes stays in oracle/_ref/, which is
+driver.cpp against it; the relief and colour sampling of render.wgsl goes the
+same way into render_ref.inc and librenderref.so (render_driver.cpp).  Everything it writes stays in oracle/_ref/, which is
 git-ignored.
 Usage: python build_ref.py [reference_root]
 """
@@ -29,6 +30,16 @@ def build(ref=None):
     lib = OUT / "libwgslref.so"
     subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "driver.cpp"),
                     "-o", str(lib)], check=True)
+    # the relief / colour sampling of render.wgsl (a subset: the beauty-mode
+    # helpers it never reaches with the plain camera are stubs)
+    sys.path.insert(0, str(HERE))
+    import translate
+    src = translate.translate_subset(str(ref), "render.wgsl",
+                                     ["surf_cubic", "base_slope", "color_sharp", "wet_bilinear"],
+                                     {"color_beauty", "color_crisp", "surf_smooth", "hwarp"}, "wgrr")
+    (OUT / "render_ref.inc").write_text(src)
+    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "render_driver.cpp"),
+                    "-o", str(OUT / "librenderref.so")], check=True)
     return lib
 
 

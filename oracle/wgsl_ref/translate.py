@@ -335,6 +335,56 @@ def translate(ref_root, real="double"):
     return "\n".join(out) + "\n"
 
 
+RGBA = {"r": "x", "g": "y", "b": "z", "a": "w"}
+
+
+def translate_subset(ref_root, module, roots, stubs, namespace, real="double"):
+    """Translate the functions `roots` of one shader module and everything they
+    call, into their own namespace; the functions in `stubs` get empty bodies
+    (the driver never reaches them).  Colour swizzles (.rgb, .a) map to xyzw."""
+    with open("%s/shaders/%s" % (ref_root, module)) as f:
+        src = f.read()
+    items = split_items(src)
+    named = {nm: (it, kind) for it, kind, nm in ((it,) + item_name(it) for it in items) if nm}
+    fns = {nm for nm, (it, kind) in named.items() if kind == "fn"}
+    need, todo = set(), list(roots)
+    while todo:
+        nm = todo.pop()
+        if nm in need:
+            continue
+        need.add(nm)
+        if nm in stubs:
+            continue
+        ids = set(re.findall(r"\b\w+\b", named[nm][0])) - {nm}
+        todo.extend(sorted(ids & fns))
+    consts, structs, globals_, protos, bodies = [], [], [], [], []
+    for it, kind, nm in ((it,) + item_name(it) for it in items):
+        if kind is None:
+            continue
+        if kind == "const":
+            consts.append(conv_global(it, kind, nm).replace("constexpr ", "const ", 1))
+        elif kind == "struct":
+            structs.append(conv_struct(re.sub(r"@\w+(\([^)]*\))?\s*", "", it), nm))
+        elif kind.startswith("var"):
+            g = conv_global(it, kind, nm)
+            g = g.replace("texture_2d<f32>", "Tex").replace("sampler ", "Sampler ")
+            globals_.append(g)
+        elif kind == "fn" and nm in need:
+            it2 = re.sub(r"\.([rgba]{1,4})\b", lambda m: "." + "".join(RGBA[ch] for ch in m.group(1)), it)
+            proto, text = conv_fn(it2, nm)
+            protos.append(proto + ";")
+            if nm in stubs:
+                ret = proto.split(" ", 1)[0]
+                bodies.append(proto + " { return %s{}; }" % ret if ret != "void" else proto + " {}")
+            else:
+                bodies.append(text)
+    hdr = ["// GENERATED by oracle/wgsl_ref/translate.py from the reference shaders; do not commit.",
+           "namespace %s {" % namespace, "using f32 = %s;" % real, "#include \"wgsl_rt_types.inc\""]
+    out = hdr + consts + structs + globals_ + protos + bodies + ["}  // namespace %s" % namespace, ""]
+    out.append("// translated: " + " ".join(sorted(need)) + "; stubs: " + " ".join(sorted(set(stubs) & need)))
+    return "\n".join(out) + "\n"
+
+
 if __name__ == "__main__":
     ref, dst = sys.argv[1], sys.argv[2]
     real = sys.argv[3] if len(sys.argv) > 3 else "double"

@@ -117,6 +117,12 @@ assert C.sizeof(Deposit) == 96
 CF_MAX_DEPOSITS = 65536
 
 
+class ReliefView(C.Structure):
+    """cf_relief_view."""
+    _fields_ = [("x0", C.c_float), ("y0", C.c_float), ("pixel_m", C.c_float), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("light", C.c_float * 3), ("ambient", C.c_float), ("reserved", C.c_uint32)]
+
+
 class BatchTuning(C.Structure):
     """cf_batch_tuning."""
     _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
@@ -194,6 +200,8 @@ def load_library(path=None):
         "cf_deposit_height_at": ([C.POINTER(Deposit), C.POINTER(f32), C.POINTER(f32)], i32),
         "cf_upload_deposits": ([vp, vp, u32, C.POINTER(u32), C.POINTER(C.c_double)], i32),
         "cf_lay_deposits": ([vp, vp], i32),
+        "cf_sample_relief": ([vp, vp, u32, vp, vp], i32),
+        "cf_render_relief": ([vp, C.POINTER(ReliefView), vp, vp], i32),
         "cf_batch_create": ([C.POINTER(vp)], i32),
         "cf_batch_destroy": ([vp], i32),
         "cf_batch_add": ([vp, vp], i32),

@@ -187,6 +187,18 @@ class Film:
         self.total_deposited = tot.value
         return sent.value
 
+    def sample_relief(self, points_ptr, n, out_ptr, stream=None):
+        """cf_sample_relief: 8 floats per canvas point (device pointers)."""
+        self._check(self.L.cf_sample_relief(self.p, points_ptr, n, out_ptr, stream), "cf_sample_relief")
+
+    def render_relief(self, out_ptr, x0, y0, pixel_m, width, height, light=(0.3, 0.5, 0.8), ambient=0.35,
+                      stream=None):
+        """cf_render_relief: a width x height RGBA8 top-down view into out_ptr (device)."""
+        v = capi.ReliefView(x0=x0, y0=y0, pixel_m=pixel_m, width=width, height=height, ambient=ambient)
+        for k in range(3):
+            v.light[k] = light[k]
+        self._check(self.L.cf_render_relief(self.p, C.byref(v), out_ptr, stream), "cf_render_relief")
+
     def lay_deposits(self, stream=None):
         """cf_lay_deposits: lays the uploaded deposits now (asynchronous)."""
         self._check(self.L.cf_lay_deposits(self.p, stream), "cf_lay_deposits")

@@ -1,0 +1,88 @@
+"""The render pass's reading of the film on the GPU (cf_sample_relief,
+cf_render_relief) against the reference's render.wgsl functions
+(tests/golden/relief_samples.npz, FP64)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from canvaz_film import capi
+
+pytestmark = pytest.mark.gpu
+
+FIX = Path(__file__).resolve().parent / "golden" / "relief_samples.npz"
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as g
+    g.build()
+    return True
+
+
+def fixture_film():
+    from canvaz_film.film import Film
+    d = np.load(FIX)
+    w, h = int(d["w"]), int(d["h"])
+    s = capi.Settings.default(width_m=float(d["width_m"]), height_m=float(d["height_m"]))
+    f = Film(s, w, h, capi.CF_PREC_FP32)
+    n = w * h
+    f.write_state({"h": d["h_plane"], "m": d["m_plane"], "rheo": np.tile([1.0, 0.0], (n, 1)).astype(np.float32),
+                   "strata_h": np.zeros((n, 4), np.float32), "strata_cure": np.zeros((n, 4), np.float32),
+                   "strata_pig": np.zeros((n, 64), np.float32), "sub_refl": np.full((n, 16), 0.5, np.float32),
+                   "lay": np.zeros(n, np.uint32)})
+    f.set_plane("color", d["color_f16"].view(np.float16).reshape(-1))  # the colour plane the renderer reads
+    return d, f
+
+
+def test_samples_match_the_reference(built):
+    import torch
+    d, f = fixture_film()
+    pts = torch.from_numpy(np.ascontiguousarray(d["points"])).cuda()
+    out = torch.empty((len(pts), 8), dtype=torch.float32, device="cuda")
+    f.sample_relief(pts.data_ptr(), len(pts), out.data_ptr())
+    torch.cuda.synchronize()
+    got, want = out.cpu().numpy().astype(np.float64), d["out"]
+    scale = np.maximum(np.abs(want).max(0), 1e-30)
+    err = np.abs(got - want) / scale
+    # f32 against FP64: heights and colours to 1e-5 of their range; the
+    # colour sharpening's smoothsteps may flip a few points at their edges
+    assert (err[:, [0, 7]] > 1e-5).mean() == 0, err[:, [0, 7]].max(0)
+    assert (err[:, 3:7] > 1e-4).mean() <= 2e-3, err[:, 3:7].max(0)
+    assert (err[:, 1:3] > 1e-3).mean() <= 2e-3, err[:, 1:3].max(0)
+
+
+def test_render_is_the_shaded_samples(built):
+    import torch
+    d, f = fixture_film()
+    W, H, x0, y0, pm = 96, 64, -1e-3, -2e-3, 0.45e-3
+    img = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+    light, amb = (0.3, 0.5, 0.8), 0.35
+    f.render_relief(img.data_ptr(), x0, y0, pm, W, H, light=light, ambient=amb)
+    yy, xx = np.mgrid[0:H, 0:W]
+    pts = np.stack([x0 + (xx.ravel() + 0.5) * pm, y0 + (yy.ravel() + 0.5) * pm], 1).astype(np.float32)
+    tp = torch.from_numpy(pts).cuda()
+    out = torch.empty((len(pts), 8), dtype=torch.float32, device="cuda")
+    f.sample_relief(tp.data_ptr(), len(pts), out.data_ptr())
+    torch.cuda.synchronize()
+    s = out.cpu().numpy().astype(np.float64)
+    l = np.array(light) / np.linalg.norm(light)
+    nx, ny = -s[:, 1], -s[:, 2]
+    diff = np.maximum((nx * l[0] + ny * l[1] + l[2]) / np.sqrt(nx * nx + ny * ny + 1), 0)
+    k = amb + (1 - amb) * diff
+    lin = np.clip(s[:, 3:6] * k[:, None], 0, 1)
+    srgb = np.where(lin <= 0.0031308, 12.92 * lin, 1.055 * lin ** (1 / 2.4) - 0.055)
+    want = np.round(np.clip(srgb, 0, 1) * 255)
+    got = img.cpu().numpy().reshape(-1, 4)
+    assert np.abs(got[:, :3].astype(np.int32) - want).max() <= 1
+    assert (got[:, 3] == 255).all()
+
+
+def test_errors(built):
+    d, f = fixture_film()
+    L = capi.load_library()
+    assert L.cf_sample_relief(f.p, None, 3, None, None) == capi.CF_ERR_INVALID_ARG
+    assert L.cf_sample_relief(f.p, None, 0, None, None) == capi.CF_OK
+    v = capi.ReliefView(x0=0, y0=0, pixel_m=0.0, width=4, height=4, ambient=0.3)
+    import ctypes as C
+    assert L.cf_render_relief(f.p, C.byref(v), C.c_void_p(16), None) == capi.CF_ERR_INVALID_ARG

@@ -1,0 +1,39 @@
+"""The relief / colour sampling restatement (oracle/relief_ref.py) against
+the reference's own render.wgsl functions (tests/golden/relief_samples.npz,
+written by their mechanical translation in FP64)."""
+from pathlib import Path
+
+import numpy as np
+
+import relief_ref as rr
+
+FIX = Path(__file__).resolve().parent / "golden" / "relief_samples.npz"
+
+
+def load():
+    d = np.load(FIX)
+    R = rr.Relief(int(d["w"]), int(d["h"]), float(d["width_m"]), float(d["height_m"]), d["h_plane"], d["m_plane"],
+                  d["color_f16"].view(np.float16).astype(np.float64))
+    return d, R
+
+
+def test_restatement_equals_the_reference_functions():
+    d, R = load()
+    got, want = R.sample(d["points"]), d["out"]
+    scale = np.maximum(np.abs(want).max(0), 1e-30)
+    assert (np.abs(got - want).max(0) / scale).max() <= 1e-12
+
+
+def test_fixture_covers_the_edge_blend_and_the_outside():
+    d, R = load()
+    pts = d["points"].astype(np.float64)
+    px, py = pts[:, 0], pts[:, 1]
+    i, j, tx, ty = R._grid(px, py)
+    hw = np.stack([R.wet_at(i, j), R.wet_at(i + 1, j), R.wet_at(i, j + 1), R.wet_at(i + 1, j + 1)])
+    hmax, hmin = hw.max(0), hw.min(0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        edge = R.smoothstep(rr.f(0.3), rr.f(0.6), 1.0 - hmin / hmax)
+    sharpened = (hmax > rr.f(1e-6)) & (edge > 0)
+    assert sharpened.sum() > 200
+    assert R.outside(px, py).sum() > 50
+    assert (d["out"][R.outside(px, py), 0] == 0).all()  # no relief outside the canvas
