@@ -245,6 +245,29 @@ def tiles_touched(deps, side, dx):
 RELIEF_WORKLOAD = "relief2048_view3840x2160_fp32"
 
 
+def relief_cpu(film, cv, st, budget_s):
+    """oracle/relief_ref.py (numpy, float64, one core) sampling the film (or,
+    without a device, the canvas as generated) at random canvas points, as
+    many batches of 200k as fit the budget."""
+    import relief_ref as rr
+    if film is not None:
+        fs = film.read_state()
+        hp, mp, col = fs["h"], fs["m"], film.color()
+    else:  # no device: the canvas as generated, a flat grey (the sampling cost does not depend on it)
+        hp, mp, col = cv.planes["h"], cv.planes["m"], np.full((cv.w * cv.h, 4), 0.5)
+    R = rr.Relief(cv.w, cv.h, float(st.width_m), float(st.height_m), hp, mp, col)
+    rng = np.random.default_rng(0)
+    pts = np.stack([rng.uniform(0, float(st.width_m), 200000), rng.uniform(0, float(st.height_m), 200000)], 1)
+    t0 = time.perf_counter()
+    n = 0
+    while n == 0 or time.perf_counter() - t0 < budget_s:
+        R.sample(pts)
+        n += len(pts)
+    el = time.perf_counter() - t0
+    return {"value": n / el / 1e6, "unit": "Mpixel/s", "cores": 1, "kind": "port",
+            "sample": "%d points of the film through oracle/relief_ref.py (numpy, float64), %.1f s" % (n, el)}
+
+
 def relief_arm(args):
     """The render pass's reading of the film: cf_render_relief of a 3840 x 2160
     top-down view of the default 2048^2 drip canvas (after 5 adaptive steps),
@@ -298,22 +321,7 @@ def relief_arm(args):
     # cells it reads are shared by about 0.56 pixels per cell (4/3 px per
     # cell), so per pixel about (8 B colour + 8 B h, m) x 0.5625 read + 4 B written
     alg = 16 * 0.5625 + 4
-    cb = None
-    if not args.no_cpu_baseline:
-        import relief_ref as rr
-        fs = film.read_state()
-        col = film.color()
-        R = rr.Relief(cv.w, cv.h, float(st.width_m), float(st.height_m), fs["h"], fs["m"], col)
-        rng = np.random.default_rng(0)
-        pts = np.stack([rng.uniform(0, float(st.width_m), 200000), rng.uniform(0, float(st.height_m), 200000)], 1)
-        t0 = time.perf_counter()
-        n = 0
-        while time.perf_counter() - t0 < min(args.cpu_seconds, 20.0):
-            R.sample(pts)
-            n += len(pts)
-        el = time.perf_counter() - t0
-        cb = {"value": n / el / 1e6, "unit": "Mpixel/s", "cores": 1, "kind": "port",
-              "sample": "%d points of the same film through oracle/relief_ref.py (numpy, float64), %.1f s" % (n, el)}
+    cb = None if args.no_cpu_baseline else relief_cpu(film, cv, st, min(args.cpu_seconds, 20.0))
     line = {"metric": "Mpixel/s", "value": value, "unit": "Mpixel/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (the default drip canvas)",
@@ -444,6 +452,17 @@ def reference_arm(args):
     """CPU reference path, same workload / metric / unit; rank 0 only."""
     rank, world, _ = dist_env()
     if rank != 0:
+        return
+    if args.workload == RELIEF_WORKLOAD:  # the CPU path needs a film state: the default canvas as written
+        cv = synth.config(1, 0)
+        st = settings_for(cv)
+        cb = relief_cpu(None, cv, st, min(150.0, 5.0 * (args.steps + args.warmup)))
+        print(json.dumps({"impl": "reference", "metric": "Mpixel/s", "value": cb["value"], "unit": "Mpixel/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                          "config": {"workload": args.workload}, "cpu_baseline": cb,
+                          "e2e": {"value": cb["value"], "unit": "Mpixel/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
         return
     if args.workload in DEPOSIT_WORKLOADS:
         cb = deposit_cpu(args.workload, min(150.0, 10.0 * (args.steps + args.warmup)))
