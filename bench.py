@@ -88,7 +88,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, RELIEF_WORKLOAD]
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, RELIEF_WORKLOAD, SNAPSHOT_WORKLOAD]
                     + sorted(DEPOSIT_WORKLOADS))
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="arrival window of the served workload")
     ap.add_argument("--serve-wall", type=float, default=60.0, help="wall-clock cut-off of the served run")
@@ -243,6 +243,75 @@ def tiles_touched(deps, side, dx):
 
 
 RELIEF_WORKLOAD = "relief2048_view3840x2160_fp32"
+
+
+SNAPSHOT_WORKLOAD = "snapshot2048_fp32"
+
+
+def snapshot_arm(args):
+    """Painting files of the default 2048^2 drip canvas after 5 adaptive steps:
+    every step saves the film (cf_snapshot_save: read_state, 32 MiB chunks
+    LZ4-compressed on all host threads) and loads the file into a second film
+    (cf_snapshot_load).  `value` = GB/s of the 8 read_state planes (212 B per
+    cell) saved and loaded; the CPU baseline decodes the same file's chunks
+    with oracle/lz4_ref.py (pure Python, one core) on a bounded sample."""
+    import torch
+    from canvaz_film.film import Film
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    cv = synth.config(1, 0)
+    st = settings_for(cv)
+    films = []
+    for _ in range(2):
+        f = Film(st, cv.w, cv.h, capi.CF_PREC_REFERENCE)
+        f.set_tables(cv.pigtab, cv.cmf)
+        films.append(f)
+    films[0].write_state(cv.planes)
+    for _ in range(5):
+        films[0].step_adaptive(1.0 / 60.0)
+    raw = 212 * cv.w * cv.h
+    for _ in range(args.warmup):
+        films[1].load_snapshot(films[0].save_snapshot())
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        size = 0
+        for _ in range(args.steps):
+            data = films[0].save_snapshot()
+            films[1].load_snapshot(data)
+            size = len(data)
+        t = time.perf_counter() - t0
+    cb = None
+    if not args.no_cpu_baseline:
+        import lz4_ref
+        import struct
+        t1 = time.perf_counter()
+        done = 0
+        off = 48  # header (44 B) and the part count
+        plen, nch = struct.unpack_from("<QI", data, off)
+        off += 12
+        csz = struct.unpack_from("<Q", data, off)[0]
+        chunk = data[off + 8: off + 8 + csz]
+        while done == 0 or time.perf_counter() - t1 < min(args.cpu_seconds, 20.0):
+            done += len(lz4_ref.decompress_size_prepended(chunk))
+        el = time.perf_counter() - t1
+        cb = {"value": done / el / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+              "sample": "decode of the file's first chunk (%d B raw) by oracle/lz4_ref.py, repeated for %.1f s"
+                        % (done, el)}
+    line = {"metric": "GB/s", "value": 2 * raw * args.steps / t / 1e9, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (the default drip canvas)",
+            "config": {"workload": SNAPSHOT_WORKLOAD, "film": [cv.w, cv.h], "raw_bytes": raw, "file_bytes": size,
+                       "ratio": raw / max(size, 1), "host_threads": os.cpu_count()},
+            "roofline": None, "gpu_launches": None, "clocks": clk.summary(),
+            "e2e": {"value": 2 * raw * args.steps / t / 1e9, "unit": "GB/s", "h2d_bytes_per_step": raw,
+                    "d2h_bytes_per_step": raw, "steps": args.steps,
+                    "path": "cf_snapshot_save + cf_snapshot_load (host coder, the film's planes over the link)"},
+            "cpu_baseline": cb}
+    print(json.dumps(line), flush=True)
 
 
 def relief_cpu(film, cv, st, budget_s):
@@ -797,6 +866,8 @@ def main():
         deposit_arm(args)
     elif args.workload == RELIEF_WORKLOAD:
         relief_arm(args)
+    elif args.workload == SNAPSHOT_WORKLOAD:
+        snapshot_arm(args)
     else:
         gpu_arm(args)
 

@@ -8,7 +8,8 @@
 //  - kp_cg_setup: the face mobilities cg_m (and, with the implicit capillary
 //    term, cg_t / cg_t2, the weighted Laplacians of h and of the hold level);
 //  - kp_cg_init: diagonal, right-hand side, residual, first direction;
-//  - per iteration, two launches: kp_cg_iter_a forms the new search direction
+//  - per iteration, two launches over the tiles and two small ones for the
+//    film scalars: kp_cg_iter_a forms the new search direction
 //    p_k = r / d + beta p_{k-1} of its own cell and of its active neighbours
 //    on the fly (so the reference's cg_iter_c needs no launch of its own),
 //    writes it to one of two ping-pong planes and computes q = A p_k;
@@ -17,9 +18,10 @@
 //    (neighbours read h as of before the dispatch), the final direction into
 //    cg_p; kp_cg_rescale: the mass correction and the h commit.
 // Each sum over a film (p.q, r.z, the mass change) is a per-tile tree sum
-// (the shader's order) written by every block of the film, then the last
-// block to finish (an atomic count, no waiting) sums the tile partials in
-// tile order and writes the film's scalars.  A neighbour in an inactive tile
+// written by every block of the film; the film's total, in tile order, comes
+// from kp_cg_scalars (one block per film) in the iterations, and from the
+// last block to finish (an atomic count, no waiting) in the once-per-step
+// kernels.  A neighbour in an inactive tile
 // is read as the reference reads it: its cg_m and cg_p as the last step that
 // covered it left them.
 #include "film_kernels.h"
@@ -352,7 +354,14 @@ __global__ void __launch_bounds__(256) kp_cg_iter_a(CG_ARGS, uint32_t step, uint
         float4 mv = make_float4(0.f, 0.f, 0.f, 0.f);
         if (x >= 0 && y >= 0 && x < (int)F.w && y < (int)F.h) {
           const uint32_t n = idx(F, x, y);
-          pv = dir_at(F, n, cell_active(F, x, y), it, beta, prev);
+          // the loads of both cases are issued together (dir_at's choice after them)
+          const bool act = cell_active(F, x, y);
+          const float pp = prev[n], pk = F.cg_p[n];
+          if (it == 0u) pv = act ? pp : pk;
+          else {
+            const float r = F.cg_r[n], d = F.cg_d[n];
+            pv = act ? r / d + beta * pp : pk;
+          }
           if (e % 18 < 17) mv = F.cg_m[n];
         }
         sp[e / 18][e % 18] = pv;
@@ -403,16 +412,7 @@ __global__ void __launch_bounds__(256) kp_cg_iter_a(CG_ARGS, uint32_t step, uint
     F.cg_q[c] = acc_v;
   }
   const float part = block_tree(sv, v);
-  if (last_block(F, t, part, 0.f, false)) {
-    const float pq = film_total(F, F.cg_part, sv);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      CgState& S = *F.cg;
-      S.pq = pq;
-      S.alpha = pq > 0.f ? S.rz / pq : 0.f;
-      S.beta = 0.f;
-      S.blocks_done = 0u;
-    }
-  }
+  if (threadIdx.x == 0 && threadIdx.y == 0) F.cg_part[t] = part;  // summed by kp_cg_scalars
 }
 
 // cg_iter_b (film.wgsl:1122-1135) and cg_reduce_b (film.wgsl:1224-1232)
@@ -430,13 +430,32 @@ __global__ void __launch_bounds__(256) kp_cg_iter_b(CG_ARGS, uint32_t step, uint
     v = r * r / F.cg_d[c];
   }
   const float part = block_tree(sv, v);
-  if (last_block(F, t, part, 0.f, false)) {
-    const float rz = film_total(F, F.cg_part, sv);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      CgState& S = *F.cg;
-      S.beta = S.rz > 0.f ? rz / S.rz : 0.f;
-      S.rz = rz;
-      S.blocks_done = 0u;
+  if (threadIdx.x == 0 && threadIdx.y == 0) F.cg_part[t] = part;  // summed by kp_cg_scalars
+}
+
+// cg_reduce_a (film.wgsl:1214-1222) after kp_cg_iter_a, cg_reduce_b
+// (:1224-1232) after kp_cg_iter_b: one block per film sums its tile partials
+// (each thread's strided sum in tile order, then the tree) and updates the
+// film's scalars.  A separate launch instead of a last-block count: at 2048^2
+// the fence and atomics of 16 k blocks made the iteration kernels several
+// times slower than their loads.
+__global__ void __launch_bounds__(256) kp_cg_scalars(const Film* __restrict__ films, uint32_t nfilms, uint32_t step,
+                                                     uint32_t it, int after_b) {
+  if (blockIdx.x >= nfilms) return;
+  const Film& F = films[blockIdx.x];
+  const DevParams& D = *F.P;
+  if (step >= D.implicit_steps || it >= D.implicit_iters) return;
+  __shared__ float sv[256];
+  const float total = film_total(F, F.cg_part, sv);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    CgState& S = *F.cg;
+    if (!after_b) {
+      S.pq = total;
+      S.alpha = total > 0.f ? S.rz / total : 0.f;
+      S.beta = 0.f;
+    } else {
+      S.beta = S.rz > 0.f ? total / S.rz : 0.f;
+      S.rz = total;
     }
   }
 }
@@ -544,8 +563,10 @@ uint32_t launch_cg_step(const PackedFrame& V, int mode, uint32_t step, uint32_t 
   for (uint32_t it = 0; it < iters; ++it) {
     if (cap_implicit) { kp_cg_lap_p<<<nt, b, 0, st>>>(A, T, nt, step, it); ++n; }
     kp_cg_iter_a<<<nt, b, 0, st>>>(A, T, nt, step, it, cap_implicit ? 1 : 0);
+    kp_cg_scalars<<<V.nfilms, b, 0, st>>>(A, V.nfilms, step, it, 0);
     kp_cg_iter_b<<<nt, b, 0, st>>>(A, T, nt, step, it);
-    n += 2;
+    kp_cg_scalars<<<V.nfilms, b, 0, st>>>(A, V.nfilms, step, it, 1);
+    n += 4;
   }
   if (cap_implicit) { kp_cg_lap_u<<<nt, b, 0, st>>>(A, T, nt, step); ++n; }
   kp_cg_finish<<<nt, b, 0, st>>>(A, T, nt, step);

@@ -281,17 +281,45 @@ __device__ __forceinline__ void plug_tile(const Film& F, TileId T) {
 }
 
 // film.wgsl:516-537
+// 64 threads per tile, 4 cells each (rows y, y + 4, y + 8, y + 12): every
+// load of the 4 cells is issued before any of them is used, so a warp keeps
+// 4x the bytes in flight behind the tile's dependent prologue.
 __device__ __forceinline__ void limiter_tile(const Film& F, TileId T) {
-  TILE_PROLOGUE
-  float4 f = F.flux[c];
-  float out = fmaxf(f.x, 0.f) + fmaxf(f.y, 0.f) + fmaxf(f.z, 0.f) + fmaxf(f.w, 0.f);
-  if (nb_ok(F, i - 1, j)) out += fmaxf(-F.flux[idx(F, i - 1, j)].x, 0.f);
-  if (nb_ok(F, i, j - 1)) out += fmaxf(-F.flux[idx(F, i, j - 1)].y, 0.f);
-  if (nb_ok(F, i - 1, j - 1)) out += fmaxf(-F.flux[idx(F, i - 1, j - 1)].z, 0.f);
-  if (nb_ok(F, i - 1, j + 1)) out += fmaxf(-F.flux[idx(F, i - 1, j + 1)].w, 0.f);
-  float a = 1.f;
-  if (out > 0.f) a = fminf(1.f, 0.5f * F.hh[c] * P.dx / (P.dt * out));
-  F.alpha[c] = a;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const cf_params& P = F.P->p;
+  const int i = (int)(T.x * 16 + threadIdx.x), W = (int)F.w, H = (int)F.h;
+  const bool al = i > 0 && cell_active(F, i - 1, (int)T.y * 16);  // the left tile (all 4 rows share it)
+  float4 f[4];
+  float nl[4], nd[4], ndl[4], ndu[4], hv[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 4 * r);
+    f[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    nl[r] = nd[r] = ndl[r] = ndu[r] = hv[r] = 0.f;
+    if (i >= W || j >= H) continue;
+    const uint32_t c = idx(F, i, j);
+    f[r] = F.flux[c];
+    hv[r] = F.hh[c];
+    if (i > 0) nl[r] = F.flux[c - 1].x;
+    if (j > 0) nd[r] = F.flux[c - F.w].y;
+    if (i > 0 && j > 0) ndl[r] = F.flux[c - F.w - 1].z;
+    if (i > 0 && j + 1 < H) ndu[r] = F.flux[c + F.w - 1].w;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 4 * r);
+    if (i >= W || j >= H) continue;
+    float out = fmaxf(f[r].x, 0.f) + fmaxf(f[r].y, 0.f) + fmaxf(f[r].z, 0.f) + fmaxf(f[r].w, 0.f);
+    // neighbours of the left tile column, the tile row below and above (film.wgsl nb_ok)
+    const bool l_ok = i > 0 && ((i & 15) ? true : al);
+    if (l_ok) out += fmaxf(-nl[r], 0.f);
+    if (j > 0 && cell_active(F, i, j - 1)) out += fmaxf(-nd[r], 0.f);
+    if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1)) out += fmaxf(-ndl[r], 0.f);
+    if (i > 0 && j + 1 < H && cell_active(F, i - 1, j + 1)) out += fmaxf(-ndu[r], 0.f);
+    float a = 1.f;
+    if (out > 0.f) a = fminf(1.f, 0.5f * hv[r] * P.dx / (P.dt * out));
+    F.alpha[idx(F, i, j)] = a;
+  }
 }
 
 // wetting back-fill (film.wgsl:847-860 / strata.wgsl:314-322) on the current
@@ -1253,7 +1281,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256, 3) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
 template <int MODE>
 __global__ void __launch_bounds__(256, 3) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
-__global__ void __launch_bounds__(256) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
+__global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILE copy_delta_tile(F, T); }
@@ -1361,7 +1389,7 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
     kp_plug<MODE><<<nt, b, 0, st>>>(A, T, nt);
     kp_fluxes<MODE><<<nt, b, 0, st>>>(A, T, nt);
-    kp_limiter<<<nt, b, 0, st>>>(A, T, nt);
+    kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
     kp_apply<MODE><<<nt, b, 0, st>>>(A, T, nt);
     kp_nose<<<nt, b, 0, st>>>(A, T, nt);
     n += 6;
@@ -1447,7 +1475,7 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "laplacian") kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
   else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
   else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
-  else if (n == "limiter") kp_limiter<<<nt, b, 0, st>>>(A, T, nt);
+  else if (n == "limiter") kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
   else if (n == "apply") CFK_LAUNCH(kp_apply, nt, b, st, A, T, nt);
   else if (n == "nose") {
     kp_copy_delta<<<nt, b, 0, st>>>(A, T, nt);  // the snapshot the frame's apply takes
