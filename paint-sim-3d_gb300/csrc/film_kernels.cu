@@ -1278,9 +1278,9 @@ __global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILE plug_t
 // three blocks per SM: the face code needs no more than 64 registers, and
 // the occupancy hides its dependent loads
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
@@ -1290,7 +1290,7 @@ __global__ void __launch_bounds__(256) kp_nose(PACKED_ARGS) { PACKED_TILE nose_t
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILE reduce16_tile<MODE>(F, T); }
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) kp_strata_fast(PACKED_ARGS) { PACKED_TILE strata_fast_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256, 5) kp_strata_fast(PACKED_ARGS) { PACKED_TILE strata_fast_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_strata_limit(PACKED_ARGS) { PACKED_TILE strata_limit_tile(F, T); }
 __global__ void __launch_bounds__(256) kp_face_flags(PACKED_ARGS) { PACKED_TILE face_flags_tile(F, T); }
 __global__ void __launch_bounds__(256) kp_fill_select(PACKED_ARGS) { PACKED_TILE fill_select_tile(F, T); }
@@ -1323,7 +1323,7 @@ __global__ void kp_adaptive_params(const Film* __restrict__ films, uint32_t nfil
 }
 // the strata full path over every film's list, with the film's tables
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) kp_strata_full(const Film* __restrict__ films, uint32_t nfilms) {
+__global__ void __launch_bounds__(256, 4) kp_strata_full(const Film* __restrict__ films, uint32_t nfilms) {
   __shared__ float tab[480];
   __shared__ float cm[48];
   __shared__ float ltab[12];
