@@ -620,12 +620,14 @@ def gpu_arm(args):
     # end to end through the C ABI with host buffers (pinned)
     e2e = None
     if args.e2e_steps > 0:
-        state = film.read_state(pig_format=capi.PREC_TO_PIG[prec] if prec != capi.CF_PREC_FP32 else capi.CF_PIG_F32)
+        # the state in the reference's own layout (write_state's planes: f16
+        # pigment slots, or BF16 where the film stores BF16)
+        pig_fmt = capi.PREC_TO_PIG[prec] if prec != capi.CF_PREC_FP32 else capi.CF_PIG_F16
+        state = film.read_state(pig_format=pig_fmt)
         pinned = {}
         for k, v in state.items():
             tv = torch.from_numpy(np.ascontiguousarray(v))
             pinned[k] = tv.pin_memory().numpy()
-        pig_fmt = capi.CF_PIG_F32 if prec == capi.CF_PREC_FP32 else capi.PREC_TO_PIG[prec]
         h_out = torch.empty(cells, dtype=torch.float32).pin_memory()
         col_out = torch.empty(cells * 4, dtype=torch.int16).pin_memory()
         import ctypes as C
@@ -687,7 +689,8 @@ def gpu_arm(args):
             te = float(tt.item())
         e2e = {"value": world * cells * args.e2e_steps / te / 1e9, "unit": "Gcell-updates/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-               "path": "per step: cf_write_state_async(whole state, pinned host) + step + cf_read_state_async(h) "
+               "path": "per step: cf_write_state_async(whole state in the reference layout, f16 or BF16 "
+                       "pigment slots, pinned host) + step + cf_read_state_async(h) "
                        "+ cf_read_color_async; two films alternate on two streams, uploads one after the "
                        "other on the host link while the other film steps; wall time over the steps"}
 

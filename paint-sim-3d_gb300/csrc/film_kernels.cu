@@ -352,37 +352,48 @@ __device__ __forceinline__ void apply_tile(const Film& F, TileId T) {
   bool moved = false;
   if (i < (int)F.w && j < (int)F.h) {
     const cf_params& P = F.P->p;
-    uint32_t c = idx(F, i, j);
-    float ac = F.alpha[c];
+    const uint32_t c = idx(F, i, j);
+    // Every load of the cell is issued before the first use (the neighbours
+    // in the grid unconditionally, their activity applied after), so a warp
+    // waits for one round trip instead of a chain of them.
+    const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
+    const uint32_t cbs[4] = {hx ? c + 1 : c, hy ? c + F.w : c, (hx && hy) ? c + F.w + 1 : c,
+                             (hx && hm) ? c - F.w + 1 : c};
+    const bool has[4] = {hx, hy, hx && hy, hx && hm};
+    const uint32_t cl = hl ? c - 1 : c, cd = hm ? c - F.w : c, cdl = (hl && hm) ? c - F.w - 1 : c,
+                   cul = (hl && hy) ? c + F.w - 1 : c;
+    const float ac = F.alpha[c];
+    const float4 f4 = F.flux[c];
+    float abn[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) abn[k] = F.alpha[cbs[k]];
+    const float ql = F.flux[cl].x, qd = F.flux[cd].y, qdl = F.flux[cdl].z, qul = F.flux[cul].w;
+    const float al = F.alpha[cl], ad = F.alpha[cd], adl = F.alpha[cdl], aul = F.alpha[cul];
+    const float h0 = F.hh[c];
+    const float4 a = F.acc[c];
     float best = 0.f, div = 0.f;
     uint32_t src = c;
-    float4 f4 = F.flux[c];
-    float f[4] = {f4.x, f4.y, f4.z, f4.w};
-    bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0;
-    uint32_t cbs[4] = {hx ? c + 1 : c, hy ? c + F.w : c, (hx && hy) ? c + F.w + 1 : c, (hx && hm) ? c - F.w + 1 : c};
-    bool has[4] = {hx, hy, hx && hy, hx && hm};
+    const float f[4] = {f4.x, f4.y, f4.z, f4.w};
     float accv[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       float q = f[k], ab = ac;
       if (q < 0.f && has[k]) {
-        ab = F.alpha[cbs[k]];
+        ab = abn[k];
         if (-q * ab > best) { best = -q * ab; src = cbs[k]; }
       }
       div += q * ab;
       accv[k] = q * ab;
     }
-    auto nb_face = [&](float q, uint32_t cn) {
-      float an = F.alpha[cn];
+    auto nb_face = [&](float q, float an, uint32_t cn) {
       if (q < 0.f) an = ac;
       if (q * an > best) { best = q * an; src = cn; }
       div -= q * an;
     };
-    if (nb_ok(F, i - 1, j)) nb_face(F.flux[c - 1].x, c - 1);
-    if (nb_ok(F, i, j - 1)) nb_face(F.flux[c - F.w].y, c - F.w);
-    if (nb_ok(F, i - 1, j - 1)) nb_face(F.flux[c - F.w - 1].z, c - F.w - 1);
-    if (nb_ok(F, i - 1, j + 1)) nb_face(F.flux[c + F.w - 1].w, c + F.w - 1);
-    float h0 = F.hh[c];
+    if (hl && cell_active(F, i - 1, j)) nb_face(ql, al, cl);
+    if (hm && cell_active(F, i, j - 1)) nb_face(qd, ad, cd);
+    if (hl && hm && cell_active(F, i - 1, j - 1)) nb_face(qdl, adl, cdl);
+    if (hl && hy && cell_active(F, i - 1, j + 1)) nb_face(qul, aul, cul);
     float hn = fmaxf(h0 - P.dt * div * P.inv_dx, 0.f);
     if (hn < h0 && hn < DRAINED_FILM) hn = 0.f;
     F.hh[c] = hn;
@@ -391,7 +402,6 @@ __device__ __forceinline__ void apply_tile(const Film& F, TileId T) {
       set_rheo<MODE>(F, c, rmu<MODE>(F, src), rtau<MODE>(F, src), rn<MODE>(F, src));
       backfill<MODE>(F, c, src, hn);
     }
-    float4 a = F.acc[c];
     F.acc[c] = make_float4(a.x + accv[0] * P.dt, a.y + accv[1] * P.dt, a.z + accv[2] * P.dt, a.w + accv[3] * P.dt);
   }
   if (__syncthreads_or(moved) && threadIdx.x == 0 && threadIdx.y == 0)
@@ -406,16 +416,28 @@ __device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
     F.fnorm[c] = make_float2(0.f, 0.f);
     return;
   }
+  // the 3x3 neighbourhood's h and delta_old are loaded before the scan
+  float hn9[9];
+  uint32_t dn9[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    const int x = i + e % 3 - 1, y = j + e / 3 - 1;
+    const uint32_t n = in_grid(F, x, y) ? idx(F, x, y) : c;
+    hn9[e] = F.hh[n];
+    dn9[e] = F.delta_old[n];
+  }
   int bx = 64, by = 64;
   float bd = 1e9f;
+#pragma unroll
   for (int dj = -1; dj <= 1; ++dj)
+#pragma unroll
     for (int di = -1; di <= 1; ++di) {
       int x = i + di, y = j + dj;
       if (!in_grid(F, x, y)) continue;
-      uint32_t n = idx(F, x, y);
+      const int e = (dj + 1) * 3 + di + 1;
       int cx = di, cy = dj;
-      if (F.hh[n] > 0.f) {
-        uint32_t dn = F.delta_old[n];
+      if (hn9[e] > 0.f) {
+        uint32_t dn = dn9[e];
         if ((dn & 0x10000u) == 0u) continue;
         int ox, oy;
         unpack_off(dn, ox, oy);
@@ -1283,9 +1305,9 @@ template <int MODE>
 __global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
-__global__ void __launch_bounds__(256) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(256, 5) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILE copy_delta_tile(F, T); }
-__global__ void __launch_bounds__(256) kp_nose(PACKED_ARGS) { PACKED_TILE nose_tile(F, T); }
+__global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILE nose_tile(F, T); }
 
 template <int MODE>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILE reduce16_tile<MODE>(F, T); }
