@@ -871,11 +871,21 @@ cf_status cf_debug_read(cf_film* f, const char* name, void* host, size_t bytes) 
     return CF_OK;
   }
   if (n == "acc_s") {  // face-major -> [cell][face]
+    // In active tiles a face counts only where strata_split set its face flag
+    // (it does not clear the faces it does not write): the plane reads as the
+    // reference's zeroed-then-written acc_s.
     std::vector<float4> v(4 * (size_t)f->n);
+    std::vector<uint32_t> ff(f->n), tf((size_t)f->tw * f->th);
     CUDA_TRY(f, cudaMemcpy(v.data(), r.ptr, bytes, cudaMemcpyDeviceToHost));
+    CUDA_TRY(f, cudaMemcpy(ff.data(), f->F.fflags, 4 * f->n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(f, cudaMemcpy(tf.data(), f->F.tile_flags, 4 * tf.size(), cudaMemcpyDeviceToHost));
     float4* o = (float4*)host;
-    for (size_t c = 0; c < f->n; ++c)
-      for (int k = 0; k < 4; ++k) o[4 * c + k] = v[(size_t)k * f->n + c];
+    for (size_t c = 0; c < f->n; ++c) {
+      const size_t i = c % f->w, j = c / f->w;
+      const bool act = (tf[(i >> 4) + (j >> 4) * f->tw] & cfk::ACTIVE) != 0u;
+      for (int k = 0; k < 4; ++k)
+        o[4 * c + k] = (!act || ((ff[c] >> k) & 1u)) ? v[(size_t)k * f->n + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     return CF_OK;
   }
   CUDA_TRY(f, cudaMemcpy(host, r.ptr, bytes, cudaMemcpyDeviceToHost));

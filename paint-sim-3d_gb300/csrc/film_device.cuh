@@ -174,6 +174,13 @@ __device__ __forceinline__ int refl_j(const Film& F, int j) {
   return min(max(r, 0), hh - 1);
 }
 __device__ __forceinline__ float4 acc_face(const Film& F, uint32_t c, int f) { return F.acc_s[(size_t)f * F.n + c]; }
+// Face f of cell c as this frame's strata_split left it.  strata_split writes
+// only the faces it evaluates and sets bit f of the cell's face flags where
+// the split is nonzero, so a face whose bit is clear carries no strata flux
+// (its acc_s entry may be stale and is not read).
+__device__ __forceinline__ float4 acc_face_live(const Film& F, uint32_t c, int f, uint32_t flags) {
+  return ((flags >> f) & 1u) ? acc_face(F, c, f) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
 
 template <int MODE>
 __device__ __forceinline__ float rmu(const Film& F, uint32_t c) {

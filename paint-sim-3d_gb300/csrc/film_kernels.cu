@@ -520,14 +520,16 @@ __device__ __forceinline__ void reduce16_tile(const Film& F, TileId T) {
 // strata.wgsl:157-173 for one active cell
 __device__ __forceinline__ float4 strata_limit_at(const Film& F, const cf_params& P, int i, int j) {
   uint32_t c = idx(F, i, j);
-  float4 a0 = acc_face(F, c, 0), a1 = acc_face(F, c, 1), a2 = acc_face(F, c, 2), a3 = acc_face(F, c, 3);
+  const uint32_t f0 = F.fflags[c];
+  float4 a0 = acc_face_live(F, c, 0, f0), a1 = acc_face_live(F, c, 1, f0), a2 = acc_face_live(F, c, 2, f0),
+         a3 = acc_face_live(F, c, 3, f0);
   float out[4];
   out[0] = fmaxf(a0.x, 0.f) + fmaxf(a1.x, 0.f) + fmaxf(a2.x, 0.f) + fmaxf(a3.x, 0.f);
   out[1] = fmaxf(a0.y, 0.f) + fmaxf(a1.y, 0.f) + fmaxf(a2.y, 0.f) + fmaxf(a3.y, 0.f);
   out[2] = fmaxf(a0.z, 0.f) + fmaxf(a1.z, 0.f) + fmaxf(a2.z, 0.f) + fmaxf(a3.z, 0.f);
   out[3] = fmaxf(a0.w, 0.f) + fmaxf(a1.w, 0.f) + fmaxf(a2.w, 0.f) + fmaxf(a3.w, 0.f);
   auto addn = [&](uint32_t n, int f) {
-    float4 v = acc_face(F, n, f);
+    float4 v = acc_face_live(F, n, f, F.fflags[n]);
     out[0] += fmaxf(-v.x, 0.f);
     out[1] += fmaxf(-v.y, 0.f);
     out[2] += fmaxf(-v.z, 0.f);
@@ -551,8 +553,9 @@ __device__ __forceinline__ void strata_limit_tile(const Film& F, TileId T) {
   F.alpha_s[c] = strata_limit_at(F, P, i, j);
 }
 
-// Face flags from acc_s as strata_split writes them (for an inspection
-// dispatch of the strata pass that does not follow a strata_split).
+// Face flags from a whole acc_s plane (for an inspection dispatch of
+// strata_limit or of the strata pass that does not follow a strata_split, on
+// an uploaded acc_s).
 __device__ __forceinline__ void face_flags_tile(const Film& F, TileId T) {
   TILE_PROLOGUE
   uint32_t flags = 0u;
@@ -564,17 +567,6 @@ __device__ __forceinline__ void face_flags_tile(const Film& F, TileId T) {
   F.fflags[c] = flags;
 }
 
-// Whether any of the 8 faces of active cell (i, j) carries a strata flux (the
-// face flags of strata_split): only then is its strata_limit alpha below 1
-// and only then does strata_update move material into or out of it.
-__device__ __forceinline__ bool flux_touched(const Film& F, int i, int j, uint32_t c) {
-  if (F.fflags[c] != 0u) return true;
-  if (i > 0 && cell_active(F, i - 1, j) && (F.fflags[c - 1] & 1u)) return true;
-  if (j > 0 && cell_active(F, i, j - 1) && (F.fflags[c - F.w] & 2u)) return true;
-  if (i > 0 && j > 0 && cell_active(F, i - 1, j - 1) && (F.fflags[c - F.w - 1] & 4u)) return true;
-  if (i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1) && (F.fflags[c + F.w - 1] & 8u)) return true;
-  return false;
-}
 // Whether the stack renormalised to h is not compact (strata.wgsl:222-228),
 // which sends a cell without strata fluxes down the full path as well.
 __device__ __forceinline__ bool not_compact(const cf_params& P, float hc, float4 t4) {
@@ -658,10 +650,13 @@ __device__ __forceinline__ void fluxes_tile(const Film& F, TileId T) {
   });
 }
 
-// strata_split (film.wgsl:475-514) for one tile: acc_s of the active cells
-// is zeroed, then every face with a frame flux is recomputed and its flux
-// split over the upstream cell's strata; the face flags are gathered in
-// shared memory.
+// strata_split (film.wgsl:475-514) for one tile: every face with a frame
+// flux is recomputed and its flux split over the upstream cell's strata; the
+// face flags (bit f: face f's split is nonzero) are gathered in shared memory.
+// The reference zeroes acc_s first; here the faces not written keep stale
+// values, and every reader takes a face only where its flag is set
+// (acc_face_live), which reads the same values without the 64 B per cell of
+// zeroing.
 template <int MODE>
 __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
   __shared__ TileFaces S;
@@ -676,10 +671,8 @@ __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
   const uint32_t c = in ? idx(F, i, j) : 0u;
   const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (in) F.acc_s[(size_t)k * F.n + c] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k = 0; k < 4; ++k)
     tile_faces_add(S, k, in && sel4(a4, k) != 0.f && in_grid(F, i + FACE_DI[k], j + FACE_DJ[k]));
-  }
   __syncthreads();
   const DevParams& D = *F.P;
   tile_faces_each(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
@@ -716,11 +709,35 @@ __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params&
                                                  uint32_t c, float hc, const float* tab, const float* cm,
                                                  const float* ltab) {
   const bool act = (F.tile_flags[T.x + T.y * F.tw] & ACTIVE) != 0u;
+  // The cell's loads are issued together: strata, dry flag and, in an active
+  // tile, the face flags of the cell and of the 4 neighbours whose faces
+  // touch it (their activity tested after).  ft: whether any of the 8 faces
+  // carries a strata flux (the face flags of strata_split); only then is the
+  // strata_limit alpha below 1 and does strata_update move material into or
+  // out of the cell.
   float4 t4 = F.sh[c], cu = F.scu[c];
+  const uint8_t was_dry = F.dry_shaded[c];
   if (act) {
-    const bool ft = flux_touched(F, i, j, c);
+    const bool hl = i > 0, hd = j > 0, hu = j + 1 < (int)F.h;
+    const uint32_t f0 = F.fflags[c], fl = hl ? F.fflags[c - 1] : 0u, fd = hd ? F.fflags[c - F.w] : 0u,
+                   fdl = (hl && hd) ? F.fflags[c - F.w - 1] : 0u, ful = (hl && hu) ? F.fflags[c + F.w - 1] : 0u;
+    const bool ft = f0 != 0u || ((fl & 1u) && cell_active(F, i - 1, j)) || ((fd & 2u) && cell_active(F, i, j - 1)) ||
+                    ((fdl & 4u) && cell_active(F, i - 1, j - 1)) || ((ful & 8u) && cell_active(F, i - 1, j + 1));
     if (ft || not_compact(P, hc, t4)) {
       F.alpha_s[c] = ft ? strata_limit_at(F, P, i, j) : make_float4(1.f, 1.f, 1.f, 1.f);
+      // The full path reads the cell's 4 faces and the 4 its active left,
+      // lower, lower-left and upper-left neighbours own, unmasked: those
+      // strata_split did not write this frame are zeroed here (a face is
+      // zeroed by at most its two cells, both writing zero, and read under
+      // its flag only until the full path).
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (!((f0 >> k) & 1u)) F.acc_s[(size_t)k * F.n + c] = z4;
+      if (hl && !(fl & 1u) && cell_active(F, i - 1, j)) F.acc_s[c - 1] = z4;
+      if (hd && !(fd & 2u) && cell_active(F, i, j - 1)) F.acc_s[F.n + c - F.w] = z4;
+      if (hl && hd && !(fdl & 4u) && cell_active(F, i - 1, j - 1)) F.acc_s[2 * (size_t)F.n + c - F.w - 1] = z4;
+      if (hl && hu && !(ful & 8u) && cell_active(F, i - 1, j + 1)) F.acc_s[3 * (size_t)F.n + c + F.w - 1] = z4;
       list_append(F.full_list, &F.stats->full_count, c);
       return;
     }
@@ -751,9 +768,9 @@ __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params&
   // and those do not change while it stays dry: when the last shade already
   // saw it dry, its colour is current.
   if (hc <= 0.f) {
-    if (F.dry_shaded[c]) return;
+    if (was_dry) return;
     F.dry_shaded[c] = 1u;
-  } else {
+  } else if (was_dry) {
     F.dry_shaded[c] = 0u;
   }
   CellAcc acc;
@@ -862,7 +879,9 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     const bool hlu = i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1);
     // face nb of the 8 (towards this cell positive): the cell's own 4 faces
     // (right, up, up-right, down-right) negated, then the 4 faces its left,
-    // lower, lower-left and upper-left neighbours own; zero where absent
+    // lower, lower-left and upper-left neighbours own; zero where absent.
+    // The strata fast path has zeroed those of them strata_split did not
+    // write this frame.
     auto face_in = [&](int nb) -> float4 {
       switch (nb) {
         case 0: return neg4(acc_face(F, c, 0));
@@ -1505,7 +1524,10 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   }
   else if (n == "strata_split") CFK_LAUNCH(kp_strata_split, nt, b, st, A, T, nt);
   else if (n == "reduce_tiles") launch_reduce(V, mode, st);
-  else if (n == "strata_limit") kp_strata_limit<<<nt, b, 0, st>>>(A, T, nt);
+  else if (n == "strata_limit") {  // the face flags of the acc_s plane it is given
+    kp_face_flags<<<nt, b, 0, st>>>(A, T, nt);
+    kp_strata_limit<<<nt, b, 0, st>>>(A, T, nt);
+  }
   else if (n == "strata_pass") {
     kp_stats_reset<<<fb, 128, 0, st>>>(A, nf);
     kp_face_flags<<<nt, b, 0, st>>>(A, T, nt);
