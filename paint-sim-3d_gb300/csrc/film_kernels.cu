@@ -838,17 +838,22 @@ __device__ __forceinline__ void lane_inflow(const Film& F, const cf_params& P, c
                                             int ni, int nj, float4 f) {
   if (!(f.x > 0.f || f.y > 0.f || f.z > 0.f || f.w > 0.f)) return;
   const uint32_t cn = idx(F, ni, nj);
-  const float4 an4 = cell_active(F, ni, nj) ? F.alpha_s[cn] : make_float4(1.f, 1.f, 1.f, 1.f);
-  const float4 th4 = F.sh[cn], cu4 = F.scu[cn];
+  const bool act = cell_active(F, ni, nj);
+  // the neighbour's stratum values are loaded one at a time in the loop
+  // (scalar loads of lines in L1) rather than held as three float4s, which
+  // keeps the loop under the kernel's register cap
+  const float* th = reinterpret_cast<const float*>(F.sh + cn);
+  const float* cu = reinterpret_cast<const float*>(F.scu + cn);
+  const float* an = reinterpret_cast<const float*>(F.alpha_s + cn);
   float z0 = 0.f;
 #pragma unroll 1
   for (int k = 0; k < 4; ++k) {
-    const float thn = sel4(th4, k);
+    const float thn = th[k];
     const float z1 = z0 + thn;
-    const float v = sel4(f, k) * sel4(an4, k) * P.inv_dx;
+    const float v = sel4(f, k) * (act ? an[k] : 1.f) * P.inv_dx;
     if (v > 0.f && thn > 0.f) {
       const float pin = PigLane<MODE>::load(F, F.pig, cn, k, H.q);
-      lane_add_band(H, s, z0, z1, v, pin, sel4(cu4, k), P.misc[0], P.misc[1]);
+      lane_add_band(H, s, z0, z1, v, pin, cu[k], P.misc[0], P.misc[1]);
     }
     z0 = z1;
   }
