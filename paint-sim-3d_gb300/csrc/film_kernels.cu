@@ -231,8 +231,8 @@ __device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
 template <int MODE>
 __device__ __forceinline__ void plug_tile(const Film& F, TileId T) {
   constexpr int R = 3, S = 16 + 2 * R;
-  __shared__ float sq[S * S], sm[S * S];  // flux q and mass h of each window cell
-  __shared__ uint8_t sy[S * S];           // bit 0: wet cell in the grid, bit 1: tau_y > 0
+  __shared__ float2 sqm[S * S];  // flux q and mass h of each window cell (0, 0 where dry or outside)
+  __shared__ uint8_t sy[S * S];  // bit 0: wet cell in the grid, bit 1: tau_y > 0
   if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
   const DevParams& D = *F.P;
   const cf_params& P = D.p;
@@ -254,8 +254,7 @@ __device__ __forceinline__ void plug_tile(const Film& F, TileId T) {
         mass = hn;
       }
     }
-    sq[q] = qq;
-    sm[q] = mass;
+    sqm[q] = make_float2(qq, mass);
     sy[q] = yl;
   }
   __syncthreads();
@@ -265,18 +264,22 @@ __device__ __forceinline__ void plug_tile(const Film& F, TileId T) {
   F.tmp[c] = 0.f;
   if (F.hh[c] <= 0.f) return;
   if (gb < 1e-6f) return;
+  // The reference adds the wet cells of the window in row-major order; the
+  // dry and outside ones hold q = mass = +0 here, and adding +0 to these
+  // non-negative sums leaves them bit for bit as they are, so every window
+  // cell is added without a branch.
   float sum = 0.f, mass = 0.f;
-  bool yielding = false;
+  uint32_t fl = 0u;
   for (int dy = 0; dy < 7; ++dy)
+#pragma unroll
     for (int dx = 0; dx < 7; ++dx) {
-      int q = (threadIdx.y + dy) * S + threadIdx.x + dx;
-      uint8_t fl = sy[q];
-      if (!(fl & 1u)) continue;  // outside the grid or dry
-      if (fl & 2u) yielding = true;
-      sum += sq[q];
-      mass += sm[q];
+      const int q = (threadIdx.y + dy) * S + threadIdx.x + dx;
+      const float2 v = sqm[q];
+      fl |= sy[q];
+      sum += v.x;
+      mass += v.y;
     }
-  if (!yielding || mass <= 0.f) return;
+  if (!(fl & 2u) || mass <= 0.f) return;
   F.tmp[c] = sum / mass;
 }
 
