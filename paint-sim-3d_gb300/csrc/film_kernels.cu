@@ -195,16 +195,30 @@ template <bool CLEAR>
 __device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
   if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
   __shared__ float su[18][18];
+  __shared__ float sh[16][16], sd[16][16];  // h and nose distance of the tile's own cells
   const cf_params& P = F.P->p;
   const int i0 = (int)T.x * 16 - 1, j0 = (int)T.y * 16 - 1;
-  for (int q = threadIdx.y * 16 + threadIdx.x; q < 18 * 18; q += 256)
-    su[q / 18][q % 18] = usurf(F, P, i0 + q % 18, j0 + q / 18);
+  for (int q = threadIdx.y * 16 + threadIdx.x; q < 18 * 18; q += 256) {
+    // usurf (film.wgsl:147-151) with its three loads issued together
+    const int qx = q % 18, qy = q / 18;
+    const uint32_t n = idx(F, refl_i(F, i0 + qx), refl_j(F, j0 + qy));
+    const float hv = F.hh[n], mv = F.m[n];
+    const uint32_t dl = F.delta[n];
+    int ox, oy;
+    unpack_off(dl, ox, oy);
+    const float d = off_len(ox, oy);
+    su[qy][qx] = hv + mv - (hv > 0.f ? hold_level(P, d) : 0.f);
+    if (qx >= 1 && qx <= 16 && qy >= 1 && qy <= 16) {  // the tile's own cells (in the grid: no reflection)
+      sh[qy - 1][qx - 1] = hv;
+      sd[qy - 1][qx - 1] = d;
+    }
+  }
   __syncthreads();
   const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   const int x = threadIdx.x + 1, y = threadIdx.y + 1;
-  const float hv = F.hh[c];
+  const float hv = sh[threadIdx.y][threadIdx.x];
   if (CLEAR) {
     F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
     F.h_frame[c] = hv;
@@ -215,7 +229,7 @@ __device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
   float dg = su[y - 1][x - 1] + su[y - 1][x + 1] + su[y + 1][x - 1] + su[y + 1][x + 1];
   float l = (W_AXIS * ax + W_DIAG_LAP * dg - (4.0f * W_AXIS + 4.0f * W_DIAG_LAP) * u0) * P.inv_dx * P.inv_dx;
   if (hv > 0.f) {
-    float d = nose_dist(F, c);
+    const float d = sd[threadIdx.y][threadIdx.x];
     if (d <= 3.0f) {
       float2 n = F.fnorm[c];
       if (n.x * n.x + n.y * n.y > 0.5f) pl = line_pressure(F, P, i, j) * expf(-(d - 1.0f) * 0.7f);
