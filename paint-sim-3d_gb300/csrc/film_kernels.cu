@@ -61,12 +61,23 @@ __device__ __forceinline__ void mark_tile(const Film& F, uint32_t t) {
   const uint32_t moved_before = lane == 0u ? F.tile_moved[t] : 0u;
   const int i0 = (int)((t % F.tw) * 16u + (lane & 1u) * 8u), j = (int)((t / F.tw) * 16u + (lane >> 1));
   float hv[8], hf[8];
+  if ((F.w & 3u) == 0u && i0 + 8 <= (int)F.w && j < (int)F.h) {
+    // the half row as two 16-byte loads per plane (planes are 256-byte
+    // aligned, rows start on a multiple of 4 cells, i0 on a multiple of 8)
+    const uint32_t c = idx(F, i0, j);
+    const float4* ph = reinterpret_cast<const float4*>(F.hh + c);
+    const float4* pf = reinterpret_cast<const float4*>(F.h_frame + c);
+    const float4 a0 = ph[0], a1 = ph[1], b0 = pf[0], b1 = pf[1];
+    hv[0] = a0.x; hv[1] = a0.y; hv[2] = a0.z; hv[3] = a0.w; hv[4] = a1.x; hv[5] = a1.y; hv[6] = a1.z; hv[7] = a1.w;
+    hf[0] = b0.x; hf[1] = b0.y; hf[2] = b0.z; hf[3] = b0.w; hf[4] = b1.x; hf[5] = b1.y; hf[6] = b1.z; hf[7] = b1.w;
+  } else {
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const bool in = i0 + k < (int)F.w && j < (int)F.h;
-    const uint32_t c = in ? idx(F, i0 + k, j) : 0u;
-    hv[k] = in ? F.hh[c] : 0.f;
-    hf[k] = in ? F.h_frame[c] : 0.f;
+    for (int k = 0; k < 8; ++k) {
+      const bool in = i0 + k < (int)F.w && j < (int)F.h;
+      const uint32_t c = in ? idx(F, i0 + k, j) : 0u;
+      hv[k] = in ? F.hh[c] : 0.f;
+      hf[k] = in ? F.h_frame[c] : 0.f;
+    }
   }
   uint32_t bits = 0u;
 #pragma unroll
@@ -83,8 +94,9 @@ __device__ __forceinline__ void mark_tile(const Film& F, uint32_t t) {
   }
 }
 
-// film.wgsl:1393-1425 (bit 32 is written in place; the bits read are not it)
-__device__ __forceinline__ void compact_tile(const Film& F, uint32_t t, int all_active) {
+// film.wgsl:1393-1425 (bit 32 is written in place; the bits read are not it).
+// Returns whether the tile is active; the caller counts the active tiles.
+__device__ __forceinline__ bool compact_tile(const Film& F, uint32_t t, int all_active) {
   int tx = (int)(t % F.tw), ty = (int)(t / F.tw);
   uint32_t own = F.tile_flags[t];
   uint32_t any = own & MOVED;
@@ -105,10 +117,10 @@ __device__ __forceinline__ void compact_tile(const Film& F, uint32_t t, int all_
   if (all_active) any = 1u;
   if (any != 0u) {
     F.tile_flags[t] = (own & ~ACTIVE) | ACTIVE;
-    atomicAdd(&F.stats->active_tiles, 1u);
-  } else {
-    F.tile_flags[t] = own & 31u;
+    return true;
   }
+  F.tile_flags[t] = own & 31u;
+  return false;
 }
 
 // The commit of the bottom stratum into the relief (cure.wgsl:119-159), the
@@ -1367,11 +1379,20 @@ __global__ void __launch_bounds__(256) kp_mark_tiles(PACKED_ARGS) {
   const uint2 pe = tiles[e];
   mark_tile(films[pe.x], pe.y);
 }
+// One thread per tile; the active tiles of a warp are counted with one atomic
+// per film instead of one per tile (all the tiles of a film otherwise add to
+// the same counter).
 __global__ void __launch_bounds__(256) kp_compact_tiles(PACKED_ARGS) {
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ntiles) return;
-  const uint2 pe = tiles[e];
-  compact_tile(films[pe.x], pe.y, (int)films[pe.x].all_active);
+  const bool in = e < ntiles;
+  const uint2 pe = in ? tiles[e] : make_uint2(0u, 0u);
+  const bool act = in && compact_tile(films[pe.x], pe.y, (int)films[pe.x].all_active);
+  const unsigned m = __ballot_sync(0xffffffffu, act);
+  if (act) {
+    const unsigned same = __match_any_sync(m, pe.x);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(same) - 1))
+      atomicAdd(&films[pe.x].stats->active_tiles, (uint32_t)__popc(same));
+  }
 }
 #undef PACKED_TILE
 #undef PACKED_ARGS
