@@ -148,6 +148,15 @@ __device__ __forceinline__ bool in_grid(const Film& F, int i, int j) {
 }
 // Appends v to a device list; one atomic per warp (the threads of the warp
 // that append at this point).
+// Folds a tile's h max and mu min (float bits of positive values) into the
+// film's: the film's value is read first and the atomic issued only where the
+// tile's would change it.  Within a pass the max only grows and the min only
+// shrinks, so a stale read costs at most an atomic that changes nothing.
+__device__ __forceinline__ void fold_cfl(DevStats* st, float hm, float mm) {
+  const uint32_t hb = __float_as_uint(hm), mb = __float_as_uint(mm);
+  if (hb > *reinterpret_cast<volatile uint32_t*>(&st->h_max_bits)) atomicMax(&st->h_max_bits, hb);
+  if (mb < *reinterpret_cast<volatile uint32_t*>(&st->mu_min_bits)) atomicMin(&st->mu_min_bits, mb);
+}
 __device__ __forceinline__ void list_append(uint32_t* list, uint32_t* count, uint32_t v) {
   const unsigned m = __activemask();
   const int lane = (int)((threadIdx.y * blockDim.x + threadIdx.x) & 31u);

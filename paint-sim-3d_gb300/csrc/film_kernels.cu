@@ -539,10 +539,7 @@ __device__ __forceinline__ void reduce16_tile(const Film& F, TileId T) {
   if (tid == 0) {
 #pragma unroll
     for (int w = 1; w < 8; ++w) { hm = fmaxf(hm, sh[w]); mm = fminf(mm, sm[w]); }
-    if (hm > 0.f) {
-      atomicMax(&F.stats->h_max_bits, __float_as_uint(hm));
-      atomicMin(&F.stats->mu_min_bits, __float_as_uint(mm));
-    }
+    if (hm > 0.f) fold_cfl(F.stats, hm, mm);
   }
 }
 
@@ -849,10 +846,7 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   if (tid == 0) {
 #pragma unroll
     for (int w = 1; w < 8; ++w) { hm = fmaxf(hm, red_h[w]); mm = fminf(mm, red_m[w]); }
-    if (hm > 0.f) {
-      atomicMax(&F.stats->h_max_bits, __float_as_uint(hm));
-      atomicMin(&F.stats->mu_min_bits, __float_as_uint(mm));
-    }
+    if (hm > 0.f) fold_cfl(F.stats, hm, mm);
   }
 }
 
