@@ -182,9 +182,14 @@ __device__ __forceinline__ void lane_add_band(const HalfWarp& H, LaneStack& s, f
   for (int k = 0; k < 4; ++k) {
     const float tk = s.th[k];
     if (tk <= 0.f) break;
+    // from here up the strata lie above the band: their overlaps are 0, so
+    // their parts are +0 and change nothing
+    if (z0 >= zhi) break;
     const float z1 = z0 + tk;
     const float ov = fmaxf(fminf(zhi, z1) - fmaxf(zlo, z0), 0.f);
-    const float part = vol * ov / span;  // exact: `above` below is compared with 1e-14
+    // exact division (`above` below is compared with 1e-14), skipped where
+    // the overlap is 0 and the part therefore +0
+    const float part = ov > 0.f ? vol * ov / span : 0.f;
     if (part > 0.f) {
       s.pg[k] = lane_mix(H.q, s.pg[k], tk, pin, part);
       s.cu[k] = __fdividef(s.cu[k] * tk + cv * part, tk + part);
