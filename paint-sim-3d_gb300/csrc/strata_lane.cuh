@@ -125,20 +125,29 @@ __device__ __forceinline__ void lane_merge(const HalfWarp& H, LaneStack& s, int 
   }
 }
 __device__ __forceinline__ void lane_compact(const HalfWarp& H, LaneStack& s, float tiny) {  // strata.wgsl:87-103
+  // Each pass changes nothing unless one of its conditions holds for the stack
+  // as it enters the pass, so a stack without a gap (or without a thin
+  // stratum under another) skips that pass's unrolled, predicated moves.
+  auto gap = [&](int k) { return s.th[k] <= 0.f && s.th[k + 1] > 0.f; };
+  if (gap(0) || gap(1) || gap(2)) {
 #pragma unroll
-  for (int sweep = 0; sweep < 4; ++sweep)
+    for (int sweep = 0; sweep < 4; ++sweep)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (gap(k)) {
+          s.th[k] = s.th[k + 1];
+          s.cu[k] = s.cu[k + 1];
+          s.pg[k] = s.pg[k + 1];
+          s.th[k + 1] = 0.f;
+          s.cu[k + 1] = 0.f;
+        }
+  }
+  auto thin = [&](int k) { return s.th[k] > 0.f && s.th[k] < tiny && s.th[k + 1] > 0.f; };
+  if (thin(0) || thin(1) || thin(2)) {
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-      if (s.th[k] <= 0.f && s.th[k + 1] > 0.f) {
-        s.th[k] = s.th[k + 1];
-        s.cu[k] = s.cu[k + 1];
-        s.pg[k] = s.pg[k + 1];
-        s.th[k + 1] = 0.f;
-        s.cu[k + 1] = 0.f;
-      }
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    if (s.th[k] > 0.f && s.th[k] < tiny && s.th[k + 1] > 0.f) lane_merge(H, s, k);
+      if (thin(k)) lane_merge(H, s, k);
+  }
 }
 // strata.wgsl:105-131
 __device__ __forceinline__ void lane_push_top(const HalfWarp& H, LaneStack& s, float vol, float pin, float cv,
