@@ -721,6 +721,18 @@ __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm
   if (tid < 12) ltab[tid] = logf(fmaxf(F.pigtab[tid * 40 + 32], 1e-3f));
 }
 
+// Shared memory of a strata fast-path block: the tables, and the tile's cells
+// to shade with the thicknesses, cure fractions and h the fast path gave them.
+struct FastShade {
+  float tab[480];
+  float cm[48];
+  float ltab[12];
+  float4 nt[256], cu[256];
+  float h[256];
+  uint32_t list[256];
+  uint32_t count;
+};
+
 // Strata pass, part 1, over every cell.  Active cells with a strata flux on a
 // face or a stack that is not compact are listed for part 2, with their
 // strata_limit alpha (strata.wgsl:157-173; 1 without fluxes).  Every other
@@ -732,8 +744,7 @@ __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm
 // without strata become strata_fill candidates.
 template <int MODE>
 __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
-                                                 uint32_t c, float hc, const float* tab, const float* cm,
-                                                 const float* ltab) {
+                                                 uint32_t c, float hc, FastShade& sh, int tid) {
   const bool act = (F.tile_flags[T.x + T.y * F.tw] & ACTIVE) != 0u;
   // The cell's loads are issued together: strata, dry flag and, in an active
   // tile, the face flags of the cell and of the 4 neighbours whose faces
@@ -799,34 +810,54 @@ __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params&
   } else if (was_dry) {
     F.dry_shaded[c] = 0u;
   }
-  CellAcc acc;
-  acc.begin(F.refl + (size_t)c * 16);
+  // shaded after the tile's pass, one cell per half-warp (fast_shade_cells)
+  sh.nt[tid] = make_float4(nt[0], nt[1], nt[2], nt[3]);
+  sh.cu[tid] = cu;
+  sh.h[tid] = hc;
+  list_append(sh.list, &sh.count, (uint32_t)tid);
+}
+// The shade (shade.wgsl:28-84) and composition aggregates (cure.wgsl:3-48)
+// of the tile's cells that the fast path listed: one cell per half-warp, the
+// lanes over pigment slots and bands (strata_lane.cuh, as the full path),
+// so a warp shades two cells with all of its lanes instead of one lane per
+// wet cell of the tile.
+template <int MODE>
+__device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params& P, TileId T, const FastShade& sh,
+                                                 int tid) {
+  const HalfWarp H(tid & 31);
   const bool dbg = P.flags[0] == 1u;
+  const uint32_t n = sh.count;
+  for (uint32_t e = (uint32_t)(tid >> 4); e < n; e += 16u) {
+    const uint32_t t = sh.list[e];
+    const uint32_t c = idx(F, (int)(T.x * 16 + (t & 15u)), (int)(T.y * 16 + (t >> 4)));
+    const float hc = sh.h[t];
+    const float4 nt = sh.nt[t], cu = sh.cu[t];
+    LaneAcc acc;
+    acc.begin(H, F.refl + (size_t)c * 16);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (nt[k] > 0.f) {
-      float pg[16];
-      PigIO<MODE>::load(F, F.pig, c, k, pg);
-      acc.add(k, nt[k], sel4(cu, k), pg, hc, ltab, tab, dbg);
-    } else {
-      acc.ssum += nt[k];
+    for (int k = 0; k < 4; ++k) {
+      const float tk = sel4(nt, k);
+      const float pg = tk > 0.f ? PigLane<MODE>::load(F, F.pig, c, k, H.q) : 0.f;
+      acc.add(H, k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, dbg);
+    }
+    const float4 agg = acc.agg(P);
+    const ushort4 col = acc.color(H, P, sh.cm, hc, F.m[c]);
+    if (H.q == 0) {
+      if (hc > 0.f) F.agg[c] = agg;  // the next cure reads the aggregates of wet cells only
+      F.color[c] = col;
     }
   }
-  // the next cure reads the aggregates of wet cells only
-  if (hc > 0.f) F.agg[c] = acc.agg(P);
-  F.color[c] = acc.color(P, cm, hc, F.m[c]);
 }
 // ... for one tile, together with the CFL reduction of reduce_tiles
 // (film.wgsl:1330-1361; the strata pass changes neither h nor mu, so the
 // order-independent max / min equal the reference's).
 template <int MODE>
 __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
-  __shared__ float tab[480];
-  __shared__ float cm[48];
-  __shared__ float ltab[12];
+  __shared__ FastShade sh;
   __shared__ float red_h[8], red_m[8];
   const int tid = threadIdx.y * 16 + threadIdx.x;
-  load_tables(F, tab, cm, ltab, tid, 256);
+  load_tables(F, sh.tab, sh.cm, sh.ltab, tid, 256);
+  if (tid == 0) sh.count = 0u;
   __syncthreads();
   const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   const cf_params& P = F.P->p;
@@ -835,7 +866,7 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
     const uint32_t c = idx(F, i, j);
     const float hc = F.hh[c];
     if (hc > 4.0f * P.ein[3]) { hm = hc; mm = rmu<MODE>(F, c); }
-    strata_fast_cell<MODE>(F, P, T, i, j, c, hc, tab, cm, ltab);
+    strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
   }
   for (int o = 16; o > 0; o >>= 1) {
     hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
@@ -848,6 +879,7 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
     for (int w = 1; w < 8; ++w) { hm = fmaxf(hm, red_h[w]); mm = fminf(mm, red_m[w]); }
     if (hm > 0.f) fold_cfl(F.stats, hm, mm);
   }
+  fast_shade_cells<MODE>(F, P, T, sh, tid);
 }
 
 // strata.wgsl:175-188 with one cell per half-warp: the material that

@@ -178,8 +178,11 @@ __device__ __forceinline__ void layer_ks_band(const float* pg, const float w[12]
 //    (rheo_from_parts adds the cure-dependent part), and
 //  - the KM shade (shade.wgsl:28-84): each stratum composited over the
 //    substrate, then the surface correction and XYZ -> linear sRGB.
-// Every path (strata pass, fill, cure commit, state upload) goes through this
-// one accumulator, so their colour and aggregates are bitwise alike.
+// The per-cell paths (fill, cure commit, state upload, deposits) go through
+// this one accumulator, so their colour and aggregates are bitwise alike; the
+// strata pass shades with the half-warp form of the same sums (LaneAcc in
+// strata_lane.cuh), whose tree-ordered sums may differ from it in the last
+// bits.
 struct CellAcc {
   // composition
   float total, lnmu, tau, thin, wsum, nsum, nw;
