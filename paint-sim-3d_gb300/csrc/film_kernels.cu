@@ -721,6 +721,9 @@ __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm
   if (tid < 12) ltab[tid] = logf(fmaxf(F.pigtab[tid * 40 + 32], 1e-3f));
 }
 
+// A warp of the strata fast path shades its cells lane by lane when at least
+// this many of its lanes have one (see strata_fast_cell).
+constexpr int FAST_SHADE_LANES = 20;
 // Shared memory of a strata fast-path block: the tables, and the tile's cells
 // to shade with the thicknesses, cure fractions and h the fast path gave them.
 struct FastShade {
@@ -743,7 +746,7 @@ struct FastShade {
 // are shaded, as the reference's full-grid shade does.  Active wet cells left
 // without strata become strata_fill candidates.
 template <int MODE>
-__device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
+__device__ __forceinline__ bool strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
                                                  uint32_t c, float hc, FastShade& sh, int tid) {
   const bool act = (F.tile_flags[T.x + T.y * F.tw] & ACTIVE) != 0u;
   // The cell's loads are issued together: strata, dry flag and, in an active
@@ -776,7 +779,7 @@ __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params&
       if (hl && hd && !(fdl & 4u) && cell_active(F, i - 1, j - 1)) F.acc_s[2 * (size_t)F.n + c - F.w - 1] = z4;
       if (hl && hu && !(ful & 8u) && cell_active(F, i - 1, j + 1)) F.acc_s[3 * (size_t)F.n + c + F.w - 1] = z4;
       list_append(F.full_list, &F.stats->full_count, c);
-      return;
+      return false;
     }
   }
   float nt[4] = {t4.x, t4.y, t4.z, t4.w};
@@ -805,16 +808,40 @@ __device__ __forceinline__ void strata_fast_cell(const Film& F, const cf_params&
   // and those do not change while it stays dry: when the last shade already
   // saw it dry, its colour is current.
   if (hc <= 0.f) {
-    if (was_dry) return;
+    if (was_dry) return false;
     F.dry_shaded[c] = 1u;
   } else if (was_dry) {
     F.dry_shaded[c] = 0u;
   }
-  // shaded after the tile's pass, one cell per half-warp (fast_shade_cells)
   sh.nt[tid] = make_float4(nt[0], nt[1], nt[2], nt[3]);
   sh.cu[tid] = cu;
   sh.h[tid] = hc;
-  list_append(sh.list, &sh.count, (uint32_t)tid);
+  return true;
+}
+// The shade and aggregates of one cell the fast path left to shade, by its
+// own lane (CellAcc).
+template <int MODE>
+__device__ __forceinline__ void fast_shade_lane(const Film& F, const cf_params& P, uint32_t c, const FastShade& sh,
+                                                int tid) {
+  const float4 nt = sh.nt[tid], cu = sh.cu[tid];
+  const float hc = sh.h[tid];
+  CellAcc acc;
+  acc.begin(F.refl + (size_t)c * 16);
+  const bool dbg = P.flags[0] == 1u;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float tk = sel4(nt, k);
+    if (tk > 0.f) {
+      float pg[16];
+      PigIO<MODE>::load(F, F.pig, c, k, pg);
+      acc.add(k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, dbg);
+    } else {
+      acc.ssum += tk;
+    }
+  }
+  // the next cure reads the aggregates of wet cells only
+  if (hc > 0.f) F.agg[c] = acc.agg(P);
+  F.color[c] = acc.color(P, sh.cm, hc, F.m[c]);
 }
 // The shade (shade.wgsl:28-84) and composition aggregates (cure.wgsl:3-48)
 // of the tile's cells that the fast path listed: one cell per half-warp, the
@@ -862,11 +889,22 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   const cf_params& P = F.P->p;
   float hm = 0.f, mm = 1e9f;
+  bool shade = false;
+  uint32_t c = 0u;
   if (i < (int)F.w && j < (int)F.h) {
-    const uint32_t c = idx(F, i, j);
+    c = idx(F, i, j);
     const float hc = F.hh[c];
     if (hc > 4.0f * P.ein[3]) { hm = hc; mm = rmu<MODE>(F, c); }
-    strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
+    shade = strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
+  }
+  // Where at least FAST_SHADE_LANES lanes of the warp have a cell to shade,
+  // each shades its own; where fewer do, the cells are shaded after the
+  // tile's pass by half-warps (fast_shade_cells), which costs about 1/20 of a
+  // warp-wide shade per cell.
+  const unsigned want = __ballot_sync(0xffffffffu, shade);
+  if (shade) {
+    if (__popc(want) >= FAST_SHADE_LANES) fast_shade_lane<MODE>(F, P, c, sh, tid);
+    else list_append(sh.list, &sh.count, (uint32_t)tid);
   }
   for (int o = 16; o > 0; o >>= 1) {
     hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
