@@ -727,6 +727,7 @@ constexpr int FAST_SHADE_LANES = 20;
 // Shared memory of a strata fast-path block: the tables, and the tile's cells
 // to shade with the thicknesses, cure fractions and h the fast path gave them.
 struct FastShade {
+  alignas(16) float kst[16 * 24];  // band-major K, S (layer_ks_band_t)
   float tab[480];
   float cm[48];
   float ltab[12];
@@ -834,7 +835,7 @@ __device__ __forceinline__ void fast_shade_lane(const Film& F, const cf_params& 
     if (tk > 0.f) {
       float pg[16];
       PigIO<MODE>::load(F, F.pig, c, k, pg);
-      acc.add(k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, dbg);
+      acc.add_t(k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, sh.kst, dbg);
     } else {
       acc.ssum += tk;
     }
@@ -884,6 +885,10 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   __shared__ float red_h[8], red_m[8];
   const int tid = threadIdx.y * 16 + threadIdx.x;
   load_tables(F, sh.tab, sh.cm, sh.ltab, tid, 256);
+  for (int e = tid; e < 16 * 24; e += 256) {
+    const int b = e / 24, r = e % 24;
+    sh.kst[e] = F.pigtab[(r < 12 ? r : r - 12) * 40 + (r < 12 ? 0 : 16) + b];
+  }
   if (tid == 0) sh.count = 0u;
   __syncthreads();
   const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);

@@ -171,6 +171,31 @@ __device__ __forceinline__ void layer_ks_band(const float* pg, const float w[12]
   k = k * scale;
   s = s * scale;
 }
+// layer_ks_band from a band-major copy of the table: kst[24 b + p] = K of
+// pigment p in band b, kst[24 b + 12 + p] = its S (16-byte aligned), read as
+// six 16-byte loads instead of 24 scalar ones.  Every pigment is added: a
+// pigment with no amount has w = 0 (layer_weights), and adding w * K = +0 to
+// these non-negative sums leaves them bit for bit as layer_ks_band's.
+__device__ __forceinline__ void layer_ks_band_t(const float w[12], float scale, const float* kst, int b, float& k,
+                                                float& s) {
+  const float4* t = reinterpret_cast<const float4*>(kst + b * 24);
+  k = 0.f;
+  s = 0.f;
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {  // pigments 4g .. 4g + 3
+    const float4 kq = t[g], sq = t[3 + g];
+    k += w[4 * g] * kq.x;
+    s += w[4 * g] * sq.x;
+    k += w[4 * g + 1] * kq.y;
+    s += w[4 * g + 1] * sq.y;
+    k += w[4 * g + 2] * kq.z;
+    s += w[4 * g + 2] * sq.z;
+    k += w[4 * g + 3] * kq.w;
+    s += w[4 * g + 3] * sq.w;
+  }
+  k = k * scale;
+  s = s * scale;
+}
 
 // Per-cell accumulation over the final strata, bottom to top, of
 //  - the pigment part of the rheology composition (cure.wgsl:3-48), kept as
@@ -231,6 +256,20 @@ struct CellAcc {
   // stratum k (in order 0..3) of thickness t, cure u and slots pg
   __device__ __forceinline__ void add(int k, float t, float u, const float* pg, float hv, const float* lnmu_tab,
                                       const float* tab, bool debug) {
+    add_with(k, t, u, pg, hv, lnmu_tab, tab, debug, [&](const float* w, float sc, int b, float& kk, float& ss) {
+      layer_ks_band(pg, w, sc, tab, b, kk, ss);
+    });
+  }
+  // the same with the K, S table band-major in shared memory (layer_ks_band_t)
+  __device__ __forceinline__ void add_t(int k, float t, float u, const float* pg, float hv, const float* lnmu_tab,
+                                        const float* tab, const float* kst, bool debug) {
+    add_with(k, t, u, pg, hv, lnmu_tab, tab, debug, [&](const float* w, float sc, int b, float& kk, float& ss) {
+      layer_ks_band_t(w, sc, kst, b, kk, ss);
+    });
+  }
+  template <class KsBand>
+  __device__ __forceinline__ void add_with(int k, float t, float u, const float* pg, float hv, const float* lnmu_tab,
+                                           const float* tab, bool debug, KsBand ks_band) {
     ssum += t;
     if (t > 0.f) {
       add_comp(t, pg, lnmu_tab);
@@ -240,7 +279,7 @@ struct CellAcc {
 #pragma unroll 4
         for (int b = 0; b < 16; ++b) {
           float kk, ss, rr, tt;
-          layer_ks_band(pg, w, sc, tab, b, kk, ss);
+          ks_band(w, sc, b, kk, ss);
           km_layer(kk, ss, t, rr, tt);
           r[b] = composite(rr, tt, r[b]);
         }
