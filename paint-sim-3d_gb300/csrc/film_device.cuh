@@ -349,14 +349,6 @@ __device__ __forceinline__ float band_flux(float up, float y, float za, float zb
   return up * ((zb - za) - n / (2.0f * n + 1.0f) * y * (ta - tb));
 }
 
-// film.wgsl:147-151
-__device__ __forceinline__ float usurf(const Film& F, const cf_params& P, int i, int j) {
-  uint32_t c = idx(F, refl_i(F, i), refl_j(F, j));
-  float hv = F.hh[c];
-  float hold = 0.f;
-  if (hv > 0.f) hold = hold_level(P, nose_dist(F, c));
-  return hv + F.m[c] - hold;
-}
 // film.wgsl:190-201
 __device__ __forceinline__ float line_pressure(const Film& F, const cf_params& P, int i, int j) {
   if (i < 1 || j < 1 || i + 1 >= (int)F.w || j + 1 >= (int)F.h) return 0.f;

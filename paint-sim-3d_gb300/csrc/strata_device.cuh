@@ -122,29 +122,6 @@ __device__ inline void stack_push_top(Stack& s, float vol, const float* pg, floa
   for (int q = 0; q < 16; ++q) s.pg[t][q] = pg[q];
   s.cu[t] = cv;
 }
-// strata.wgsl:133-155
-__device__ inline void stack_add_band(Stack& s, float zlo, float zhi, float vol, const float* pg, float cv, float tiny,
-                                      float close_d) {
-  if (vol <= 0.f) return;
-  float span = fmaxf(zhi - zlo, 1e-12f);
-  float z0 = 0.f, above = vol;
-  for (int k = 0; k < 4; ++k) {
-    float tk = s.th[k];
-    if (tk <= 0.f) break;
-    float z1 = z0 + tk;
-    float ov = fmaxf(fminf(zhi, z1) - fmaxf(zlo, z0), 0.f);
-    float part = vol * ov / span;
-    if (part > 0.f) {
-      pig_mix(s.pg[k], tk, pg, part, s.pg[k]);
-      s.cu[k] = (s.cu[k] * tk + cv * part) / (tk + part);
-      s.th[k] = tk + part;
-      above -= part;
-    }
-    z0 = z1;
-  }
-  if (above > 1e-14f) stack_push_top(s, above, pg, cv, tiny, close_d);
-}
-
 // km.wgsl:17-33 for all bands at once: K,S of one stratum's pigment mix.
 __device__ __forceinline__ void layer_weights(const float* pg, const float* tab, float w[12], float& scale) {
   float amount = 0.f, weight = 0.f;
