@@ -375,62 +375,93 @@ template <int MODE>
 // Every tile (active or not) also snapshots delta into delta_old for the
 // nose that follows (apply does not write delta).
 __device__ __forceinline__ void apply_tile(const Film& F, TileId T) {
-  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
-  if (i < (int)F.w && j < (int)F.h) F.delta_old[idx(F, i, j)] = F.delta[idx(F, i, j)];
-  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
-  bool moved = false;
-  if (i < (int)F.w && j < (int)F.h) {
-    const cf_params& P = F.P->p;
-    const uint32_t c = idx(F, i, j);
-    // Every load of the cell is issued before the first use (the neighbours
-    // in the grid unconditionally, their activity applied after), so a warp
-    // waits for one round trip instead of a chain of them.
-    const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
-    const uint32_t cbs[4] = {hx ? c + 1 : c, hy ? c + F.w : c, (hx && hy) ? c + F.w + 1 : c,
-                             (hx && hm) ? c - F.w + 1 : c};
-    const bool has[4] = {hx, hy, hx && hy, hx && hm};
-    const uint32_t cl = hl ? c - 1 : c, cd = hm ? c - F.w : c, cdl = (hl && hm) ? c - F.w - 1 : c,
-                   cul = (hl && hy) ? c + F.w - 1 : c;
-    const float ac = F.alpha[c];
-    const float4 f4 = F.flux[c];
-    float abn[4];
+  // 128 threads per tile, 2 cells each (rows y and y + 8): every load of
+  // both cells (the neighbours in the grid unconditionally, their activity
+  // applied after) is issued before the first use.
+  constexpr int R = 2;
+  const int i = (int)(T.x * 16 + threadIdx.x);
+  const bool ci = i < (int)F.w;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) abn[k] = F.alpha[cbs[k]];
-    const float ql = F.flux[cl].x, qd = F.flux[cd].y, qdl = F.flux[cdl].z, qul = F.flux[cul].w;
-    const float al = F.alpha[cl], ad = F.alpha[cd], adl = F.alpha[cdl], aul = F.alpha[cul];
-    const float h0 = F.hh[c];
-    const float4 a = F.acc[c];
+  for (int r = 0; r < R; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 8 * r);
+    if (ci && j < (int)F.h) F.delta_old[idx(F, i, j)] = F.delta[idx(F, i, j)];
+  }
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const cf_params& P = F.P->p;
+  bool moved = false;
+  uint32_t cc[R], cbs[R][4], cl[R], cd[R], cdl[R], cul[R];
+  float ac[R], abn[R][4], ql[R], qd[R], qdl[R], qul[R], al[R], ad[R], adl[R], aul[R], h0[R];
+  float4 f4[R], a4[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 8 * r);
+    const bool in = ci && j < (int)F.h;
+    const uint32_t c = in ? idx(F, i, j) : 0u;
+    cc[r] = c;
+    const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
+    cbs[r][0] = hx ? c + 1 : c;
+    cbs[r][1] = hy ? c + F.w : c;
+    cbs[r][2] = (hx && hy) ? c + F.w + 1 : c;
+    cbs[r][3] = (hx && hm) ? c - F.w + 1 : c;
+    cl[r] = hl ? c - 1 : c;
+    cd[r] = hm ? c - F.w : c;
+    cdl[r] = (hl && hm) ? c - F.w - 1 : c;
+    cul[r] = (hl && hy) ? c + F.w - 1 : c;
+    if (!in) continue;
+    ac[r] = F.alpha[c];
+    f4[r] = F.flux[c];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) abn[r][k] = F.alpha[cbs[r][k]];
+    ql[r] = F.flux[cl[r]].x;
+    qd[r] = F.flux[cd[r]].y;
+    qdl[r] = F.flux[cdl[r]].z;
+    qul[r] = F.flux[cul[r]].w;
+    al[r] = F.alpha[cl[r]];
+    ad[r] = F.alpha[cd[r]];
+    adl[r] = F.alpha[cdl[r]];
+    aul[r] = F.alpha[cul[r]];
+    h0[r] = F.hh[c];
+    a4[r] = F.acc[c];
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 8 * r);
+    if (!(ci && j < (int)F.h)) continue;
+    const uint32_t c = cc[r];
+    const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
+    const bool has[4] = {hx, hy, hx && hy, hx && hm};
     float best = 0.f, div = 0.f;
     uint32_t src = c;
-    const float f[4] = {f4.x, f4.y, f4.z, f4.w};
+    const float f[4] = {f4[r].x, f4[r].y, f4[r].z, f4[r].w};
     float accv[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      float q = f[k], ab = ac;
+      float q = f[k], ab = ac[r];
       if (q < 0.f && has[k]) {
-        ab = abn[k];
-        if (-q * ab > best) { best = -q * ab; src = cbs[k]; }
+        ab = abn[r][k];
+        if (-q * ab > best) { best = -q * ab; src = cbs[r][k]; }
       }
       div += q * ab;
       accv[k] = q * ab;
     }
     auto nb_face = [&](float q, float an, uint32_t cn) {
-      if (q < 0.f) an = ac;
+      if (q < 0.f) an = ac[r];
       if (q * an > best) { best = q * an; src = cn; }
       div -= q * an;
     };
-    if (hl && cell_active(F, i - 1, j)) nb_face(ql, al, cl);
-    if (hm && cell_active(F, i, j - 1)) nb_face(qd, ad, cd);
-    if (hl && hm && cell_active(F, i - 1, j - 1)) nb_face(qdl, adl, cdl);
-    if (hl && hy && cell_active(F, i - 1, j + 1)) nb_face(qul, aul, cul);
-    float hn = fmaxf(h0 - P.dt * div * P.inv_dx, 0.f);
-    if (hn < h0 && hn < DRAINED_FILM) hn = 0.f;
+    if (hl && cell_active(F, i - 1, j)) nb_face(ql[r], al[r], cl[r]);
+    if (hm && cell_active(F, i, j - 1)) nb_face(qd[r], ad[r], cd[r]);
+    if (hl && hm && cell_active(F, i - 1, j - 1)) nb_face(qdl[r], adl[r], cdl[r]);
+    if (hl && hy && cell_active(F, i - 1, j + 1)) nb_face(qul[r], aul[r], cul[r]);
+    float hn = fmaxf(h0[r] - P.dt * div * P.inv_dx, 0.f);
+    if (hn < h0[r] && hn < DRAINED_FILM) hn = 0.f;
     F.hh[c] = hn;
-    moved = fabsf(hn - h0) > MOVE_EPS;
-    if (h0 <= 0.f && src != c) {
+    moved = moved || fabsf(hn - h0[r]) > MOVE_EPS;
+    if (h0[r] <= 0.f && src != c) {
       set_rheo<MODE>(F, c, rmu<MODE>(F, src), rtau<MODE>(F, src), rn<MODE>(F, src));
       backfill<MODE>(F, c, src, hn);
     }
+    const float4 a = a4[r];
     F.acc[c] = make_float4(a.x + accv[0] * P.dt, a.y + accv[1] * P.dt, a.z + accv[2] * P.dt, a.w + accv[3] * P.dt);
   }
   if (__syncthreads_or(moved) && threadIdx.x == 0 && threadIdx.y == 0)
@@ -1427,7 +1458,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
-__global__ void __launch_bounds__(256, 5) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
+__global__ void __launch_bounds__(128) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILE copy_delta_tile(F, T); }
 __global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILE nose_tile(F, T); }
 
@@ -1543,7 +1574,7 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     kp_plug<MODE><<<nt, b, 0, st>>>(A, T, nt);
     kp_fluxes<MODE><<<nt, b, 0, st>>>(A, T, nt);
     kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
-    kp_apply<MODE><<<nt, b, 0, st>>>(A, T, nt);
+    kp_apply<MODE><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
     kp_nose<<<nt, b, 0, st>>>(A, T, nt);
     n += 6;
   }
@@ -1629,7 +1660,7 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
   else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
   else if (n == "limiter") kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
-  else if (n == "apply") CFK_LAUNCH(kp_apply, nt, b, st, A, T, nt);
+  else if (n == "apply") CFK_LAUNCH(kp_apply, nt, dim3(16, 8), st, A, T, nt);
   else if (n == "nose") {
     kp_copy_delta<<<nt, b, 0, st>>>(A, T, nt);  // the snapshot the frame's apply takes
     kp_nose<<<nt, b, 0, st>>>(A, T, nt);
