@@ -321,6 +321,17 @@ cf_status cf_lay_deposits(cf_film* film, void* stream);
  * `out` are device memory; enqueued on `stream`. */
 cf_status cf_sample_relief(cf_film* film, const float* points, uint32_t n, float* out, void* stream);
 
+/* The renderer's key-light shadow (render.wgsl shadow_at :846-866, plain
+ * camera): per point (x, y, z0) in metres, 2 floats: surf_bilinear(x, y)
+ * (:314-326) and the shadow factor in [0, 1] of a ray from height z0 toward
+ * `light` (unit vector, z up; 1 for light[2] <= 0.05), marched 20 steps of
+ * 1.5 cells over the bilinear relief until it rises above `top`
+ * (cam.canvas.w: the renderer passes max(h_max, s_max) + 0.5 mm).
+ * `points` (3 floats each) and `out` are device memory; enqueued on
+ * `stream`. */
+cf_status cf_relief_shadow(cf_film* film, const float* points, uint32_t n, const float* light, float top, float* out,
+                           void* stream);
+
 /* A top-down view: pixel (x, y) samples the canvas point
  * (x0 + (x + 0.5) pixel_m, y0 + (y + 0.5) pixel_m), row 0 at the lowest y;
  * colour = color_sharp x (ambient + (1 - ambient) max(n . light, 0)) with

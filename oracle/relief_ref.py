@@ -6,7 +6,8 @@ with the plain camera (no beauty mode, colour plane at the film's
 resolution):
   surf_at :305-312, surf_cubic :335-353, cr_w :328-333,
   wet_at :355-361, wet_bilinear :394-406, col_at :644-652,
-  color_sharp :706-750, base_slope :628-638.
+  color_sharp :706-750, base_slope :628-638; the key-light shadow march
+  surf_bilinear :314-326, shadow_at :846-866 (surf_march = surf_bilinear).
 Pinned by tests/golden/relief_samples.npz, which the reference's own shader
 functions (mechanically translated, oracle/wgsl_ref) wrote.
 """
@@ -73,6 +74,39 @@ class Relief:
         a, b, c, d = self.wet_at(i, j), self.wet_at(i + 1, j), self.wet_at(i, j + 1), self.wet_at(i + 1, j + 1)
         r0, r1 = a * (1 - tx) + b * tx, c * (1 - tx) + d * tx
         return np.where(self.outside(px, py), 0.0, r0 * (1 - ty) + r1 * ty)
+
+    def surf_bilinear(self, px, py):
+        i, j, tx, ty = self._grid(px, py)
+        a, b, c, d = self.surf_at(i, j), self.surf_at(i + 1, j), self.surf_at(i, j + 1), self.surf_at(i + 1, j + 1)
+        r0, r1 = a * (1 - tx) + b * tx, c * (1 - tx) + d * tx
+        return np.where(self.outside(px, py), 0.0, r0 * (1 - ty) + r1 * ty)
+
+    def shadow_at(self, px, py, z0, light, top):
+        """shadow_at with the plain camera: 20 steps of 1.5 cells toward the
+        light over the bilinear relief, stopping where the ray rises above
+        `top` (cam.canvas.w); 1 - the deepest penetration over its penumbra."""
+        lx, ly, lz = (float(v) for v in light)
+        if lz <= f(0.05):
+            return np.ones_like(px)
+        step = self.dx * 1.5
+        spread = np.tan(f(0.12))  # tan(KEY_HALF_ANGLE)
+        sh = np.ones_like(px)
+        live = np.ones(px.shape, bool)
+        for k in range(1, 21):
+            d = float(k) * step
+            zs = self.surf_bilinear(px + lx / lz * d, py + ly / lz * d)
+            zr = z0 + d
+            live &= ~(zr > float(top))
+            pen = d * spread / lz + 0.5 * step
+            sh = np.where(live, np.minimum(sh, 1.0 - np.clip((zs - zr) / pen, 0.0, 1.0)), sh)
+        return sh
+
+    def shadow(self, pts, z0, light, top):
+        """The 2 values per point of cf_relief_shadow: surf_bilinear, shadow_at."""
+        pts = np.asarray(pts, np.float64).reshape(-1, 2)
+        px, py = pts[:, 0], pts[:, 1]
+        return np.column_stack([self.surf_bilinear(px, py),
+                                self.shadow_at(px, py, np.asarray(z0, np.float64), light, top)])
 
     def base_slope(self, px, py):
         e = f(0.7) * self.dx

@@ -35,7 +35,8 @@ def build(ref=None):
     sys.path.insert(0, str(HERE))
     import translate
     src = translate.translate_subset(str(ref), "render.wgsl",
-                                     ["surf_cubic", "base_slope", "color_sharp", "wet_bilinear"],
+                                     ["surf_cubic", "base_slope", "color_sharp", "wet_bilinear", "surf_bilinear",
+                                      "shadow_at"],
                                      {"color_beauty", "color_crisp", "surf_smooth", "hwarp"}, "wgrr")
     (OUT / "render_ref.inc").write_text(src)
     subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "render_driver.cpp"),

@@ -1,6 +1,7 @@
 // render_driver.cpp — evaluates the reference's relief and colour sampling
 // (shaders/render.wgsl: surf_cubic :335-353, base_slope :628-638,
-// color_sharp :706-750, wet_bilinear :394-406), mechanically translated by
+// color_sharp :706-750, wet_bilinear :394-406) and its key-light shadow march
+// (surf_bilinear :314-326, shadow_at :846-866), mechanically translated by
 // translate.py (translate_subset) into render_ref.inc.
 //
 // TEST INFRASTRUCTURE.  Built by build_ref.py into oracle/_ref/ only where the
@@ -48,6 +49,20 @@ void wgrr_sample(const double* pts, uint32_t n, double* out) {
     o[2] = sl.y;
     o[3] = col.x; o[4] = col.y; o[5] = col.z; o[6] = col.w;
     o[7] = wet_bilinear(p);
+  }
+}
+
+// cam.canvas.w: the top of the relief volume the shadow march stops at
+void wgrr_set_top(float top) { wgrr::cam.canvas.w = top; }
+
+// out per point (x, y, z0): surf_bilinear(x, y), shadow_at((x, y), z0, light)
+void wgrr_shadow(const double* pts, uint32_t n, const double* light, double* out) {
+  using namespace wgrr;
+  const vec3<f32> l((f32)light[0], (f32)light[1], (f32)light[2]);
+  for (uint32_t k = 0; k < n; ++k) {
+    const vec2<f32> p((f32)pts[3 * k], (f32)pts[3 * k + 1]);
+    out[2 * k] = surf_bilinear(p);
+    out[2 * k + 1] = shadow_at(p, (f32)pts[3 * k + 2], l);
   }
 }
 

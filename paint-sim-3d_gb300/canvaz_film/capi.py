@@ -201,6 +201,7 @@ def load_library(path=None):
         "cf_upload_deposits": ([vp, vp, u32, C.POINTER(u32), C.POINTER(C.c_double)], i32),
         "cf_lay_deposits": ([vp, vp], i32),
         "cf_sample_relief": ([vp, vp, u32, vp, vp], i32),
+        "cf_relief_shadow": ([vp, vp, u32, C.POINTER(f32), f32, vp, vp], i32),
         "cf_render_relief": ([vp, C.POINTER(ReliefView), vp, vp], i32),
         "cf_batch_create": ([C.POINTER(vp)], i32),
         "cf_batch_destroy": ([vp], i32),

@@ -191,6 +191,12 @@ class Film:
         """cf_sample_relief: 8 floats per canvas point (device pointers)."""
         self._check(self.L.cf_sample_relief(self.p, points_ptr, n, out_ptr, stream), "cf_sample_relief")
 
+    def relief_shadow(self, points_ptr, n, light, top, out_ptr, stream=None):
+        """cf_relief_shadow: per (x, y, z0) point, surf_bilinear and the key
+        light's shadow factor (device pointers)."""
+        lt = (C.c_float * 3)(*light)
+        self._check(self.L.cf_relief_shadow(self.p, points_ptr, n, lt, top, out_ptr, stream), "cf_relief_shadow")
+
     def render_relief(self, out_ptr, x0, y0, pixel_m, width, height, light=(0.3, 0.5, 0.8), ambient=0.35,
                       stream=None):
         """cf_render_relief: a width x height RGBA8 top-down view into out_ptr (device)."""

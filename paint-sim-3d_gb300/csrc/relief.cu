@@ -8,6 +8,9 @@
 //   wet_at, wet_bilinear       render.wgsl:355-361, 394-406
 //   col_at, color_sharp        render.wgsl:644-652, 706-750
 //   base_slope, normal_from_slope  render.wgsl:628-642
+//   surf_bilinear, shadow_at   render.wgsl:314-326, 846-866 (the key light's
+//                              shadow march over the relief; surf_march is
+//                              surf_bilinear with the plain camera)
 //
 // The sampling follows the shader's f32 arithmetic; the view's shading (a
 // key light and an ambient term over the sampled colour and normal) is this
@@ -76,6 +79,36 @@ __device__ float wet_bilinear(const Film& F, const Canvas& cv, float px, float p
   const float a = wet_at(F, i, j), b = wet_at(F, i + 1, j), c = wet_at(F, i, j + 1), d = wet_at(F, i + 1, j + 1);
   const float r0 = a * (1.0f - tx) + b * tx, r1 = c * (1.0f - tx) + d * tx;
   return r0 * (1.0f - ty) + r1 * ty;
+}
+// render.wgsl:314-326, mix(a, b, t) = a (1 - t) + b t
+__device__ float surf_bilinear(const Film& F, const Canvas& cv, float px, float py) {
+  if (outside(cv, px, py)) return 0.f;
+  const float gx = px / cv.dx - 0.5f, gy = py / cv.dx - 0.5f;
+  const float fx = floorf(gx), fy = floorf(gy), tx = gx - fx, ty = gy - fy;
+  const int i = (int)fx, j = (int)fy;
+  const float a = surf_at(F, i, j), b = surf_at(F, i + 1, j), c = surf_at(F, i, j + 1), d = surf_at(F, i + 1, j + 1);
+  const float r0 = a * (1.0f - tx) + b * tx, r1 = c * (1.0f - tx) + d * tx;
+  return r0 * (1.0f - ty) + r1 * ty;
+}
+// render.wgsl:846-866 with the plain camera: 20 steps of 1.5 cells along the
+// light over the bilinear relief from height z0, stopping once the ray is
+// above `top` (cam.canvas.w); each step darkens by how far the relief rises
+// above the ray, over a penumbra that widens with the distance.
+__device__ float shadow_at(const Film& F, const Canvas& cv, float px, float py, float z0, float3 l, float top) {
+  if (l.z <= 0.05f) return 1.0f;
+  const float step = cv.dx * 1.5f;
+  const float spread = tanf(0.12f);  // KEY_HALF_ANGLE
+  const float sx = l.x / l.z, sy = l.y / l.z;
+  float sh = 1.0f;
+  for (int k = 1; k <= 20; ++k) {
+    const float d = (float)k * step;
+    const float zs = surf_bilinear(F, cv, px + sx * d, py + sy * d);
+    const float zr = z0 + d;
+    if (zr > top) break;
+    const float pen = d * spread / l.z + 0.5f * step;
+    sh = fminf(sh, 1.0f - fminf(fmaxf((zs - zr) / pen, 0.f), 1.f));
+  }
+  return sh;
 }
 // render.wgsl:628-638 (plain camera)
 __device__ float2 base_slope(const Film& F, const Canvas& cv, float px, float py) {
@@ -156,6 +189,15 @@ __global__ void __launch_bounds__(256) k_sample_relief(Film F, Canvas cv, const 
   o[7] = wet_bilinear(F, cv, p.x, p.y);
 }
 
+// out per point (x, y, z0): surf_bilinear, shadow_at
+__global__ void __launch_bounds__(256) k_relief_shadow(Film F, Canvas cv, const float3* __restrict__ pts, uint32_t n,
+                                                       float3 l, float top, float2* __restrict__ out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float3 p = pts[k];
+  out[k] = make_float2(surf_bilinear(F, cv, p.x, p.y), shadow_at(F, cv, p.x, p.y, p.z, l, top));
+}
+
 // linear -> sRGB (resolve.wgsl:52-56), then 8 bits
 __device__ __forceinline__ uint32_t srgb8(float c) {
   c = fminf(fmaxf(c, 0.f), 1.f);
@@ -188,6 +230,17 @@ cf_status cf_sample_relief(cf_film* f, const float* points, uint32_t n, float* o
   if (n == 0) return CF_OK;
   k_sample_relief<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(f->F, canvas_of(f), (const float2*)points, n,
                                                                       out);
+  CUDA_TRY(f, cudaGetLastError());
+  return CF_OK;
+}
+
+cf_status cf_relief_shadow(cf_film* f, const float* points, uint32_t n, const float* light, float top, float* out,
+                           void* stream) {
+  if (!f || !light || (n && (!points || !out))) return fail(f, CF_ERR_INVALID_ARG, "cf_relief_shadow");
+  if (n == 0) return CF_OK;
+  const float3 l = make_float3(light[0], light[1], light[2]);
+  k_relief_shadow<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(f->F, canvas_of(f), (const float3*)points, n, l,
+                                                                      top, (float2*)out);
   CUDA_TRY(f, cudaGetLastError());
   return CF_OK;
 }

@@ -1,6 +1,7 @@
 """Generates tests/golden/relief_samples.npz: the reference's relief and
-colour sampling (shaders/render.wgsl, translated by oracle/wgsl_ref and
-evaluated in FP64 by oracle/_ref/librenderref.so) on a small seeded film.
+colour sampling and its key-light shadow march (shaders/render.wgsl,
+translated by oracle/wgsl_ref and evaluated in FP64 by
+oracle/_ref/librenderref.so) on a small seeded film.
 
 Runs where the reference checkout exists (REFERENCE, default /root/reference).
 Usage: python tests/golden/make_relief.py
@@ -57,8 +58,32 @@ def main():
     out = np.zeros((len(pts), 8), np.float64)
     p64 = np.ascontiguousarray(pts.astype(np.float64))
     L.wgrr_sample(p64.ctypes.data_as(C.POINTER(C.c_double)), len(pts), out.ctypes.data_as(C.POINTER(C.c_double)))
+    # the key-light shadow march (shadow_at) from the bilinear surface height
+    # of each point, for a high, a low and a grazing light; the march stops at the top of
+    # the relief volume (cam.canvas.w = max(h + m) + 0.5 mm)
+    L.wgrr_set_top.argtypes = [C.c_float]
+    L.wgrr_shadow.argtypes = [C.POINTER(C.c_double), C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    top = np.float32(float(np.max(hp + mp)) + 0.5e-3)
+    L.wgrr_set_top(top)
+    sp = np.zeros((len(pts), 3), np.float64)
+    sp[:, :2] = pts
+    lights = np.array([[0.6, 0.2, 0.5], [-0.3, -0.7, 0.25], [0.9, 0.3, 0.08]], np.float32)
+    lights = (lights / np.linalg.norm(lights, axis=1, keepdims=True)).astype(np.float32)
+    sh_out = []
+    for li in lights:
+        l64 = np.ascontiguousarray(li.astype(np.float64))
+        o = np.zeros((len(pts), 2), np.float64)
+        L.wgrr_shadow(sp.ctypes.data_as(C.POINTER(C.c_double)), len(pts), l64.ctypes.data_as(C.POINTER(C.c_double)),
+                      o.ctypes.data_as(C.POINTER(C.c_double)))
+        sp[:, 2] = o[:, 0].astype(np.float32)  # z0 = the surface height under the point
+        L.wgrr_shadow(sp.ctypes.data_as(C.POINTER(C.c_double)), len(pts), l64.ctypes.data_as(C.POINTER(C.c_double)),
+                      o.ctypes.data_as(C.POINTER(C.c_double)))
+        sh_out.append(o)
     np.savez_compressed(HERE / "relief_samples.npz", w=w, h=h, width_m=wm, height_m=hm, h_plane=hp, m_plane=mp,
-                        color_f16=col.view(np.uint16), points=pts, out=out)
+                        color_f16=col.view(np.uint16), points=pts, out=out, shadow_z0=sp[:, 2].astype(np.float32),
+                        shadow_top=top, shadow_lights=lights, shadow_out=np.stack(sh_out))
+    print("shadow samples: %d per light, in shadow (< 1): %s" % (
+        len(pts), [int((o[:, 1] < 1).sum()) for o in sh_out]))
     print("relief_samples: %d points, edge-blended colour at %d" % (
         len(pts), int((np.abs(out[:, 3:7]).sum(1) > 0).sum())))
 

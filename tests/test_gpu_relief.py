@@ -1,6 +1,6 @@
 """The render pass's reading of the film on the GPU (cf_sample_relief,
-cf_render_relief) against the reference's render.wgsl functions
-(tests/golden/relief_samples.npz, FP64)."""
+cf_relief_shadow, cf_render_relief) against the reference's render.wgsl
+functions (tests/golden/relief_samples.npz, FP64)."""
 from pathlib import Path
 
 import numpy as np
@@ -86,3 +86,32 @@ def test_errors(built):
     v = capi.ReliefView(x0=0, y0=0, pixel_m=0.0, width=4, height=4, ambient=0.3)
     import ctypes as C
     assert L.cf_render_relief(f.p, C.byref(v), C.c_void_p(16), None) == capi.CF_ERR_INVALID_ARG
+
+
+def test_shadow_march_matches_the_reference(built):
+    """cf_relief_shadow against the reference's shadow_at (FP64), for a high,
+    a low and a grazing light; and no shadow for a light at or below the
+    shader's 0.05 cut."""
+    import torch
+    d, f = fixture_film()
+    n = len(d["points"])
+    p3 = np.zeros((n, 3), np.float32)
+    p3[:, :2] = d["points"]
+    p3[:, 2] = d["shadow_z0"]
+    pts = torch.from_numpy(p3).cuda()
+    out = torch.empty((n, 2), dtype=torch.float32, device="cuda")
+    top = float(d["shadow_top"])
+    for li, want in zip(d["shadow_lights"], d["shadow_out"]):
+        f.relief_shadow(pts.data_ptr(), n, [float(v) for v in li], top, out.data_ptr())
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().astype(np.float64)
+        # f32 against FP64: the height to 1e-5 of its range; the shadow factor
+        # (a min of clamped ratios) to 1e-4, a floor() at a sample's cell
+        # boundary may move a few points further
+        assert np.abs(got[:, 0] - want[:, 0]).max() <= 1e-5 * np.abs(want[:, 0]).max()
+        err = np.abs(got[:, 1] - want[:, 1])
+        assert (err > 1e-4).mean() <= 1e-3, err.max()
+        assert ((got[:, 1] < 1) == (want[:, 1] < 1)).mean() >= 0.999
+    f.relief_shadow(pts.data_ptr(), n, [0.99, 0.0, 0.05], top, out.data_ptr())
+    torch.cuda.synchronize()
+    assert (out[:, 1] == 1).all()

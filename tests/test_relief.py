@@ -1,6 +1,7 @@
-"""The relief / colour sampling restatement (oracle/relief_ref.py) against
-the reference's own render.wgsl functions (tests/golden/relief_samples.npz,
-written by their mechanical translation in FP64)."""
+"""The relief / colour sampling and shadow-march restatement
+(oracle/relief_ref.py) against the reference's own render.wgsl functions
+(tests/golden/relief_samples.npz, written by their mechanical translation in
+FP64)."""
 from pathlib import Path
 
 import numpy as np
@@ -37,3 +38,18 @@ def test_fixture_covers_the_edge_blend_and_the_outside():
     assert sharpened.sum() > 200
     assert R.outside(px, py).sum() > 50
     assert (d["out"][R.outside(px, py), 0] == 0).all()  # no relief outside the canvas
+
+
+def test_shadow_restatement_equals_the_reference_march():
+    d, R = load()
+    for li, want in zip(d["shadow_lights"], d["shadow_out"]):
+        got = R.shadow(d["points"], d["shadow_z0"], li, d["shadow_top"])
+        assert np.abs(got[:, 0] - want[:, 0]).max() <= 1e-12 * max(np.abs(want[:, 0]).max(), 1e-30)
+        assert np.abs(got[:, 1] - want[:, 1]).max() <= 1e-12
+
+
+def test_shadow_fixture_has_shadowed_points():
+    d, _ = load()
+    shadowed = [(o[:, 1] < 1).sum() for o in d["shadow_out"]]
+    assert sum(shadowed) > 50 and max(shadowed) > 40
+    assert (d["shadow_out"][:, :, 1] >= 0).all() and (d["shadow_out"][:, :, 1] <= 1).all()
