@@ -773,10 +773,12 @@ struct FastShade {
 // strata_limit alpha (strata.wgsl:157-173; 1 without fluxes).  Every other
 // cell takes the fast path of strata_update (strata.wgsl:212-237): the stack
 // renormalised to h into the next generation of thicknesses, its pigments left
-// in place (this path never changes them), then the shade (shade.wgsl:28-84)
-// and the composition aggregates.  Inactive tiles carry their strata over and
-// are shaded, as the reference's full-grid shade does.  Active wet cells left
-// without strata become strata_fill candidates.
+// in place (this path never changes them).  Inactive tiles carry their strata
+// over and are shaded, as the reference's full-grid shade does.  Active wet
+// cells left without strata become strata_fill candidates.  Returns whether
+// the cell needs the shade (shade.wgsl:28-84) and composition aggregates,
+// whose inputs it leaves in the block's FastShade slot (the tile function
+// shades it by lane or by half-warp).
 template <int MODE>
 __device__ __forceinline__ bool strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
                                                  uint32_t c, float hc, FastShade& sh, int tid) {
