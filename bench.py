@@ -1,13 +1,15 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 thin-film step (one JSON line on rank 0).
 
-Workload (default): a 2048 x 2048 FP32 canvas (1 mm cells) tilted 60 deg with
-gravity along +y, seeded with 200 random drip polylines (width 2-8 cells,
-height 0.2-3 mm, per-line Herschel-Bulkley rheology and Dirichlet(0.5)
-pigments), stepped with adaptive-CFL steps.  One step = the device-side dt
-choice + one frame of film + strata/pigment transport + cure + KM shade
-(cf_step_adaptive), every 16x16 tile active.  The canvas state (~3.4 GB)
-is far larger than L2, so no flush is needed between steps.
+Workload (default): a 4096 x 4096 FP32 canvas (1 mm cells) seeded with 500
+Gaussian paint blobs (sigma 5-40 cells, peak 0.1-2 mm, per-blob
+Herschel-Bulkley rheology and Dirichlet(0.5) pigments) over a 0.05 mm cured
+ground layer, stepped at a fixed dt of 1e-3 s (one substep per frame).  One
+step = one frame of film + strata/pigment transport + cure + KM shade
+(cf_encode_frame), every 16x16 tile active.  The state (13.7 GB) is far larger
+than L2, so no flush is needed between steps.  The same canvas with BF16
+pigment and rheology storage is timed too and reported inside the line
+("bf16").
 
 Arms:
   --impl gb300 (default): the CUDA library through its C ABI.  `value` is
@@ -56,7 +58,9 @@ WORKLOADS = {
     "pour2048_implicit_fp32": (lambda seed: synth.config(5, seed), capi.CF_PREC_FP32, 1.0 / 60.0, True),
     "pour512_implicit_fp32": (lambda seed: synth.config(5, seed, scale=4), capi.CF_PREC_FP32, 1.0 / 60.0, True),
 }
-DEFAULT_WORKLOAD = "drips2048_tilt60_fp32"
+DEFAULT_WORKLOAD = "blobs4096_dt1e-3_fp32"
+# the storage variant timed beside a single-canvas workload in the same run
+BF16_TWIN = {"blobs4096_dt1e-3_fp32": "blobs4096_dt1e-3_bf16"}
 
 # Compulsory persistent-state bytes per cell-step (read once + write once):
 # h 4R+4W, m 4R, rheo 3 fields R+W, delta 4R+4W, strata_h 16R+16W,
@@ -84,7 +88,7 @@ DEPOSIT_BYTES_PER_CELL = (4 + 4 + 16 + 16 + 256 + 32) + (4 + 16 + 16 + 256 + 4 +
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
@@ -111,26 +115,91 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def step_traffic():
-    """dram bytes per cell-step from the committed ncu summary (or None)."""
+def step_traffic(workload):
+    """DRAM bytes per cell-step of `workload` from the committed ncu summary
+    (a line `dram_bytes_per_cell_step[<workload>]=<bytes>`), or None."""
     p = ROOT / "profiles" / "step_traffic.txt"
     if not p.exists():
         return None
+    key = "dram_bytes_per_cell_step[%s]=" % workload
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_cell_step="):
+        if line.startswith(key):
             return float(line.split("=", 1)[1].split()[0])
     return None
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml):
+    SM clock, its maximum, power and the active clock-event reasons."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, cuda_index):
+        import ctypes as C
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        bus = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(cuda_index)
+            bus = ("%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)).encode()
+        except Exception:
+            bus = None
+        ok = bus is not None and self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus, C.byref(self.h)) == 0
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(cuda_index), C.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn if fn is not None else self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        C = self.C
+        sm, mx, pw, rs = C.c_uint(), C.c_uint(), C.c_uint(), C.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(sm))
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx))
+        self.lib.nvmlDeviceGetPowerUsage(self.h, C.byref(pw))
+        self.reasons_fn(self.h, C.byref(rs))
+        return float(sm.value), float(mx.value), pw.value / 1000.0, int(rs.value)
+
+
 class Clocks:
-    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+    """Samples SM clocks and throttle reasons during a region: NVML every
+    5 ms from a thread (read-only queries) where the driver library loads,
+    else nvidia-smi every 200 ms.  mark(True) / mark(False) bracket the timed
+    region; the summary keeps the samples inside it."""
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.file = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
+        self.nvml = None
+        self.rows = []  # (t, sm, max, power_w, reasons set)
+        self.t0 = self.t1 = None
+        self.file = None
+        try:
+            self.nvml = _Nvml(gpu_index)
+        except Exception:
+            self.nvml = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                sm, mx, pw, rs = self.nvml.sample()
+                self.rows.append((time.perf_counter(), sm, mx, pw,
+                                  {n for b, n in _Nvml.REASONS.items() if rs & b}))
+            except Exception:
+                pass
+            self._stop.wait(0.005)
 
     def __enter__(self):
+        if self.nvml is not None:
+            self._stop = threading.Event()
+            self._th = threading.Thread(target=self._run, daemon=True)
+            self._th.start()
+            time.sleep(0.05)
+            return self
+        self.file = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -143,7 +212,17 @@ class Clocks:
         time.sleep(0.3)
         return self
 
+    def mark(self, start):
+        if start:
+            self.t0 = time.perf_counter()
+        else:
+            self.t1 = time.perf_counter()
+
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self._stop.set()
+            self._th.join(2)
+            return
         if self.proc:
             self.proc.terminate()
             try:
@@ -152,7 +231,23 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            rows = self.rows
+            if self.t0 is not None and self.t1 is not None:
+                inside = [r for r in rows if self.t0 <= r[0] <= self.t1]
+                rows = inside if inside else rows
+            if not rows:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+            reasons = set()
+            for r in rows:
+                reasons |= r[4]
+            return {"sm_mhz": statistics.median(r[1] for r in rows), "sm_max_mhz": rows[0][2],
+                    "reasons": sorted(reasons), "samples": len(rows), "source": "nvml 5 ms",
+                    "power_w_median": statistics.median(r[3] for r in rows),
+                    "timed_region_s": None if self.t0 is None or self.t1 is None else self.t1 - self.t0}
         rows = []
+        if self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         try:
             for line in Path(self.file.name).read_text().splitlines():
                 f = [x.strip() for x in line.split(",")]
@@ -170,7 +265,7 @@ class Clocks:
                 if r[5 + k].lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(rows[0][2]) if rows else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+                "reasons": sorted(reasons), "samples": len(rows), "source": "nvidia-smi 200 ms"}
 
 
 def settings_for(cv):
@@ -518,7 +613,7 @@ def deposit_arm(args):
 
 
 def reference_arm(args):
-    """CPU reference path, same workload / metric / unit; rank 0 only."""
+    """CPU reference path, same workload / metric / unit / config; rank 0 only."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -542,18 +637,148 @@ def reference_arm(args):
                           "e2e": {"value": cb["value"], "unit": "Mdeposits/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return
-    workload = args.workload if args.workload in WORKLOADS else "blobs512_dt1e-3_fp32"  # batch / served: same physics
-    gen, prec, dt_max, adaptive = WORKLOADS[workload]
+    if args.workload == BATCH_WORKLOAD:
+        reference_batch(args)
+        return
+    if args.workload == SERVE_WORKLOAD:
+        reference_serve(args)
+        return
+    gen, prec, dt_max, adaptive = WORKLOADS[args.workload]
     cv = gen(0)
     per_step_budget = 150.0 / max(args.steps + args.warmup, 1)
-    cb = cpu_baseline(cv, workload, per_step_budget * (args.steps + args.warmup), steps_hint=args.steps + args.warmup)
+    cb = cpu_baseline(cv, args.workload, per_step_budget * (args.steps + args.warmup), steps_hint=args.steps + args.warmup)
     line = {"impl": "reference", "metric": "Gcell-updates/s", "value": cb["value"], "unit": "Gcell-updates/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": PREC_NAME[prec], "data": "synthetic",
-            "config": {"workload": args.workload, "cells": cv.w * cv.h, "all_tiles_active": True},
+            "scaling": "weak", "vs_baseline": None, "dtype": PREC_NAME[prec],
+            "data": "synthetic (seeded drip polylines / Gaussian blobs; no public dataset)",
+            "config": single_config(args.workload, cv, prec, adaptive, dt_max, world),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def cpu_step_canvases(canvases, prec, dt, budget_s):
+    """The oracle's FP32 restatement stepping each canvas one fixed-dt frame
+    in turn (all host cores), round after round while the budget lasts (at
+    least one round).  One canvas's oracle is held at a time (set up outside
+    the timing), so host memory stays at one canvas's worth.  Returns
+    (cell-updates, timed seconds, rounds)."""
+    import pyoracle as po
+    po.build()
+    pig = capi.PREC_TO_PIG[prec]
+    el, cells, rounds = 0.0, 0, 0
+    while rounds == 0 or el < budget_s:
+        for cv in canvases:
+            o = po.Oracle(cv.w, cv.h, settings_for(cv), pig, 32)
+            o.set_tables(cv.pigtab, cv.cmf)
+            o.write_state(cv.planes)
+            o.update_params(dt, 1)
+            t0 = time.perf_counter()
+            o.encode_frame(1)
+            el += time.perf_counter() - t0
+            cells += cv.w * cv.h
+            del o
+        rounds += 1
+    return cells, el, rounds
+
+
+def reference_batch(args):
+    """Config 3 on the host cores: the same 64 canvases as the GPU arm (rank 0's
+    seed), each stepped one frame after the other, rounds while the budget lasts."""
+    canv = list(batch64_canvases(seed=0))
+    cells, el, rounds = cpu_step_canvases(canv, capi.CF_PREC_FP32, 1e-3, min(150.0, 5.0 * (args.steps + args.warmup)))
+    v = cells / el / 1e9
+    cb = {"value": v, "unit": "Gcell-updates/s", "cores": os.cpu_count(), "kind": "port",
+          "sample": "%d round(s) of one frame of each of the %d batch canvases (%d cells a round), FP32 oracle "
+                    "restatement, OpenMP %d threads, %.1f s" % (rounds, len(canv), cells // rounds, os.cpu_count(), el)}
+    print(json.dumps({"impl": "reference", "metric": "Gcell-updates/s", "value": v, "unit": "Gcell-updates/s",
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                      "data": "synthetic (seeded Gaussian blob fields; no public dataset)",
+                      "config": batch_config(canv), "cpu_baseline": cb,
+                      "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def reference_serve(args):
+    """Config 4 on the host cores: the served stream's template canvases (every
+    side, FP32 and BF16 storage) stepped one frame each, one job at a time,
+    rounds while the budget lasts."""
+    from canvaz_film import serve
+    pool = serve.TemplatePool(SERVE_SIDES, seed=0)
+    budget = min(150.0, 5.0 * (args.steps + args.warmup))
+    c32, e32, r32 = cpu_step_canvases(pool.canvases, capi.CF_PREC_FP32, serve.DT, budget / 2)
+    c16, e16, r16 = cpu_step_canvases(pool.canvases, capi.CF_PREC_BF16, serve.DT, budget / 2)
+    v = (c32 + c16) / (e32 + e16) / 1e9
+    cb = {"value": v, "unit": "Gcell-updates/s", "cores": os.cpu_count(), "kind": "port",
+          "sample": "one frame of each served template canvas (sides %s), %d FP32 and %d BF16 round(s), FP32 oracle "
+                    "restatement, OpenMP %d threads, %.1f s" % (SERVE_SIDES, r32, r16, os.cpu_count(), e32 + e16)}
+    print(json.dumps({"impl": "reference", "metric": "served Gcell-updates/s", "value": v,
+                      "unit": "Gcell-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "f32+f32pig|f32+bf16pig", "data": "synthetic (seeded Gaussian blob fields)",
+                      "config": serve_config(args), "cpu_baseline": cb,
+                      "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def single_config(workload, cv, prec, adaptive, dt_max, world):
+    """The `config` of a single-canvas line: the GPU arm and the reference arm
+    build it with this one function, so both carry the same keys and values."""
+    cells = cv.w * cv.h
+    try:
+        l2 = "working set %.1f GB > L2 (129 MB): no flush needed" % (film_bytes(cells, prec) / 1e9)
+    except Exception:  # the library is not built (reference arm on a host without it)
+        l2 = "working set > L2 (129 MB): no flush needed"
+    return {"workload": workload, "w": cv.w, "h": cv.h, "cells_per_gpu": cells, "precision": PREC_NAME[prec],
+            "adaptive_dt": adaptive, "dt_max": dt_max, "all_tiles_active": True,
+            "parallelism": "replicas" if world > 1 else "single", "seed": "rank", "l2": l2}
+
+
+def timed_film(workload, rank, steps, warmup, stream, clk=None):
+    """A film of `workload` (seeded by rank) with its state resident, `warmup`
+    untimed steps, then `steps` steps timed with CUDA events on `stream`."""
+    import torch
+    from canvaz_film.film import Film
+    gen, prec, dt_max, adaptive = WORKLOADS[workload]
+    cv = gen(rank)  # one replica canvas per rank, own seed
+    st = settings_for(cv)
+    film = Film(st, cv.w, cv.h, prec)
+    film.set_tables(cv.pigtab, cv.cmf)
+    film.write_state(cv.planes)
+    s0 = film.stats()
+    sh = stream.cuda_stream
+
+    def step():
+        if adaptive:
+            film.step_adaptive(dt_max, sh)
+        else:
+            film.encode_frame(1, sh)
+
+    if not adaptive:
+        film.update_params(dt_max, 1)
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = film.stats()["launches"]
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if clk is not None:
+        clk.mark(True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if clk is not None:
+        clk.mark(False)
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        torch.distributed.barrier()
+    t = e0.elapsed_time(e1) / 1e3
+    s1 = film.stats()
+    return film, cv, st, t, s1["launches"] - l0, s0, s1
 
 
 def gpu_arm(args):
@@ -568,57 +793,25 @@ def gpu_arm(args):
         import __graft_entry__ as g
         g.build()
     gen, prec, dt_max, adaptive = WORKLOADS[args.workload]
-    cv = gen(rank)  # one replica canvas per rank, own seed
-    st = settings_for(cv)
-    film = Film(st, cv.w, cv.h, prec)
-    film.set_tables(cv.pigtab, cv.cmf)
-    film.write_state(cv.planes)
-    s0 = film.stats()
     stream = torch.cuda.Stream()
-    sh = stream.cuda_stream
-
-    def step():
-        if adaptive:
-            film.step_adaptive(dt_max, sh)
-        else:
-            film.encode_frame(1, sh)
-
-    if not adaptive:
-        film.update_params(dt_max, 1)
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    l0 = film.stats()["launches"]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    t = e0.elapsed_time(e1) / 1e3
+        film, cv, st, t, launches, s0, s1 = timed_film(args.workload, rank, args.steps, args.warmup, stream, clk)
     if world > 1:
         tt = torch.tensor([t], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t = float(tt.item())
-    s1 = film.stats()
-    launches = s1["launches"] - l0
     cells = cv.w * cv.h
     value = world * cells * args.steps / t / 1e9
     alg = ALG_BYTES_PER_CELL[prec]
     peak, peak_kind = peaks()
     achieved = alg * cells * args.steps / t / 1e9
-    traffic_pc = step_traffic()
+    traffic_pc = step_traffic(args.workload)
     mass0 = s0["wet_volume"] + s0["relief_volume"]
     mass1 = s1["wet_volume"] + s1["relief_volume"]
 
     # end to end through the C ABI with host buffers (pinned)
     e2e = None
+    film_b = pair = outs = None
     if args.e2e_steps > 0:
         # the state in the reference's own layout (write_state's planes: f16
         # pigment slots, or BF16 where the film stores BF16)
@@ -694,6 +887,29 @@ def gpu_arm(args):
                        "+ cf_read_color_async; two films alternate on two streams, uploads one after the "
                        "other on the host link while the other film steps; wall time over the steps"}
 
+    # the same canvas with BF16 pigment / rheology storage, timed the same way
+    bf16 = None
+    twin = BF16_TWIN.get(args.workload)
+    if twin is not None:
+        torch.cuda.synchronize()
+        if film_b is not None:
+            film_b.close()
+        pair = outs = film_b = None
+        film.close()
+        film = None
+        fb, cvb, _, tb, lb, _, _ = timed_film(twin, rank, args.steps, args.warmup, stream)
+        if world > 1:
+            tt = torch.tensor([tb], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            tb = float(tt.item())
+        pb = WORKLOADS[twin][1]
+        ab = ALG_BYTES_PER_CELL[pb] * cells * args.steps / tb / 1e9
+        bf16 = {"workload": twin, "value": world * cells * args.steps / tb / 1e9, "unit": "Gcell-updates/s",
+                "ms_per_step": 1e3 * tb / args.steps, "dtype": PREC_NAME[pb], "gpu_launches": int(lb),
+                "roofline": {"bound": "hbm", "achieved": ab, "peak": peak, "unit": "GB/s", "frac": ab / peak,
+                             "peak_source": peak_kind, "alg_bytes_per_cell": ALG_BYTES_PER_CELL[pb],
+                             "scope": "whole step (all kernels of cf_encode_frame)"}}
+        fb.close()
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(cv, args.workload, args.cpu_seconds)
@@ -704,13 +920,12 @@ def gpu_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": PREC_NAME[prec],
             "data": "synthetic (seeded drip polylines / Gaussian blobs; no public dataset)",
-            "config": {"workload": args.workload, "w": cv.w, "h": cv.h, "cells_per_gpu": cells,
-                       "precision": PREC_NAME[prec], "adaptive_dt": adaptive, "dt_max": dt_max,
-                       "all_tiles_active": True, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "working set %.1f GB > L2 (129 MB): no flush needed" % (film_bytes(cells, prec) / 1e9)},
+            "config": single_config(args.workload, cv, prec, adaptive, dt_max, world),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
-                         "alg_bytes_per_cell": alg, "scope": "whole step (all kernels of cf_step_adaptive)",
+                         "alg_bytes_per_cell": alg,
+                         "scope": "whole step (all kernels of %s)" % ("cf_step_adaptive" if adaptive
+                                                                      else "cf_encode_frame"),
                          "traffic": None if traffic_pc is None else traffic_pc * cells},
             "gpu_launches": int(launches),
             "clocks": clocks,
@@ -718,6 +933,7 @@ def gpu_arm(args):
             "cpu_baseline": cb,
             "mass_drift_rel": abs(mass1 - mass0) / max(mass0, 1e-300),
             "last_dt": s1["last_dt"],
+            "bf16": bf16,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -739,6 +955,16 @@ def batch64_canvases(count=64, seed=0):
         yield synth.blob_canvas(side, side, 1000 + k, n_blobs=int(rng.integers(10, 201)))
 
 
+def batch_config(canvases):
+    """`config` of the batch workload (the GPU and reference arms share it)."""
+    sides = [cv.w for cv in canvases]
+    return {"workload": BATCH_WORKLOAD, "canvases": len(canvases), "cells": sum(cv.w * cv.h for cv in canvases),
+            "side_min": min(sides), "side_max": max(sides), "dt": 1e-3, "substeps": 1, "precision": "f32",
+            "all_tiles_active": True,
+            "l2": "working set > L2 (129 MB, %d canvases of %d-%d cells a side): no flush needed"
+                  % (len(sides), min(sides), max(sides))}
+
+
 def batch_arm(args):
     """Config 3: the batch (one launch per dispatch over all canvases' tiles,
     graph replay, autotuned) against the same canvases stepped one after the
@@ -751,7 +977,8 @@ def batch_arm(args):
         import __graft_entry__ as g
         g.build()
     films, cells, sides = [], 0, []
-    for cv in batch64_canvases(seed=rank):
+    canvases = list(batch64_canvases(seed=rank))
+    for cv in canvases:
         f = Film(settings_for(cv), cv.w, cv.h, capi.CF_PREC_FP32)
         f.set_tables(cv.pigtab, cv.cmf)
         f.write_state(cv.planes)
@@ -770,10 +997,12 @@ def batch_arm(args):
     l0 = b.info()["launches"]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
+        clk.mark(True)
         e0.record(stream)
         b.step(args.steps, 1, 0.0, sh)
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.mark(False)
     tb = e0.elapsed_time(e1) / 1e3
     launches = b.info()["launches"] - l0
     b.close()
@@ -800,11 +1029,8 @@ def batch_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tb / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian blob fields; no public dataset)",
-            "config": {"workload": BATCH_WORKLOAD, "canvases": len(films), "cells": cells,
-                       "side_min": min(sides), "side_max": max(sides), "dt": 1e-3, "substeps": 1,
-                       "all_tiles_active": True, "tuning": tuning, "autotune_ms_per_frame": tune_ms,
-                       "l2": "working set %.1f GB > L2 (129 MB): no flush needed"
-                             % (sum(capi.film_bytes(x, x, capi.CF_PREC_FP32) for x in sides) / 1e9)},
+            "config": batch_config(canvases),
+            "tuning": tuning, "autotune_ms_per_frame": tune_ms,
             "sequential": {"value": seq, "unit": "Gcell-updates/s", "steps": seq_steps,
                            "form": "64 films one after another per step, single-film launches"},
             "speedup_vs_sequential": value / seq,
@@ -818,6 +1044,17 @@ def batch_arm(args):
         f.close()
 
 
+SERVE_SIDES = [256, 368, 528, 768, 1104, 1584, 2048]
+
+
+def serve_config(args):
+    """`config` of the served workload (the GPU and reference arms share it)."""
+    return {"workload": SERVE_WORKLOAD, "arrival_rate_per_s": 20.0, "window_s": args.serve_seconds,
+            "wall_cutoff_s": args.serve_wall,
+            "steps_range": [max(1, round(100 * args.serve_steps_scale)), round(3000 * args.serve_steps_scale)],
+            "sides": SERVE_SIDES, "budget_bytes": 150e9, "dt": 1e-3}
+
+
 def serve_arm(args):
     """Config 4: Poisson arrivals at 20/s, side log-spaced 256-2048, steps
     uniform 100-3000 (scaled), FP32 / BF16 pigments 50/50, 150 GB budget."""
@@ -826,7 +1063,7 @@ def serve_arm(args):
     if not capi.LIB_PATH.exists():
         import __graft_entry__ as g
         g.build()
-    pool = serve.TemplatePool([256, 368, 528, 768, 1104, 1584, 2048], seed=rank)
+    pool = serve.TemplatePool(SERVE_SIDES, seed=rank)
     jobs = serve.poisson_jobs(args.serve_seconds, 20.0, pool, steps_scale=args.serve_steps_scale, seed=1 + rank)
     for s_ in pool.sides:  # templates resident before the clock starts
         for p_ in (capi.CF_PREC_FP32, capi.CF_PREC_BF16):
@@ -842,10 +1079,7 @@ def serve_arm(args):
             "metric": "served Gcell-updates/s", "value": rep["gcell_updates_per_s"], "unit": "Gcell-updates/s",
             "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f32pig|f32+bf16pig", "data": "synthetic (seeded Gaussian blob fields)",
-            "config": {"workload": SERVE_WORKLOAD, "arrival_rate_per_s": 20.0, "window_s": args.serve_seconds,
-                       "wall_cutoff_s": args.serve_wall,
-                       "steps_range": [max(1, round(100 * args.serve_steps_scale)), round(3000 * args.serve_steps_scale)],
-                       "sides": pool.sides, "budget_bytes": 150e9, "dt": 1e-3},
+            "config": serve_config(args),
             "step_ms_p50": rep["step_ms_p50"], "step_ms_p99": rep["step_ms_p99"],
             "queue_wait_s_p50": rep["queue_wait_s_p50"], "queue_wait_s_p99": rep["queue_wait_s_p99"],
             "jobs": {"arrived": rep["jobs_arrived"], "done": rep["jobs_done"], "peak_resident": rep["peak_resident_jobs"]},

@@ -454,12 +454,15 @@ const char* cf_batch_last_error(const cf_batch* batch);
  * h > 4 h_min; mu_min = 1 when no cell qualifies) and writes them to
  * d_out[0], d_out[1] (device memory) on `stream` (NULL = legacy default).
  * It allocates nothing: its scratch is a fixed array in the library's device
- * image.  The first call on each device looks up that array's address with
- * the device current; make that first call before any stream capture.
- * Every call on a device shares the one array, so calls that overlap on the
- * GPU (different streams or host threads, without ordering) race.
- * Grids of more than CF_NOALLOC_MAX_TILES tiles return CF_ERR_INVALID_ARG
- * before anything is launched. */
+ * image.  The first call on each device (and again the first call after the
+ * device's context was destroyed and created anew, e.g. by cudaDeviceReset)
+ * looks up that array's address with the device current; make that first
+ * call before any stream capture.  Every call on a device shares the one
+ * array, and every call writes all the partials it reads, so nothing is
+ * cleared between calls; calls that overlap on the GPU (different streams or
+ * host threads, without ordering) race.  Grids of more than
+ * CF_NOALLOC_MAX_TILES tiles, of any shape (one tile wide and 65,536 tall is
+ * accepted), return CF_ERR_INVALID_ARG before anything is launched. */
 cf_status cf_cfl_stats_noalloc(const float* d_h, const float* d_mu, uint32_t w, uint32_t h,
                                float h_min, float* d_out, void* stream);
 

@@ -1,7 +1,9 @@
 """Builds oracle/_ref/libwgslref.so from the reference shaders.
 
-TEST INFRASTRUCTURE.  Needs the reference checkout (argument or REFERENCE env
-var, default /root/reference); does nothing when it is absent.  Steps:
+TEST INFRASTRUCTURE.  Needs the reference checkout (argument, else the
+REFERENCE env var, else the checkout's mount point in the build container:
+reference_root() below is the one place that names it); does nothing when it
+is absent.  Steps:
 translate.py writes oracle/_ref/ref_shaders.inc (FP64), then g++ compiles
 driver.cpp against it; the relief and colour sampling of render.wgsl goes the
 same way into render_ref.inc and librenderref.so (render_driver.cpp).  Everything it writes stays in oracle/_ref/, which is
@@ -18,8 +20,17 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
 
 
+# where the build container mounts the reference checkout (read-only)
+_MOUNT = "/root/reference"
+
+
+def reference_root(ref=None):
+    """The reference checkout: `ref`, else $REFERENCE, else the mount point."""
+    return Path(ref or os.environ.get("REFERENCE") or _MOUNT)
+
+
 def build(ref=None):
-    ref = Path(ref or os.environ.get("REFERENCE", "/root/reference"))
+    ref = reference_root(ref)
     if not (ref / "shaders" / "film.wgsl").exists():
         print("reference shaders not found at %s; skipping" % ref)
         return None

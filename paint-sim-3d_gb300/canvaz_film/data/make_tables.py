@@ -74,7 +74,10 @@ def pigment_table(ref):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE", "/root/reference"))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE")
+    if not root:
+        sys.exit("usage: make_tables.py REFERENCE_ROOT (or set REFERENCE)")
+    ref = Path(root)
     cmf = cmf_table(ref)
     pig, names = pigment_table(ref)
     out = Path(__file__).with_name("reference_tables.npz")

@@ -221,12 +221,19 @@ __global__ void __launch_bounds__(256) k_render_relief(Film F, Canvas cv, cf_rel
 
 Canvas canvas_of(const cf_film* f) { return Canvas{f->S.width_m, f->S.height_m, f->S.width_m / (float)f->w}; }
 
+// The kernels read points and write results as float2 / float3 / uint32
+// vectors: a buffer that is valid byte by byte but not aligned to them is
+// refused here rather than faulting on the device.
+bool aligned(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
 }  // namespace
 
 extern "C" {
 
 cf_status cf_sample_relief(cf_film* f, const float* points, uint32_t n, float* out, void* stream) {
   if (!f || (n && (!points || !out))) return fail(f, CF_ERR_INVALID_ARG, "cf_sample_relief");
+  if (n && (!aligned(points, 8) || !aligned(out, 4)))
+    return fail(f, CF_ERR_INVALID_ARG, "cf_sample_relief: points must be 8-byte and out 4-byte aligned");
   if (n == 0) return CF_OK;
   k_sample_relief<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(f->F, canvas_of(f), (const float2*)points, n,
                                                                       out);
@@ -237,6 +244,8 @@ cf_status cf_sample_relief(cf_film* f, const float* points, uint32_t n, float* o
 cf_status cf_relief_shadow(cf_film* f, const float* points, uint32_t n, const float* light, float top, float* out,
                            void* stream) {
   if (!f || !light || (n && (!points || !out))) return fail(f, CF_ERR_INVALID_ARG, "cf_relief_shadow");
+  if (n && (!aligned(points, 4) || !aligned(out, 8)))
+    return fail(f, CF_ERR_INVALID_ARG, "cf_relief_shadow: points must be 4-byte and out 8-byte aligned");
   if (n == 0) return CF_OK;
   const float3 l = make_float3(light[0], light[1], light[2]);
   k_relief_shadow<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(f->F, canvas_of(f), (const float3*)points, n, l,
@@ -248,6 +257,7 @@ cf_status cf_relief_shadow(cf_film* f, const float* points, uint32_t n, const fl
 cf_status cf_render_relief(cf_film* f, const cf_relief_view* v, uint8_t* rgba8, void* stream) {
   if (!f || !v || !rgba8 || v->width == 0 || v->height == 0 || !(v->pixel_m > 0.f))
     return fail(f, CF_ERR_INVALID_ARG, "cf_render_relief");
+  if (!aligned(rgba8, 4)) return fail(f, CF_ERR_INVALID_ARG, "cf_render_relief: rgba8 must be 4-byte aligned");
   float lx = v->light[0], ly = v->light[1], lz = v->light[2];
   const float ll = std::sqrt(lx * lx + ly * ly + lz * lz);
   if (!(ll > 0.f)) return fail(f, CF_ERR_INVALID_ARG, "cf_render_relief: light");

@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <thread>
+#include <new>
 #include <vector>
 
 #include "film_handle.h"
@@ -210,12 +211,17 @@ bool unpack_parts(const uint8_t* data, size_t n, std::vector<std::vector<uint8_t
     std::memcpy(&len, p, 8);
     if (!take(4, p)) return false;
     nchunks = read32(p);
+    // every chunk takes at least its 8-byte length and a 4-byte raw size, and
+    // holds at most CHUNK raw bytes: sizes the file cannot back are rejected
+    // before anything is allocated for them
+    if (nchunks > (n - off) / 12 || len > (uint64_t)nchunks * CHUNK) return false;
     std::vector<const uint8_t*> cp(nchunks);
     std::vector<uint64_t> cl(nchunks);
     for (uint32_t k = 0; k < nchunks; ++k) {
       if (!take(8, p)) return false;
       std::memcpy(&cl[k], p, 8);
       if (!take(cl[k], cp[k]) || cl[k] < 4) return false;
+      if (read32(cp[k]) > CHUNK) return false;
     }
     std::vector<std::vector<uint8_t>> dec(nchunks);
     bool ok = true;
@@ -261,7 +267,11 @@ cf_status cf_lz4_decompress(const uint8_t* src, uint64_t n, uint8_t* dst, uint64
   return CF_OK;
 }
 
-cf_status cf_snapshot_save(cf_film* f, const cf_snapshot_info* info, uint8_t** out, uint64_t* out_len) {
+}  // extern "C"
+
+namespace {
+
+cf_status snapshot_save(cf_film* f, const cf_snapshot_info* info, uint8_t** out, uint64_t* out_len) {
   if (!f || !info || !out || !out_len) return fail(f, CF_ERR_INVALID_ARG, "cf_snapshot_save: null");
   size_t sz[8];
   part_sizes(f->n, sz);
@@ -303,12 +313,7 @@ cf_status cf_snapshot_save(cf_film* f, const cf_snapshot_info* info, uint8_t** o
   return CF_OK;
 }
 
-cf_status cf_snapshot_free(uint8_t* buf) {
-  std::free(buf);
-  return CF_OK;
-}
-
-cf_status cf_snapshot_load(cf_film* f, const uint8_t* data, uint64_t len, cf_snapshot_info* info) {
+cf_status snapshot_load(cf_film* f, const uint8_t* data, uint64_t len, cf_snapshot_info* info) {
   if (!f || !data) return fail(f, CF_ERR_INVALID_ARG, "cf_snapshot_load: null");
   if (len < HEADER || std::memcmp(data, "PSIM", 4) != 0) return fail(f, CF_ERR_INVALID_ARG, "not a painting file");
   if (read32(data + 4) != VERSION) return fail(f, CF_ERR_INVALID_ARG, "painting file of another version");
@@ -340,6 +345,38 @@ cf_status cf_snapshot_load(cf_film* f, const uint8_t* data, uint64_t len, cf_sna
   v.pig_format = CF_PIG_F16;
   v.device = 0;
   return cf_write_state(f, &v);
+}
+
+}  // namespace
+
+extern "C" {
+
+// No exception crosses the C ABI: host memory that runs out while a file is
+// packed or unpacked becomes CF_ERR_OUT_OF_MEMORY, anything else thrown
+// CF_ERR_INVALID_ARG.
+cf_status cf_snapshot_save(cf_film* f, const cf_snapshot_info* info, uint8_t** out, uint64_t* out_len) {
+  try {
+    return snapshot_save(f, info, out, out_len);
+  } catch (const std::bad_alloc&) {
+    return fail(f, CF_ERR_OUT_OF_MEMORY, "cf_snapshot_save: host memory");
+  } catch (...) {
+    return fail(f, CF_ERR_INVALID_ARG, "cf_snapshot_save");
+  }
+}
+
+cf_status cf_snapshot_free(uint8_t* buf) {
+  std::free(buf);
+  return CF_OK;
+}
+
+cf_status cf_snapshot_load(cf_film* f, const uint8_t* data, uint64_t len, cf_snapshot_info* info) {
+  try {
+    return snapshot_load(f, data, len, info);
+  } catch (const std::bad_alloc&) {
+    return fail(f, CF_ERR_OUT_OF_MEMORY, "cf_snapshot_load: host memory");
+  } catch (...) {
+    return fail(f, CF_ERR_INVALID_ARG, "cf_snapshot_load");
+  }
 }
 
 }  // extern "C"

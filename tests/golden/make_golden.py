@@ -1,6 +1,7 @@
 """Generates the golden fixtures tests/golden/*.npz.
 
-Runs where the reference checkout exists (REFERENCE, default /root/reference):
+Runs where the reference checkout exists (REFERENCE, else where
+oracle/wgsl_ref/build_ref.py's reference_root finds it):
   1. oracle/wgsl_ref/build_ref.py translates the reference WGSL to C++ and
      builds oracle/_ref/libwgslref.so;
   2. each case below is a small seeded canvas; its frame schedule (frame dt,
@@ -139,7 +140,9 @@ def deposit_set(cv, seed):
 
 
 def main():
-    ref = os.environ.get("REFERENCE", "/root/reference")
+    sys.path.insert(0, str(ROOT / "oracle" / "wgsl_ref"))
+    import build_ref
+    ref = str(build_ref.reference_root())
     subprocess.run([sys.executable, str(ROOT / "oracle" / "wgsl_ref" / "build_ref.py"), ref], check=True)
     import pyoracle as po
     po.build()

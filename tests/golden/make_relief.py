@@ -3,7 +3,8 @@ colour sampling and its key-light shadow march (shaders/render.wgsl,
 translated by oracle/wgsl_ref and evaluated in FP64 by
 oracle/_ref/librenderref.so) on a small seeded film.
 
-Runs where the reference checkout exists (REFERENCE, default /root/reference).
+Runs where the reference checkout exists (REFERENCE, else where
+oracle/wgsl_ref/build_ref.py's reference_root finds it).
 Usage: python tests/golden/make_relief.py
 """
 import ctypes as C
@@ -35,7 +36,9 @@ def film_planes(w, h, seed):
 
 
 def main():
-    ref = os.environ.get("REFERENCE", "/root/reference")
+    sys.path.insert(0, str(ROOT / "oracle" / "wgsl_ref"))
+    import build_ref
+    ref = str(build_ref.reference_root())
     subprocess.run([sys.executable, str(ROOT / "oracle" / "wgsl_ref" / "build_ref.py"), ref], check=True)
     L = C.CDLL(str(ROOT / "oracle" / "_ref" / "librenderref.so"))
     fp = C.POINTER(C.c_float)

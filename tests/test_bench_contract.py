@@ -31,6 +31,12 @@ def test_reference_arm_line():
     assert d["value"] > 0 and d["higher_is_better"] is True
     assert d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 0
     assert d["config"]["workload"] == "blobs512_dt1e-3_fp32"
+    # the same config object the GPU arm prints for this workload
+    sys.path.insert(0, str(ROOT))
+    import bench
+    gen, prec, dt_max, adaptive = bench.WORKLOADS["blobs512_dt1e-3_fp32"]
+    want = bench.single_config("blobs512_dt1e-3_fp32", gen(0), prec, adaptive, dt_max, 1)
+    assert d["config"] == json.loads(json.dumps(want))
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]

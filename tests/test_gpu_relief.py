@@ -115,3 +115,28 @@ def test_shadow_march_matches_the_reference(built):
     f.relief_shadow(pts.data_ptr(), n, [0.99, 0.0, 0.05], top, out.data_ptr())
     torch.cuda.synchronize()
     assert (out[:, 1] == 1).all()
+
+
+def test_misaligned_buffers_are_refused(built):
+    """Buffers valid byte by byte but not aligned to the vectors the kernels
+    use return CF_ERR_INVALID_ARG before any launch (nothing is written)."""
+    import torch
+    from canvaz_film.capi import FilmError
+    d, f = fixture_film()
+    buf = torch.zeros(4096, dtype=torch.uint8, device="cuda")
+    base = buf.data_ptr()
+    assert base % 256 == 0
+    with pytest.raises(FilmError):
+        f.sample_relief(base + 4, 8, base + 1024)      # points not 8-byte aligned
+    with pytest.raises(FilmError):
+        f.sample_relief(base, 8, base + 1026)          # out not 4-byte aligned
+    with pytest.raises(FilmError):
+        f.relief_shadow(base + 2, 8, (0.3, 0.5, 0.8), 1e-3, base + 1024)  # points not 4-byte aligned
+    with pytest.raises(FilmError):
+        f.relief_shadow(base, 8, (0.3, 0.5, 0.8), 1e-3, base + 1028)      # out not 8-byte aligned
+    with pytest.raises(FilmError):
+        f.render_relief(base + 2, 0.0, 0.0, 1e-3, 8, 8)                    # rgba8 not 4-byte aligned
+    torch.cuda.synchronize()
+    assert torch.count_nonzero(buf).item() == 0
+    f.sample_relief(base, 8, base + 1024)  # aligned: runs
+    torch.cuda.synchronize()

@@ -79,3 +79,20 @@ def test_load_rejects_other_files(built):
             f.load_snapshot(bad)
     with pytest.raises(FilmError):
         other.load_snapshot(data)
+
+
+def test_load_rejects_sizes_the_file_cannot_back(built):
+    """A damaged or hostile file that claims 2^32 - 1 chunks, or a chunk of
+    more than 32 MiB raw, is refused with an error status, before the library
+    allocates anything for those sizes."""
+    import struct
+    from canvaz_film.capi import FilmError
+    cv, f = stepped_film(capi.CF_PREC_REFERENCE)
+    data = f.save_snapshot()
+    head = data[:44]
+    many = head + struct.pack("<IQI", 8, 4 * cv.w * cv.h, 0xFFFFFFFF) + b"\0" * 64
+    raw = head + struct.pack("<IQIQ", 8, 4 * cv.w * cv.h, 1, 8) + struct.pack("<I", 0xFFFFFFF0) + b"\0" * 4
+    for bad in (many, raw):
+        with pytest.raises(FilmError):
+            f.load_snapshot(bad)
+    f.load_snapshot(data)  # the film is still usable
