@@ -6,7 +6,9 @@ reference_root() below is the one place that names it); does nothing when it
 is absent.  Steps:
 translate.py writes oracle/_ref/ref_shaders.inc (FP64), then g++ compiles
 driver.cpp against it; the relief and colour sampling of render.wgsl goes the
-same way into render_ref.inc and librenderref.so (render_driver.cpp).  Everything it writes stays in oracle/_ref/, which is
+same way into render_ref.inc and librenderref.so (render_driver.cpp), and the
+display fragment of resolve.wgsl into resolve_ref.inc and libresolveref.so
+(resolve_driver.cpp).  Everything it writes stays in oracle/_ref/, which is
 git-ignored.
 Usage: python build_ref.py [reference_root]
 """
@@ -52,6 +54,13 @@ def build(ref=None):
     (OUT / "render_ref.inc").write_text(src)
     subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "render_driver.cpp"),
                     "-o", str(OUT / "librenderref.so")], check=True)
+    # the display fragment of resolve.wgsl, in f32 as the shader computes
+    # (one rounding per operation: no contraction), its uniform's fields a, b,
+    # c kept as they are named
+    src = translate.translate_subset(str(ref), "resolve.wgsl", ["fs"], set(), "wgres", "float", members={"R"})
+    (OUT / "resolve_ref.inc").write_text(src)
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", str(OUT),
+                    str(HERE / "resolve_driver.cpp"), "-o", str(OUT / "libresolveref.so")], check=True)
     return lib
 
 

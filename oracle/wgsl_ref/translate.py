@@ -171,7 +171,8 @@ def conv_body(body):
 
 def conv_fn(it, name):
     it = re.sub(r"@compute\s*@workgroup_size\([^)]*\)\s*", "", it)
-    m = re.match(r"fn\s+(\w+)\s*\((.*?)\)\s*(->\s*([^{]+?))?\s*\{", it, re.S)
+    it = re.sub(r"^\s*@(fragment|vertex)\s*", "", it)  # stage attributes of render entry points
+    m = re.match(r"fn\s+(\w+)\s*\((.*?)\)\s*(->\s*(?:@\w+\([^)]*\)\s*)?([^{]+?))?\s*\{", it, re.S)
     assert m, it[:80]
     params = []
     for p in split_top(m.group(2)):
@@ -338,10 +339,12 @@ def translate(ref_root, real="double"):
 RGBA = {"r": "x", "g": "y", "b": "z", "a": "w"}
 
 
-def translate_subset(ref_root, module, roots, stubs, namespace, real="double"):
+def translate_subset(ref_root, module, roots, stubs, namespace, real="double", members=()):
     """Translate the functions `roots` of one shader module and everything they
     call, into their own namespace; the functions in `stubs` get empty bodies
-    (the driver never reaches them).  Colour swizzles (.rgb, .a) map to xyzw."""
+    (the driver never reaches them).  Colour swizzles (.rgb, .a) map to xyzw,
+    except on the variables named in `members`, whose fields are called a, b,
+    c (a uniform struct such as resolve.wgsl's Res)."""
     with open("%s/shaders/%s" % (ref_root, module)) as f:
         src = f.read()
     items = split_items(src)
@@ -370,7 +373,9 @@ def translate_subset(ref_root, module, roots, stubs, namespace, real="double"):
             g = g.replace("texture_2d<f32>", "Tex").replace("sampler ", "Sampler ")
             globals_.append(g)
         elif kind == "fn" and nm in need:
-            it2 = re.sub(r"\.([rgba]{1,4})\b", lambda m: "." + "".join(RGBA[ch] for ch in m.group(1)), it)
+            it2 = re.sub(r"(\b\w+)?\.([rgba]{1,4})\b",
+                         lambda m: m.group(0) if m.group(1) in members
+                         else (m.group(1) or "") + "." + "".join(RGBA[ch] for ch in m.group(2)), it)
             proto, text = conv_fn(it2, nm)
             protos.append(proto + ";")
             if nm in stubs:

@@ -96,3 +96,34 @@ def test_load_rejects_sizes_the_file_cannot_back(built):
         with pytest.raises(FilmError):
             f.load_snapshot(bad)
     f.load_snapshot(data)  # the film is still usable
+
+
+def test_hand_written_painting_file_loads_and_saves(built):
+    """The byte vector written from the format (tests/golden/psim_vector.py)
+    loads into a 2 x 1 film as exactly its planes and header; the film saved
+    again parses (independent parser) to the same header and planes."""
+    import importlib.util
+    from pathlib import Path
+    import lz4_ref
+    from canvaz_film.film import Film
+    spec = importlib.util.spec_from_file_location("psim_vector", Path(__file__).parent / "golden" / "psim_vector.py")
+    v = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(v)
+    st = capi.Settings.default(width_m=2e-3, height_m=1e-3)
+    f = Film(st, v.W, v.H, capi.CF_PREC_REFERENCE)
+    cv = synth.blob_canvas(16, 16, 1, n_blobs=1, tables="reference")
+    f.set_tables(cv.pigtab, cv.cmf)
+    info = f.load_snapshot(v.FILE)
+    assert (info["w"], info["h"]) == (v.W, v.H)
+    for k, want in v.HEADER.items():
+        assert np.float32(info[k]) == np.float32(want), k
+    got = f.read_state(pig_format=capi.CF_PIG_F16)
+    want = v.planes()
+    for k in v.ORDER:  # read_state widens f16 slots and bands to f32, exactly
+        np.testing.assert_array_equal(np.asarray(got[k]).reshape(-1),
+                                      np.asarray(want[k]).astype(np.asarray(got[k]).dtype).reshape(-1), err_msg=k)
+    data = f.save_snapshot(**{k: v.HEADER[k] for k in ("tilt_deg", "tilt_dir_deg", "cure_rate", "h_max", "s_max",
+                                                       "total_deposited")})
+    hdr, parts = lz4_ref.parse_painting(data)
+    assert data[:44] == v.FILE[:44]
+    assert parts == v.parts()

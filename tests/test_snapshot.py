@@ -87,3 +87,33 @@ def test_rejects_malformed_blocks(lib):
     for chunk in bad:
         st, _ = decompress(lib, chunk)
         assert st == capi.CF_ERR_INVALID_ARG
+
+
+def _vector():
+    import importlib.util
+    from pathlib import Path
+    spec = importlib.util.spec_from_file_location("psim_vector", Path(__file__).parent / "golden" / "psim_vector.py")
+    v = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(v)
+    return v
+
+
+def test_hand_written_painting_file_parses():
+    """The byte vector written from the format (tests/golden/psim_vector.py)
+    parses with the independent parser into the header and the 8 planes."""
+    v = _vector()
+    hdr, parts = lz4_ref.parse_painting(v.FILE)
+    assert hdr["version"] == 1 and (hdr["w"], hdr["h"]) == (v.W, v.H)
+    for k, want in v.HEADER.items():
+        assert np.float64(hdr[k]) == np.float64(np.float32(want)) or hdr[k] == want, k
+    assert parts == v.parts()
+
+
+def test_hand_written_blocks_decode_in_the_library(lib):
+    """Each hand-written chunk (literal runs, zero runs at offset 1, an f16
+    pattern at offset 2, length bytes in both nibbles) decodes in the
+    library's own LZ4 decoder to its plane."""
+    v = _vector()
+    for (off, clen), want in zip(v.chunks(), v.parts()):
+        st, back = decompress(lib, v.FILE[off:off + clen])
+        assert st == capi.CF_OK and back == want
