@@ -22,8 +22,9 @@ from canvaz_film.deposit import DEPOSIT_DTYPE
 
 pytestmark = pytest.mark.gpu
 
-# the frame fixtures (relief_samples.npz holds render samples, tests/test_relief.py)
-GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz") if p.stem != "relief_samples")
+# the frame fixtures (relief_samples.npz and resolve_samples.npz hold render and
+# display samples: tests/test_relief.py, tests/test_resolve_fixture.py)
+GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz") if p.stem not in ("relief_samples", "resolve_samples"))
 
 # oracle plane -> (CUDA plane(s), per-cell count)
 TRANSFER = ["h", "m", "strata_h", "strata_cure", "strata_pig", "sub_refl", "lay", "pres", "flux", "acc", "alpha",
