@@ -835,8 +835,8 @@ def gpu_arm(args):
         if pig_fmt == capi.CF_PIG_F16:
             pig = pig.astype(np.float16)
         elif pig_fmt == capi.CF_PIG_BF16:
-            from canvaz_film.film import _f32_to_bf16
-            pig = _f32_to_bf16(pig)
+            from canvaz_film.film import _pig_to_bf16
+            pig = _pig_to_bf16(pig)
         pigp = torch.from_numpy(np.ascontiguousarray(pig)).pin_memory().numpy()
         v.strata_pig = pigp.ctypes.data
         h2d = sum(pinned[k].nbytes for k in ("h", "m", "rheo", "strata_h", "strata_cure", "lay")) + subp.nbytes + pigp.nbytes

@@ -52,7 +52,7 @@ typedef enum cf_status {
 typedef enum cf_precision {
     CF_PREC_REFERENCE = 0, /* f16 pigment slots, f32 rheology: the reference layout */
     CF_PREC_FP32 = 1,      /* f32 pigment slots, f32 rheology                       */
-    CF_PREC_BF16 = 2       /* bf16 pigment slots, bf16 rheology                     */
+    CF_PREC_BF16 = 2       /* bf16 pigment slots, bf16 rheology (slot 14 kept as mu) */
 } cf_precision;
 
 /* Element format of the strata_pig plane handed to cf_write_state / cf_read_state. */
@@ -61,6 +61,11 @@ typedef enum cf_pig_format {
     CF_PIG_F32 = 1,  /* 4 strata x 16 slots x float:     256 B per cell                    */
     CF_PIG_BF16 = 2  /* 4 strata x 16 slots x bfloat16:  128 B per cell                    */
 } cf_pig_format;
+/* In the bfloat16 format (and in CF_PREC_BF16 films' storage) slot 14 of each
+ * stratum, whose value is the viscosity override ln mu + 10 (0 = none), is
+ * stored as mu itself in Pa s (0 = none): bfloat16's 8 significant bits step
+ * by 0.0625 on ln mu + 10 (about 6 % on mu) but by 0.4 % on mu.  Every other
+ * slot, and every other format, stores the slot's value. */
 
 /* FilmSettings (src/film/mod.rs:281-350).  The reference reads its ablation
  * switches from environment variables inside update_params

@@ -85,10 +85,15 @@ inline double f16_value(uint16_t b) {
   return s ? -v : v;
 }
 
-// Storage rounding of a pigment slot value.
-inline double round_pig(double x, int mode) {
+// Storage rounding of the value of pigment slot `slot`.  BF16 storage keeps
+// slot 14 (the viscosity override ln mu + 10, 0 = none) as mu itself, so that
+// slot rounds on mu (bfloat16 on ln mu + 10 would step by 0.0625 there).
+inline double round_pig(double x, int mode, int slot) {
   if (mode == CF_PIG_F16) return round_f16(x);
-  if (mode == CF_PIG_BF16) return round_bf16(x);
+  if (mode == CF_PIG_BF16) {
+    if (slot == 14) return x > 0.0 ? std::log(round_bf16(std::exp(x - 10.0))) + 10.0 : 0.0;
+    return round_bf16(x);
+  }
   return (double)(float)x;
 }
 
@@ -374,7 +379,7 @@ struct Film {
     R t = clampR((x - e0) / (e1 - e0), R(0), R(1));
     return t * t * (R(3) - R(2) * t);
   }
-  R pig_store(R v) const { return (R)round_pig((double)v, pig_mode); }
+  R pig_store(R v, int slot) const { return (R)round_pig((double)v, pig_mode, slot); }
 
   // common.wgsl:140-171
   bool cell_active(int i, int j) const {
@@ -986,7 +991,7 @@ struct Film {
     for (int k = 0; k < 4; ++k) {
       th[4 * c + k] = s.th[k];
       cu[4 * c + k] = s.cu[k];
-      for (int q = 0; q < 16; ++q) pg[64 * c + 16 * k + q] = pig_store(s.pg[k][q]);
+      for (int q = 0; q < 16; ++q) pg[64 * c + 16 * k + q] = pig_store(s.pg[k][q], q);
     }
   }
   static R pig_dist(const R* a, const R* b) {

@@ -201,7 +201,7 @@ int cfo_buffer(void* p, const char* name, double* io, int write) {
         bool refp = n == "sub_refl";
         for (size_t i = 0; i < v.size(); ++i) {
           double x = io[i];
-          if (pigp) x = cfo::round_pig(x, F.pig_mode);
+          if (pigp) x = cfo::round_pig(x, F.pig_mode, (int)(i % 16));
           else if (refp) x = cfo::round_f16(x);
           v[i] = (decltype(v[0] + 0))x;
         }

@@ -41,7 +41,7 @@ def build(ref=None):
                    check=True)
     shutil.copy(HERE / "wgsl_rt_types.inc", OUT / "wgsl_rt_types.inc")
     lib = OUT / "libwgslref.so"
-    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "driver.cpp"),
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "driver.cpp"),
                     "-o", str(lib)], check=True)
     # the relief / colour sampling of render.wgsl (a subset: the beauty-mode
     # helpers it never reaches with the plain camera are stubs)
@@ -52,7 +52,7 @@ def build(ref=None):
                                       "shadow_at"],
                                      {"color_beauty", "color_crisp", "surf_smooth", "hwarp"}, "wgrr")
     (OUT / "render_ref.inc").write_text(src)
-    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "render_driver.cpp"),
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "render_driver.cpp"),
                     "-o", str(OUT / "librenderref.so")], check=True)
     # the display fragment of resolve.wgsl, in f32 as the shader computes
     # (one rounding per operation: no contraction), its uniform's fields a, b,

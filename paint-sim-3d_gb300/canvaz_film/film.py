@@ -35,6 +35,32 @@ def _f32_to_bf16(x):
     return ((u + r) >> 16).astype(np.uint16)
 
 
+def _pig_to_bf16(x):
+    """Pigment slots (16 per stratum, last axis a multiple of 16) as the BF16
+    format's bits: slot 14, the viscosity override ln mu + 10 (0 = none), is
+    stored as mu itself (Pa s); every other slot as its value."""
+    a = np.array(x, np.float32)
+    v = a.reshape(-1, 16)
+    s14 = v[:, 14].astype(np.float64)
+    v[:, 14] = np.where(s14 > 0, np.exp(np.where(s14 > 0, s14, 10.0) - 10.0), 0.0).astype(np.float32)
+    return _f32_to_bf16(a)
+
+
+def _pig_from_bf16(u16):
+    """The inverse of _pig_to_bf16: slot values as float32 (slot 14 back to
+    ln mu + 10, 0 where no override is stored)."""
+    u = np.asarray(u16, np.uint16)
+    a = _bf16_to_f32(u).copy()
+    v = a.reshape(-1, 16)
+    b = u.reshape(-1, 16)[:, 14]
+    mu = np.where(b != 0, v[:, 14], np.float32(1.0)).astype(np.float32)
+    v[:, 14] = np.where(b != 0, np.log(mu) + np.float32(10.0), np.float32(0.0)).astype(np.float32)
+    return a
+
+
+_PIG_PLANES = ("strata_pig", "strata_pig2")
+
+
 def _lib():
     L = capi.load_library()
     if not hasattr(L, "_debug_bound"):
@@ -122,7 +148,7 @@ class Film:
             elif fmt == capi.CF_PIG_F16:
                 a = x.astype(np.float16)
             else:
-                a = _f32_to_bf16(x)
+                a = _pig_to_bf16(x)
             a = np.ascontiguousarray(a)
             keep["strata_pig"] = a
             v.strata_pig = a.ctypes.data
@@ -143,7 +169,7 @@ class Film:
         if pig_format == capi.CF_PIG_F16:
             pig = pig.view(np.float16).astype(np.float32)
         elif pig_format == capi.CF_PIG_BF16:
-            pig = _bf16_to_f32(pig)
+            pig = _pig_from_bf16(pig)
         out["strata_pig"] = pig
         out["sub_refl"] = out["sub_refl"].astype(np.float32)
         return out
@@ -270,7 +296,8 @@ class Film:
         raw = np.zeros(nb.value, np.uint8)
         self._check(self.L.cf_debug_read(self.p, name.encode(), raw.ctypes.data, nb.value), name)
         if dt == "bf16":
-            return _bf16_to_f32(raw.view(np.uint16)).astype(np.float64)
+            conv = _pig_from_bf16 if name in _PIG_PLANES else _bf16_to_f32
+            return conv(raw.view(np.uint16)).astype(np.float64)
         a = raw.view(dt)
         return a.astype(np.uint64) if dt in (np.uint32,) else a.astype(np.float64)
 
@@ -280,7 +307,7 @@ class Film:
         dt = _ELEM_DTYPE[el.value]
         v = np.asarray(values).reshape(-1)
         if dt == "bf16":
-            a = _f32_to_bf16(v.astype(np.float32))
+            a = (_pig_to_bf16 if name in _PIG_PLANES else _f32_to_bf16)(v.astype(np.float32))
         else:
             a = np.ascontiguousarray(v.astype(dt))
         assert a.nbytes == nb.value, (name, a.nbytes, nb.value)

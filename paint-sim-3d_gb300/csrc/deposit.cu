@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256) k_deposit_lay(cfk::Film F, DepTables D, c
 #pragma unroll
     for (int k = 0; k < 4; ++k)
 #pragma unroll
-      for (int q = 0; q < 16; ++q) s.pg[k][q] = PigIO<MODE>::round(s.pg[k][q]);
+      for (int q = 0; q < 16; ++q) s.pg[k][q] = PigIO<MODE>::round(s.pg[k][q], q);
     F.agg[c] = stack_agg(P, lt, s);
   }
 }

@@ -217,6 +217,23 @@ __device__ __forceinline__ uint32_t f_to_h16(float v) { return (uint32_t)__half_
 __device__ __forceinline__ float b16_to_f(uint32_t bits) { return __uint_as_float(bits << 16); }
 __device__ __forceinline__ uint32_t f_to_b16(float v) { return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v)); }
 
+// Pigment slot 14 carries a stratum's viscosity override as ln mu + 10 (0 =
+// none: the pigments' own viscosities apply; cure.wgsl:3-48).  Its values lie
+// in about 9.3..13.9, where bfloat16's 8 significant bits step by 0.0625 and
+// would put mu off by up to 6 %.  BF16 storage therefore keeps mu itself in
+// that slot (Pa s, 0 = none): 8 bits on mu hold it to 0.2 %.  Every other
+// slot, and the value the kernels compute with, stay as the reference has
+// them.
+constexpr int SLOT_LNMU = 14;
+__device__ __forceinline__ uint32_t b16_from_slot(float v, int slot) {
+  if (slot == SLOT_LNMU) return v > 0.f ? f_to_b16(expf(v - 10.0f)) : 0u;
+  return f_to_b16(v);
+}
+__device__ __forceinline__ float slot_from_b16(uint32_t bits, int slot) {
+  if (slot == SLOT_LNMU) return bits != 0u ? logf(b16_to_f(bits)) + 10.0f : 0.f;
+  return b16_to_f(bits);
+}
+
 // ---- pigment slots: 16 per stratum, 4 strata per cell, chunk-major ----
 template <int MODE>
 struct PigIO {
@@ -241,8 +258,8 @@ struct PigIO {
             o[8 * q + 2 * e] = h16_to_f(wv[e] & 0xffffu);
             o[8 * q + 2 * e + 1] = h16_to_f(wv[e] >> 16);
           } else {
-            o[8 * q + 2 * e] = b16_to_f(wv[e] & 0xffffu);
-            o[8 * q + 2 * e + 1] = b16_to_f(wv[e] >> 16);
+            o[8 * q + 2 * e] = slot_from_b16(wv[e] & 0xffffu, 8 * q + 2 * e);
+            o[8 * q + 2 * e + 1] = slot_from_b16(wv[e] >> 16, 8 * q + 2 * e + 1);
           }
         }
       }
@@ -259,17 +276,18 @@ struct PigIO {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           if constexpr (MODE == CF_PREC_REFERENCE) wv[e] = f_to_h16(v[8 * q + 2 * e]) | (f_to_h16(v[8 * q + 2 * e + 1]) << 16);
-          else wv[e] = f_to_b16(v[8 * q + 2 * e]) | (f_to_b16(v[8 * q + 2 * e + 1]) << 16);
+          else wv[e] = b16_from_slot(v[8 * q + 2 * e], 8 * q + 2 * e) |
+                       (b16_from_slot(v[8 * q + 2 * e + 1], 8 * q + 2 * e + 1) << 16);
         }
       }
       base[at(F, c, k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
     }
   }
-  // a slot value as the store above keeps it
-  __device__ static __forceinline__ float round(float v) {
+  // the value of slot `slot` as the store above keeps it
+  __device__ static __forceinline__ float round(float v, int slot) {
     if constexpr (MODE == CF_PREC_FP32) return v;
     else if constexpr (MODE == CF_PREC_REFERENCE) return h16_to_f(f_to_h16(v));
-    else return b16_to_f(f_to_b16(v));
+    else return slot_from_b16(b16_from_slot(v, slot), slot);
   }
   // bit-exact copy of stratum ks of cell cs (in src) to stratum kd of cell cd (in dst)
   __device__ static __forceinline__ void copy(const Film& F, uint4* dst, uint32_t cd, int kd, const uint4* src,

@@ -1096,7 +1096,7 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     for (int k = 0; k < 4; ++k) {
       const float pk = get4(s.pg, k);
       PigLane<MODE>::store(F, F.pig2, c, k, H.q, pk);
-      acc.add(H, k, get4(s.th, k), get4(s.cu, k), PigLane<MODE>::round(pk), hc, ltab, tab, dbg);
+      acc.add(H, k, get4(s.th, k), get4(s.cu, k), PigLane<MODE>::round(pk, H.q), hc, ltab, tab, dbg);
     }
     const float4 agg = acc.agg(P);
     const ushort4 col = acc.color(H, P, cm, hc, F.m[c]);
@@ -1353,7 +1353,7 @@ __global__ void __launch_bounds__(256) k_pig_import_t(Film F, uint4* dst, const 
     float x;
     if (fmt == CF_PIG_F32) x = ((const float*)src)[s];
     else if (fmt == CF_PIG_F16) x = h16_to_f(((const uint16_t*)src)[s]);
-    else x = b16_to_f(((const uint16_t*)src)[s]);
+    else x = slot_from_b16(((const uint16_t*)src)[s], e % 16);
     sv[e / 64][e % 64] = x;
   }
   __syncthreads();
@@ -1366,7 +1366,7 @@ __global__ void __launch_bounds__(256) k_pig_import_t(Film F, uint4* dst, const 
     for (int w = 0; w < 4; ++w) {
       if (MODE == CF_PREC_FP32) wv[w] = __float_as_uint(v[w]);
       else if (MODE == CF_PREC_REFERENCE) wv[w] = f_to_h16(v[2 * w]) | (f_to_h16(v[2 * w + 1]) << 16);
-      else wv[w] = f_to_b16(v[2 * w]) | (f_to_b16(v[2 * w + 1]) << 16);
+      else wv[w] = b16_from_slot(v[2 * w], q * PER + 2 * w) | (b16_from_slot(v[2 * w + 1], q * PER + 2 * w + 1) << 16);
     }
     dst[PigIO<MODE>::at(F, (uint32_t)(c0 + cl), k, q)] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
   }
@@ -1391,7 +1391,7 @@ __global__ void __launch_bounds__(256) k_pig_export_t(Film F, const uint4* srcp,
       if (MODE == CF_PREC_FP32) v[x] = __uint_as_float(wv[x]);
       else {
         const uint32_t bits = (x & 1) ? (wv[x / 2] >> 16) : (wv[x / 2] & 0xffffu);
-        v[x] = MODE == CF_PREC_REFERENCE ? h16_to_f(bits) : b16_to_f(bits);
+        v[x] = MODE == CF_PREC_REFERENCE ? h16_to_f(bits) : slot_from_b16(bits, q * PER + x);
       }
     }
   }
@@ -1401,7 +1401,7 @@ __global__ void __launch_bounds__(256) k_pig_export_t(Film F, const uint4* srcp,
     const float x = sv[e / 64][e % 64];
     if (fmt == CF_PIG_F32) ((float*)dst)[s] = x;
     else if (fmt == CF_PIG_F16) ((uint16_t*)dst)[s] = (uint16_t)f_to_h16(x);
-    else ((uint16_t*)dst)[s] = (uint16_t)f_to_b16(x);
+    else ((uint16_t*)dst)[s] = (uint16_t)b16_from_slot(x, e % 16);
   }
 }
 template <class Rh>

@@ -56,19 +56,19 @@ struct PigLane {
     if constexpr (F32) return reinterpret_cast<const float*>(base)[at(F, c, k, q)];
     else {
       uint32_t b = reinterpret_cast<const uint16_t*>(base)[at(F, c, k, q)];
-      return MODE == CF_PREC_REFERENCE ? h16_to_f(b) : b16_to_f(b);
+      return MODE == CF_PREC_REFERENCE ? h16_to_f(b) : slot_from_b16(b, q);
     }
   }
   __device__ static __forceinline__ void store(const Film& F, uint4* base, uint32_t c, int k, int q, float v) {
     if constexpr (F32) reinterpret_cast<float*>(base)[at(F, c, k, q)] = v;
     else reinterpret_cast<uint16_t*>(base)[at(F, c, k, q)] =
-        (uint16_t)(MODE == CF_PREC_REFERENCE ? f_to_h16(v) : f_to_b16(v));
+        (uint16_t)(MODE == CF_PREC_REFERENCE ? f_to_h16(v) : b16_from_slot(v, q));
   }
-  // the value a store followed by a load gives
-  __device__ static __forceinline__ float round(float v) {
+  // the value a store of slot q followed by a load gives
+  __device__ static __forceinline__ float round(float v, int q) {
     if constexpr (F32) return v;
     else if constexpr (MODE == CF_PREC_REFERENCE) return h16_to_f(f_to_h16(v));
-    else return b16_to_f(f_to_b16(v));
+    else return slot_from_b16(b16_from_slot(v, q), q);
   }
 };
 
