@@ -54,6 +54,8 @@ WORKLOADS = {
     "blobs512_dt1e-3_fp32": (lambda seed: synth.config(0, seed), capi.CF_PREC_FP32, 1e-3, False),
     "blobs4096_dt1e-3_bf16": (lambda seed: synth.config(2, seed), capi.CF_PREC_BF16, 1e-3, False),
     "blobs4096_dt1e-3_fp32": (lambda seed: synth.config(2, seed), capi.CF_PREC_FP32, 1e-3, False),
+    # the same field at a quarter of the side (31 blobs): small case for kernel captures
+    "blobs1024_dt1e-3_fp32": (lambda seed: synth.config(2, seed, scale=4), capi.CF_PREC_FP32, 1e-3, False),
     # thick pours with the implicit hydrostatic CG steps (the reference's default), adaptive
     "pour2048_implicit_fp32": (lambda seed: synth.config(5, seed), capi.CF_PREC_FP32, 1.0 / 60.0, True),
     "pour512_implicit_fp32": (lambda seed: synth.config(5, seed, scale=4), capi.CF_PREC_FP32, 1.0 / 60.0, True),

@@ -89,9 +89,15 @@ def test_deposit_dispatch_matches_oracle(built, case):
     o.run("deposit")
     f.run("deposit")
     assert (o.buf("h") - h0).max() > 0  # paint was laid
-    for plane in ("h", "strata_h", "strata_cure", "lay", "tile_moved"):
-        gp.compare(plane, gp.cuda_plane(f, plane), o.buf(plane))
-    gp.compare("strata_pig", gp.cuda_plane(f, "strata_pig"), o.buf("strata_pig"), rtol=2e-3, frac=2e-3)
+    # the FP32 mirror from identical f32 inputs: every value to rounding, the
+    # cells whose stack push / merge decision flipped counted (at most 2)
+    flipped = set()
+    for plane in ("h", "strata_h", "strata_cure", "strata_pig", "lay", "tile_moved"):
+        cells = gp.flipped_cells(plane, gp.cuda_plane(f, plane), o.buf(plane))
+        if cells:
+            print("deposit %s %s: %d cell(s) off, first %s" % (case, plane, len(cells), sorted(cells)[:8]))
+        flipped |= cells
+    assert len(flipped) <= 2, sorted(flipped)[:16]
 
 
 @pytest.mark.parametrize("prec", [capi.CF_PREC_REFERENCE, capi.CF_PREC_FP32, capi.CF_PREC_BF16])

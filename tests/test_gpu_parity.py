@@ -1,13 +1,21 @@
 """CUDA kernels against the oracle (GPU).
 
-Per-dispatch parity: the oracle runs a few frames to reach a state with
-fronts, multi-strata stacks and sleeping tiles; that whole internal state
-(rounded to f32, the storage precision) is copied into the CUDA film, one
-dispatch runs on both sides, and every plane it writes is compared.
+Per-dispatch parity: the oracle's FP32 mirror (the same restatement in f32,
+one rounding per operation) runs a few frames to reach a state with fronts,
+multi-strata stacks and sleeping tiles; that whole internal state is copied
+into the CUDA film, one dispatch runs on both sides from identical f32
+inputs, and every plane it writes is compared value by value: integer planes
+(front offsets, tile bits) exactly, float planes to 1e-5 relative with a
+floor of 1e-6 of the plane's largest value, the colour to one f16 step.  A
+value outside that is counted as a branch flip (a discrete stack decision -
+merge, push - that the last bit of a sum decides differently); the flipped
+cells are reported, and only the strata pass, whose half-warp sums are
+tree-ordered, may have any.
 
 Frame parity: the CUDA film replays the golden fixtures (inputs, schedule,
 params) and is compared with the reference's FP64 outputs through the
-branch-robust metrics of tests/parity.py.
+branch-robust metrics of tests/parity.py; the tile activity bits must match
+the reference's exactly.
 """
 import json
 from pathlib import Path
@@ -78,9 +86,9 @@ def make_case(name):
     return cv, sched
 
 
-def oracle_state(cv, sched):
+def oracle_state(cv, sched, bits=32):
     st = po.make_settings(cv.settings)
-    o = po.Oracle(cv.w, cv.h, st, 0, 64)
+    o = po.Oracle(cv.w, cv.h, st, 0, bits)
     o.set_tables(cv.pigtab, cv.cmf)
     o.write_state(cv.planes)
     fdt, n, frames = sched
@@ -121,18 +129,34 @@ def cuda_plane(f, name):
     return f.plane(name)
 
 
-def compare(name, got, want, rtol=1e-4, frac=2e-3):
-    got = np.asarray(got, np.float64)
-    want = np.asarray(want, np.float64)
+# values per cell of each compared plane (oracle layout)
+PER_CELL = {"pres": 2, "flux": 4, "acc": 4, "acc_s": 16, "alpha_s": 4, "strata_h": 4, "strata_cure": 4,
+            "strata_pig": 64, "sub_refl": 16, "rheo": 3, "fnorm": 2, "color": 4}
+# dispatches whose half-warp tree sums may flip a discrete stack decision in a
+# few cells, and how many flipped cells a case may have
+FLIP_BUDGET = {"strata_pass": 8}
+RTOL, ATOL = 1e-5, 1e-6
+
+
+def flipped_cells(name, got, want):
+    """Cells where the CUDA plane differs from the FP32 mirror beyond rounding:
+    integer planes at any bit, the colour by more than one f16 step (the
+    mirror's colour rounded to f16 as the plane stores it), other floats by
+    more than RTOL relative with a floor of ATOL x the plane's largest value."""
+    got = np.asarray(got, np.float64).ravel()
+    want = np.asarray(want, np.float64).ravel()
     assert got.shape == want.shape, (name, got.shape, want.shape)
-    if name in ("delta", "tile_flags", "tile_moved"):
+    if name in ("delta", "tile_flags", "tile_moved", "lay"):
         bad = got.astype(np.uint64) != want.astype(np.uint64)
-        assert bad.mean() <= frac, (name, int(bad.sum()))
-        return
-    scale = max(float(np.abs(want).max()), 1e-30)
-    err = np.abs(got - want) / scale
-    bad = err > rtol
-    assert bad.mean() <= frac, (name, int(bad.sum()), got.size, float(err.max()))
+    elif name == "color":
+        w16 = want.astype(np.float16)
+        step = np.spacing(np.abs(w16)).astype(np.float64)
+        bad = np.abs(got - w16.astype(np.float64)) > step
+    else:
+        scale = max(float(np.abs(want).max()), 1e-30)
+        bad = np.abs(got - want) > RTOL * np.abs(want) + ATOL * scale
+    k = PER_CELL.get(name, 1)
+    return set(np.nonzero(bad.reshape(-1, k).any(axis=1))[0].tolist())
 
 
 @pytest.mark.parametrize("case", ["drip", "blob", "mixed"])
@@ -147,15 +171,14 @@ def test_dispatch_parity(built, case, kernel):
     for k in ORACLE_SEQ.get(kernel, [kernel]):
         o.run(k)
     f.run(kernel)
+    flipped = set()
     for plane in WRITES[kernel]:
-        want = o.buf(plane)
-        got = cuda_plane(f, plane)
-        if plane == "color":
-            compare(plane, got, want, rtol=2e-3, frac=1e-3)
-        elif plane in ("strata_pig", "strata_pig2"):
-            compare(plane, got, want, rtol=2e-3, frac=2e-3)
-        else:
-            compare(plane, got, want)
+        cells = flipped_cells(plane, cuda_plane(f, plane), o.buf(plane))
+        if cells:
+            print("%s %s %s: %d cell(s) off, first %s" % (case, kernel, plane, len(cells), sorted(cells)[:8]))
+        flipped |= cells
+    print("%s %s: %d flipped cell(s) of %d" % (case, kernel, len(flipped), cv.w * cv.h))
+    assert len(flipped) <= FLIP_BUDGET.get(kernel, 0), (case, kernel, sorted(flipped)[:16])
 
 
 def replay_cuda(d, precision=capi.CF_PREC_REFERENCE):
@@ -179,29 +202,42 @@ def replay_cuda(d, precision=capi.CF_PREC_REFERENCE):
     return f
 
 
-# deposit_strokes lays a second set of strokes onto paint that is spreading at
-# its yield threshold; the frames after it amplify single-cell branch flips.
-# Perturbing the input heights by 1e-7 (relative) moves the oracle's FP32
-# mirror of the reference arithmetic between 2e-7 and 4e-6 from FP64 on this
-# fixture, and the CUDA path between 1.5e-7 and 2.3e-5; deposit_fresh (strokes
-# on bare canvas) holds the usual 1e-5.  implicit_pour runs 8 CG solves of 40
-# iterations in f32: the FP32 mirror lands 2.4e-5 to 4.8e-5 from FP64 under
-# the same perturbations, the CUDA path 2.4e-5.
-H_REL_BRANCHY = {"deposit_strokes": 5e-5, "implicit_pour": 1e-4}
+def mirror_replay(d, bits=32):
+    """The oracle (FP32 mirror by default) replaying a fixture."""
+    w, h = int(d["w"]), int(d["h"])
+    st = po.make_settings(json.loads(str(d["settings"])))
+    o = po.Oracle(w, h, st, 0, bits)
+    o.set_tables(d["pigtab"], d["cmf"])
+    o.write_state({k[3:]: d[k] for k in d.files if k.startswith("in_")})
+    for fr, (fdt, n) in enumerate(d["schedule"]):
+        if "deposits_%d" % fr in d.files:
+            o.upload_deposits(d["deposits_%d" % fr].reshape(-1).view(DEPOSIT_DTYPE))
+        o.update_params(float(fdt), int(n))
+        o.encode_frame(int(n))
+    return o
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[p.stem for p in GOLDEN])
 def test_frames_vs_reference_fixture(built, path):
+    """Height within 1e-5 (relative L2) of the reference's FP64 outputs, or
+    within 1.5x the FP32 mirror's own distance where f32 arithmetic itself
+    cannot get closer (implicit_pour: 8 CG solves of 40 iterations put the
+    mirror 4.7e-5 away); tile activity bits exactly the reference's."""
     d = np.load(path)
     f = replay_cuda(d)
     s = f.read_state()
     got = {"h": s["h"], "m": s["m"], "strata_h": s["strata_h"], "strata_pig": s["strata_pig"], "color": f.color()}
     want = {k: d["out_" + k] for k in got}
     m = parity.metrics(got, want)
-    print(path.stem, m)
-    parity.check(m, h_rel=H_REL_BRANCHY.get(path.stem, parity.H_REL_L2))
+    o = mirror_replay(d)
+    mirror = {"h": o.buf("h"), "m": o.buf("m"), "strata_h": o.buf("strata_h"), "strata_pig": o.buf("strata_pig"),
+              "color": o.buf("color")}
+    mm = parity.metrics(mirror, want)
+    bound = max(parity.H_REL_L2, 1.5 * mm["h_rel_l2"]) if mm["h_rel_l2"] < 1.0 else parity.H_REL_L2
+    print(path.stem, "CUDA", m, "FP32 mirror h rel L2 %.3e, bound %.3e" % (mm["h_rel_l2"], bound))
+    parity.check(m, h_rel=bound)
     tf = f.plane("tile_flags").astype(np.uint64)
-    assert (tf == d["out_tile_flags"].astype(np.uint64)).mean() >= 0.95
+    np.testing.assert_array_equal(tf, d["out_tile_flags"].astype(np.uint64))
 
 
 def test_state_roundtrip(built):
