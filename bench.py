@@ -870,6 +870,17 @@ def gpu_arm(args):
             assert L.cf_read_state_async(fl.p, C.byref(hv), s.cuda_stream) == 0
             assert L.cf_read_color_async(fl.p, cp, s.cuda_stream) == 0
 
+        # a probe of the host link on this machine (three torch copies of the
+        # pigment plane, pinned host -> device), reported beside the e2e figure
+        dev_buf = torch.empty(pigp.nbytes, dtype=torch.uint8, device="cuda")
+        src_buf = torch.from_numpy(pigp.view(np.uint8).reshape(-1))
+        torch.cuda.synchronize()
+        tl = time.perf_counter()
+        for _ in range(3):
+            dev_buf.copy_(src_buf, non_blocking=True)
+        torch.cuda.synchronize()
+        link_gbs = 3 * pigp.nbytes / (time.perf_counter() - tl) / 1e9
+        del dev_buf, src_buf
         e2e_step(0)
         e2e_step(1)
         torch.cuda.synchronize()
@@ -884,6 +895,7 @@ def gpu_arm(args):
             te = float(tt.item())
         e2e = {"value": world * cells * args.e2e_steps / te / 1e9, "unit": "Gcell-updates/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+               "host_link_probe_gbs": link_gbs,
                "path": "per step: cf_write_state_async(whole state in the reference layout, f16 or BF16 "
                        "pigment slots, pinned host) + step + cf_read_state_async(h) "
                        "+ cf_read_color_async; two films alternate on two streams, uploads one after the "

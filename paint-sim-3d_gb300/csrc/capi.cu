@@ -4,6 +4,7 @@
 // reference's buffers of Film::new, src/film/mod.rs:586-628, in the same
 // layout) plus the device-resident params and stats.  All entry points return
 // cf_status; CUDA errors are caught and reported through cf_last_error.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -167,6 +168,53 @@ cf_status cf_pack_params(const cf_settings* s, uint32_t w, uint32_t h, float fra
 
 }  // extern "C"
 
+// cuTensorMapEncodeTiled, found through the runtime (the library does not
+// link the driver library itself); null where the driver does not offer it.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// The flow tile's descriptors (cfk::FlowMap order): h, m and the front
+// offsets as 24 x 24 boxes of 4-byte cells, the rheology planes as 24 x 24
+// boxes of f32 or 32 x 24 boxes of bf16; zero fill outside the grid.  Each
+// row pitch must be a multiple of 16 bytes, and the grid at least one box:
+// returns false otherwise (the tile then stages with plain loads).
+static bool encode_flow_maps(const cfk::Film& F, int precision, CUtensorMap maps[cfk::FLOW_MAPS]) {
+  EncodeTiledFn enc = encode_tiled();
+  const bool b16 = precision == CF_PREC_BF16;
+  const size_t rb = b16 ? 2 : 4;
+  if (!enc || F.w < 32 || F.h < 24 || (F.w * 4u) % 16u != 0u || (F.w * rb) % 16u != 0u) return false;
+  auto one = [&](CUtensorMap* m, void* base, CUtensorMapDataType t, size_t esz, cuuint32_t box_w) {
+    const cuuint64_t dims[2] = {F.w, F.h};
+    const cuuint64_t strides[1] = {(cuuint64_t)F.w * esz};
+    const cuuint32_t box[2] = {box_w, 24};
+    const cuuint32_t es[2] = {1, 1};
+    return enc(m, t, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  const CUtensorMapDataType rt = b16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const cuuint32_t rw = b16 ? 32 : 24;
+  return one(&maps[cfk::MAP_H], F.hh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 24) &&
+         one(&maps[cfk::MAP_M], F.m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 24) &&
+         one(&maps[cfk::MAP_DELTA], F.delta, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, 24) &&
+         one(&maps[cfk::MAP_MU], F.mu, rt, rb, rw) && one(&maps[cfk::MAP_TAU], F.tau, rt, rb, rw) &&
+         one(&maps[cfk::MAP_N], F.nn, rt, rb, rw);
+}
+
 // The device planes of a film (n cells, nt tiles) in arena order; add(p, bytes)
 // receives each plane's pointer slot and size.
 template <class Add>
@@ -181,7 +229,8 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, bool 
   add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
   add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n);
   add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
-  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n); add((void**)&F.dry_shaded, n);
+  add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n); add((void**)&F.shade_state, n);
+  add((void**)&F.spec, 64 * n);
   add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
   if (cg) {  // implicit hydrostatic step (settings.implicit_hydro)
     add((void**)&F.cg_m, 16 * n);
@@ -201,7 +250,8 @@ cf_status cf_film_bytes(uint32_t w, uint32_t h, int32_t precision, uint64_t* byt
   cfk::Film F{};
   size_t total = 0;
   carve_planes(F, n, nt, precision, false, [&](void**, size_t b) { total += (b + 255) & ~(size_t)255; });
-  total += sizeof(DevParams) + sizeof(DevStats) + sizeof(float) * 528 + 2 * sizeof(cfk::Film) + sizeof(uint2) * nt;
+  total += sizeof(DevParams) + sizeof(DevStats) + sizeof(float) * 528 + 2 * sizeof(cfk::Film) + sizeof(uint2) * nt +
+           sizeof(CUtensorMap) * cfk::FLOW_MAPS;
   *bytes = total;
   return CF_OK;
 }
@@ -263,6 +313,19 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
   F.all_active = s->all_active ? 1u : 0u;
   F.P = f->d_params; F.stats = f->d_stats;
   F.pigtab = f->d_tables; F.cmf = f->d_tables + 480;
+  {  // tensor-load descriptors of the flow tile's planes, where the pitch allows
+    alignas(64) CUtensorMap maps[cfk::FLOW_MAPS];
+    F.tmap = nullptr;
+    if (encode_flow_maps(F, precision, maps)) {
+      if (cudaMalloc(&f->d_tmaps, sizeof(maps)) != cudaSuccess ||
+          cudaMemcpy(f->d_tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice) != cudaSuccess) {
+        f->err = "cudaMalloc tensor maps";
+        cudaGetLastError();
+        return bail(CF_ERR_OUT_OF_MEMORY);
+      }
+      F.tmap = f->d_tmaps;
+    }
+  }
   {  // the film's own packed view (see solo_view)
     cfk::Film rec[2] = {F, F};
     std::swap(rec[1].sh, rec[1].sh2);
@@ -356,6 +419,7 @@ cf_status cf_destroy(cf_film* f) {
   if (f->h_params) cudaFreeHost(f->h_params);
   if (f->params_ev) cudaEventDestroy(f->params_ev);
   if (f->d_recs) cudaFree(f->d_recs);
+  if (f->d_tmaps) cudaFree(f->d_tmaps);
   if (f->d_tiles) cudaFree(f->d_tiles);
   if (f->d_deps) cudaFree(f->d_deps);
   if (f->d_dep_tiles) cudaFree(f->d_dep_tiles);
@@ -368,7 +432,7 @@ cf_status cf_set_tables(cf_film* f, const float* pigtab, const float* cmf) {
   if (!f || !pigtab || !cmf) return fail(f, CF_ERR_INVALID_ARG, "cf_set_tables: null");
   CUDA_TRY(f, cudaMemcpy(f->d_tables, pigtab, sizeof(float) * 480, cudaMemcpyHostToDevice));
   CUDA_TRY(f, cudaMemcpy(f->d_tables + 480, cmf, sizeof(float) * 48, cudaMemcpyHostToDevice));
-  CUDA_TRY(f, cudaMemset(f->F.dry_shaded, 0, f->n));  // dry colours depend on the CMF table
+  CUDA_TRY(f, cudaMemset(f->F.shade_state, 0, f->n));  // dry colours depend on the CMF table
   return CF_OK;
 }
 
@@ -786,6 +850,10 @@ cf_status cf_get_stats(cf_film* f, cf_stats* out) {
   out->nan_cells = ds.nan_cells;
   out->wet_cells = ds.wet_cells;
   out->launches = f->launches;
+  if (ds.tma_timeouts != 0u) {  // a flow tile's staged loads never arrived: its fluxes were not computed
+    f->err = "cf_get_stats: " + std::to_string(ds.tma_timeouts) + " flow tile(s) timed out waiting for their loads";
+    return CF_ERR_TIMEOUT;
+  }
   return CF_OK;
 }
 
@@ -897,7 +965,7 @@ cf_status cf_debug_write(cf_film* f, const char* name, const void* host, size_t 
   PlaneRef r;
   if (!find_plane(f, name, r) || r.bytes != bytes) return fail(f, CF_ERR_INVALID_ARG, "plane name or size");
   CUDA_TRY(f, cudaDeviceSynchronize());
-  CUDA_TRY(f, cudaMemset(f->F.dry_shaded, 0, f->n));  // any plane may feed a colour
+  CUDA_TRY(f, cudaMemset(f->F.shade_state, 0, f->n));  // any plane may feed a colour
   std::string n(name);
   if (n == "strata_pig" || n == "strata_pig2") {
     void* tmp = nullptr;

@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(256) k_deposit_lay(cfk::Film F, DepTables D, c
     F.tile_moved[(uint32_t)(i >> 4) + (uint32_t)(j >> 4) * F.tw] = 1u;  // mark_moved
     stack_compact(s, P.misc[0]);
     stack_store<MODE>(F, F.sh, F.scu, F.pig, c, s);
-    F.dry_shaded[c] = 0u;
+    F.shade_state[c] = SHADE_NONE;
     // The next cure reads the composition aggregates of the stack instead of
     // the stack itself: refresh them from the strata as stored (rounded), as
     // the strata pass does for the cells it writes.

@@ -8,6 +8,7 @@
 // plane, reference layout) that every kernel receives by value.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -66,6 +67,7 @@ struct DevStats {
   unsigned long long nan_cells;
   float last_dt;
   uint32_t full_count;   // entries of Film::full_list (cells of the strata full path)
+  uint32_t tma_timeouts; // tiles whose staged loads did not arrive within the wait limit (0 unless faulty)
 };
 
 template <int MODE> struct Prec;
@@ -125,7 +127,8 @@ struct Film {
   uint32_t* tile_moved;
   int32_t* fill_src;
   uint32_t* fflags;  // bit f: strata_split wrote a nonzero acc_s face f this frame
-  uint8_t* dry_shaded;  // 1: color holds the colour of a dry cell for the current sub_refl, m and cmf
+  uint8_t* shade_state;  // SHADE_*: what of a cell's colour is still current (below)
+  float4* spec;          // composite spectrum of a wet cell (SHADE_WET): band 4q+e at chunk q*n + c, component e
   uint32_t* full_list;  // cells of the strata full path (DevStats::full_count)
   uint32_t* fill_list;  // strata fill candidates (DevStats::fill_count)
   // implicit CG planes (null when the film's settings turn the implicit
@@ -140,7 +143,25 @@ struct Film {
   uint32_t all_active;      // keep every tile active (settings.all_active)
   const float* pigtab;  // 12 x 40
   const float* cmf;     // 16 x 3
+  // TMA descriptors of the planes a flow tile stages (FLOW_MAPS of them, in
+  // that order), 64-byte aligned in device memory; null where the grid's row
+  // pitch is not a multiple of 16 bytes (the tile then loads them itself)
+  const CUtensorMap* tmap;
 };
+// Film::shade_state of a cell.  The KM shade of a wet cell composites each
+// stratum over the substrate (the composite spectrum depends on the strata's
+// thicknesses and pigments, the substrate reflectance and the pigment
+// table), then applies the surface correction, whose wetness follows the top
+// stratum's cure (which ages every frame).  SHADE_WET keeps the composite
+// spectrum in Film::spec, valid for the cell's current thicknesses and
+// pigments: the strata pass reuses it while the thicknesses it computes are
+// bit for bit the current ones, and redoes only the surface correction.
+// Every other writer of a cell's strata, pigments or substrate resets the
+// state to SHADE_NONE.  SHADE_DRY: the colour holds the dry cell's colour,
+// which depends only on the substrate, the relief and the CMF table.
+constexpr uint8_t SHADE_NONE = 0, SHADE_DRY = 1, SHADE_WET = 2;
+// Planes staged by the flow kernel's tensor loads, in Film::tmap order.
+enum FlowMap { MAP_H = 0, MAP_M, MAP_DELTA, MAP_MU, MAP_TAU, MAP_N, FLOW_MAPS };
 
 __device__ __forceinline__ uint32_t idx(const Film& F, int i, int j) { return (uint32_t)j * F.w + (uint32_t)i; }
 __device__ __forceinline__ bool in_grid(const Film& F, int i, int j) {
@@ -519,10 +540,12 @@ struct FaceOut {
   float q, y, up, n;
 };
 
+// Where face() reads the plug mobility tmp of its two cells: a pair source
+// from PtGlobal / PtTile below (tmp(false) = cell a, tmp(true) = cell b).
 // film.wgsl:297-372 (face between cell a and neighbour b)
-template <int MODE>
-__device__ FaceOut face(const Film& F, const DevParams& D, uint32_t ca, uint32_t cb, float2 gcap, float2 ghyd,
-                        float2 gtilt, bool diag, float2 fd) {
+template <int MODE, class Pair>
+__device__ FaceOut face(const Film& F, const DevParams& D, const Pair& pt, uint32_t ca, uint32_t cb, float2 gcap,
+                        float2 ghyd, float2 gtilt, bool diag, float2 fd) {
   const cf_params& P = D.p;
   FaceOut out = {0.f, 0.f, 0.f, 0.f};
   float ha = F.hh[ca], hb = F.hh[cb];
@@ -543,11 +566,9 @@ __device__ FaceOut face(const Film& F, const DevParams& D, uint32_t ca, uint32_t
     shape = front_shape(F, P, dry, n) * wet_gain(n);
     if (shape <= 0.f) return out;
   }
-  float rax = rmu<MODE>(F, ca), ray = rtau<MODE>(F, ca);
-  float rbx = rmu<MODE>(F, cb), rby = rtau<MODE>(F, cb);
+  float ray = rtau<MODE>(F, ca), rby = rtau<MODE>(F, cb);
   float wa = ha / (ha + hb);
   float wb = 1.0f - wa;
-  float mu = expf(wa * logf(fmaxf(rax, 1e-4f)) + wb * logf(fmaxf(rbx, 1e-4f)));
   float ty = wa * ray + wb * rby;
   float na = rn<MODE>(F, ca), nb = rn<MODE>(F, cb);
   float nf = na == nb ? na : wa * na + wb * nb;
@@ -568,16 +589,24 @@ __device__ FaceOut face(const Film& F, const DevParams& D, uint32_t ca, uint32_t
   float gmag = sqrtf(gg.x * gg.x + gg.y * gg.y);
   float ydep = hf;  // yield_depth (film.wgsl:89-92)
   if (ty > 0.f) ydep = gg.x >= 0.f ? ha : hb;
-  float qq, qy, qup;
-  hb_flux(gmag, ydep, mu, ty, nf, qq, qy, qup);
+  float qq = 0.f, qy = 0.f, qup = 0.f;
+  // hb_flux gives zero, without reading mu, for a face with no gradient or
+  // below its yield stress (y = ydep - ty / |g| <= 0): the log-mean viscosity
+  // (film.wgsl:326, an exp and two logs) is evaluated only where it is used
+  if (!(gmag < 1e-9f || ydep <= 0.f) && fmaxf(ydep - ty / gmag, 0.f) > 0.f) {
+    const float rax = rmu<MODE>(F, ca), rbx = rmu<MODE>(F, cb);
+    const float mu = expf(wa * logf(fmaxf(rax, 1e-4f)) + wb * logf(fmaxf(rbx, 1e-4f)));
+    hb_flux(gmag, ydep, mu, ty, nf, qq, qy, qup);
+  }
   float meff = qq > 0.f ? qq / fmaxf(gmag, 1e-9f) : 0.f;
   float mtilt = meff;
   if (ty > 0.f) {  // plug_mobility (film.wgsl:51-56)
     float gb = sqrtf(gtilt.x * gtilt.x + gtilt.y * gtilt.y);
     if (gb < 1e-6f) mtilt = 0.f;
     else {
-      uint32_t up = gtilt.x >= 0.f ? ca : cb;
-      mtilt = F.tmp[up] * F.hh[up] / gb;
+      const bool ub = !(gtilt.x >= 0.f);
+      uint32_t up = ub ? cb : ca;
+      mtilt = pt.tmp(ub) * F.hh[up] / gb;
     }
   }
   if (meff <= 0.f && mtilt <= 0.f) return out;
@@ -621,12 +650,54 @@ __device__ __forceinline__ float2 pres_wet(const Film& F, int i, int j, float2 f
   return make_float2(fb.x, p.y);
 }
 
+// Sources of the pressures (laplacian) and plug mobilities (plug) the face
+// fluxes read.  PtGlobal reads the film's planes, as the dispatches of the
+// reference leave them; PtTile reads the flow kernel's shared memory, where
+// the tile and its 1-cell ring were evaluated just before (cells of the ring
+// in inactive tiles hold the planes' values, as the reference leaves them).
+struct PtGlobal {
+  const Film& F;
+  struct Pair {
+    const float* t;
+    uint32_t a, b;
+    __device__ __forceinline__ float tmp(bool bsel) const { return t[bsel ? b : a]; }
+  };
+  __device__ __forceinline__ float2 pres(int i, int j) const { return pres_at(F, i, j); }
+  __device__ __forceinline__ float2 pwet(int i, int j, float2 fb) const { return pres_wet(F, i, j, fb); }
+  __device__ __forceinline__ Pair pair(int, int, uint32_t ca, int, int, uint32_t cb) const { return {F.tmp, ca, cb}; }
+};
+// Shared-memory boxes of a flow tile: pres and tmp on 18 x 18 cells from
+// (i0 - 1, j0 - 1), the staged h on 24 x 24 cells from (i0 - 4, j0 - 4).
+struct PtTile {
+  const Film& F;
+  const float2* sp;
+  const float* st;
+  const float* sh;
+  int i0, j0;
+  struct Pair {
+    const float* t;
+    int a, b;
+    __device__ __forceinline__ float tmp(bool bsel) const { return t[bsel ? b : a]; }
+  };
+  __device__ __forceinline__ int at18(int i, int j) const { return (j - j0 + 1) * 18 + (i - i0 + 1); }
+  __device__ __forceinline__ float2 pres(int i, int j) const { return sp[at18(refl_i(F, i), refl_j(F, j))]; }
+  __device__ __forceinline__ float2 pwet(int i, int j, float2 fb) const {
+    const int ri = refl_i(F, i), rj = refl_j(F, j);
+    const float2 p = sp[at18(ri, rj)];
+    if (sh[(rj - j0 + 4) * 24 + (ri - i0 + 4)] > 0.f) return p;
+    return make_float2(fb.x, p.y);
+  }
+  __device__ __forceinline__ Pair pair(int i, int j, uint32_t, int x, int y, uint32_t) const {
+    return {st, at18(i, j), at18(x, y)};
+  }
+};
+
 // film.wgsl:375-446, face k in {0: +x, 1: +y, 2: +x+y, 3: +x-y}.  The
 // direction only selects the neighbour, the pressure-gradient stencil, the
 // tilt components and the weight; face() then runs once, so a kernel holds a
 // single copy of it.
-template <int MODE>
-__device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k) {
+template <int MODE, class PT>
+__device__ FaceOut face_k(const Film& F, const DevParams& D, const PT& pt, int i, int j, int k) {
   const cf_params& P = D.p;
   FaceOut z = {0.f, 0.f, 0.f, 0.f};
   const float s2 = 0.70710678f;
@@ -636,7 +707,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
   if (!(in_grid(F, x, y) && cell_active(F, x, y))) return z;
   const uint32_t c = idx(F, i, j), cb = idx(F, x, y);
   if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;  // face() is zero on a dry pair
-  const float2 p00 = pres_at(F, i, j), pb = pres_at(F, x, y);
+  const float2 p00 = pt.pres(i, j), pb = pt.pres(x, y);
   const float2 gxy = make_float2(P.phys[0] * P.g[0], P.phys[0] * P.g[1]);
   float2 gcap, ghyd, gt, fd;
   float wgt;
@@ -644,8 +715,8 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
     // normal gradient across the face, tangential one from the 4 cells beside it
     const int ti = k == 0 ? 0 : 1, tj = k == 0 ? 1 : 0;
     const float2 gm = make_float2(-(pb.x - p00.x) * P.inv_dx, -(pb.y - p00.y) * P.inv_dx);
-    const float2 a = pres_wet(F, i + ti, j + tj, p00), b = pres_wet(F, x + ti, y + tj, pb);
-    const float2 cc = pres_wet(F, i - ti, j - tj, p00), d = pres_wet(F, x - ti, y - tj, pb);
+    const float2 a = pt.pwet(i + ti, j + tj, p00), b = pt.pwet(x + ti, y + tj, pb);
+    const float2 cc = pt.pwet(i - ti, j - tj, p00), d = pt.pwet(x - ti, y - tj, pb);
     const float2 pt = make_float2(a.x + b.x - cc.x - d.x, a.y + b.y - cc.y - d.y);
     const float2 gtt = make_float2(-pt.x * 0.25f * P.inv_dx, -pt.y * 0.25f * P.inv_dx);
     gcap = make_float2(gm.x, gtt.x);
@@ -655,7 +726,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
     wgt = W_AXIS;
   } else {
     const float2 ga = make_float2(-(pb.x - p00.x) * P.inv_dx * s2, -(pb.y - p00.y) * P.inv_dx * s2);
-    const float2 pa = pres_wet(F, i + 1, j, p00), pc = pres_wet(F, i, j + dj, pb);
+    const float2 pa = pt.pwet(i + 1, j, p00), pc = pt.pwet(i, j + dj, pb);
     const float2 gp = make_float2(-(pa.x - pc.x) * P.inv_dx * s2, -(pa.y - pc.y) * P.inv_dx * s2);
     const float hs = P.ein[3];
     const bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j + dj)] > hs;
@@ -667,7 +738,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, int i, int j, int k
     fd = make_float2(s2, k == 2 ? s2 : -s2);
     wgt = W_DIAG_FLUX;
   }
-  FaceOut f = face<MODE>(F, D, c, cb, gcap, ghyd, gt, diag, fd);
+  FaceOut f = face<MODE>(F, D, pt.pair(i, j, c, x, y, cb), c, cb, gcap, ghyd, gt, diag, fd);
   f.q *= wgt;
   return f;
 }

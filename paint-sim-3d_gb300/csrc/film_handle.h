@@ -38,6 +38,7 @@ struct cf_film {
   // the film's own packed view: its record as created and with the strata
   // generations swapped, and a table of its tiles
   cfk::Film* d_recs = nullptr;
+  CUtensorMap* d_tmaps = nullptr;  // the flow tile's tensor-load descriptors (cfk::FLOW_MAPS), or none
   uint2* d_tiles = nullptr;
   float4* sh_created = nullptr;  // F.sh at create: tells which record is current
   // deposits for the next frame (cf_upload_deposits)

@@ -27,6 +27,7 @@
 #include "film_kernels.h"
 #include "strata_device.cuh"
 #include "strata_lane.cuh"
+#include "tma.cuh"
 
 namespace cfk {
 
@@ -164,6 +165,7 @@ static __device__ __noinline__ void cure_commit(const Film& F, const cf_params& 
   set_rheo<MODE>(F, c, mu, ty, n);
   stack_store<MODE>(F, F.sh, F.scu, F.pig, c, s);
   F.agg[c] = agg;
+  F.shade_state[c] = SHADE_NONE;  // strata and substrate changed
 }
 // cure.wgsl:119-159 (full grid).  The pigment part of the composition comes
 // from agg (written by the last strata pass); the stack is only read when
@@ -368,6 +370,7 @@ __device__ __forceinline__ void backfill(const Film& F, uint32_t c, uint32_t src
   float4 cs = F.scu[src];
   float cv = ks == 0 ? cs.x : (ks == 1 ? cs.y : (ks == 2 ? cs.z : cs.w));
   F.scu[c] = make_float4(cv, 0.f, 0.f, 0.f);
+  F.shade_state[c] = SHADE_NONE;  // new strata and pigments
 }
 
 // film.wgsl:539-561, 803-863
@@ -703,7 +706,227 @@ __device__ __forceinline__ void fluxes_tile(const Film& F, TileId T) {
   const DevParams& D = *F.P;
   float* fl = reinterpret_cast<float*>(F.flux);
   tile_faces_each(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
-    fl[4 * (size_t)fc + k] = face_k<MODE>(F, D, fi, fj, k).q;
+    fl[4 * (size_t)fc + k] = face_k<MODE>(F, D, PtGlobal{F}, fi, fj, k).q;
+  });
+}
+
+// ---- the flow tile: laplacian + plug + fluxes of one substep, fused ----
+// The reference's dispatches laplacian -> plug -> fluxes (film.wgsl:16-87,
+// 448-455) pass the pressures and plug mobilities of every cell through
+// device memory.  A flow block does the three for one 16x16 tile: it stages
+// h, m, the front offsets and the rheology of the tile and a 4-cell halo in
+// shared memory (tensor loads where the film has descriptors), evaluates the
+// surface levels on the tile + 2 rings, the pressures and plug mobilities of
+// the tile + 1 ring (what the faces read), then the faces.  Each value is the
+// expression the separate kernels evaluate, so the fluxes are the separate
+// dispatches' to rounding.  The plug mobilities of the tile go to the tmp
+// plane (strata_split reads the last substep's); the pressures stay on chip:
+// laplacian is dispatched again before strata_split, and no other kernel
+// reads them in between.
+constexpr int FB = 24;                 // staged box: tile + 4 cells each side
+constexpr uint32_t FLOW_WAIT_POLLS = 1u << 22;
+struct FlowSmem {
+  float h[FB * FB];                    // box origin (i0 - 4, j0 - 4)
+  float m[FB * FB];
+  uint32_t dl[FB * FB];
+  uint32_t rh[3][FB * FB];             // mu, tau, n: f32 24 x 24, or bf16 32 x 24 from (i0 - 8, j0 - 4)
+  float su[20 * 20];                   // surface levels, origin (i0 - 2, j0 - 2)
+  float2 pres[18 * 18];                // origin (i0 - 1, j0 - 1)
+  float tmp[18 * 18];
+  float2 qm[FB * FB];                  // plug flux q and mass h of the window cells
+  uint8_t yl[FB * FB];
+  TileFaces faces;
+  uint64_t bar;
+};
+template <int MODE>
+__device__ __forceinline__ float staged_rh(const FlowSmem& S, int plane, int b) {
+  if constexpr (MODE == CF_PREC_BF16) {
+    const int bx = b % FB, by = b / FB;
+    return b16_to_f(reinterpret_cast<const uint16_t*>(S.rh[plane])[by * 32 + bx + 4]);
+  } else {
+    return __uint_as_float(S.rh[plane][b]);
+  }
+}
+// The tile's box of the six planes into shared memory: tensor loads when the
+// film has descriptors, else loads by the block's threads (zero outside the
+// grid, as the tensor loads fill).  Returns false (counted in the film's
+// stats) when the tensor loads did not arrive within the wait limit.
+template <int MODE>
+__device__ __forceinline__ bool flow_stage(const Film& F, FlowSmem& S, int i0, int j0, int tid) {
+  constexpr bool B16 = MODE == CF_PREC_BF16;
+  if (F.tmap != nullptr) {
+    if (tid == 0) {
+      mbar_init(&S.bar, 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const uint32_t rb = B16 ? 32 * FB * 2 : FB * FB * 4;
+      mbar_arrive_expect_tx(&S.bar, 3u * FB * FB * 4u + 3u * rb);
+      tma_load_2d(S.h, F.tmap + MAP_H, i0 - 4, j0 - 4, &S.bar);
+      tma_load_2d(S.m, F.tmap + MAP_M, i0 - 4, j0 - 4, &S.bar);
+      tma_load_2d(S.dl, F.tmap + MAP_DELTA, i0 - 4, j0 - 4, &S.bar);
+      const int rx = B16 ? i0 - 8 : i0 - 4;
+      tma_load_2d(S.rh[0], F.tmap + MAP_MU, rx, j0 - 4, &S.bar);
+      tma_load_2d(S.rh[1], F.tmap + MAP_TAU, rx, j0 - 4, &S.bar);
+      tma_load_2d(S.rh[2], F.tmap + MAP_N, rx, j0 - 4, &S.bar);
+    }
+    const bool arrived = __syncthreads_and(mbar_wait_bounded(&S.bar, 0, FLOW_WAIT_POLLS));
+    if (!arrived) {
+      if (tid == 0) {
+        atomicAdd(&F.stats->tma_timeouts, 1u);
+        mbar_wait_bounded(&S.bar, 0, FLOW_WAIT_POLLS);  // let loads still in flight land
+      }
+      __syncthreads();
+      return false;
+    }
+    __syncthreads();
+    if (tid == 0) mbar_inval(&S.bar);
+    return true;
+  }
+  for (int q = tid; q < FB * FB; q += 256) {
+    const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
+    const bool in = in_grid(F, x, y);
+    const uint32_t c = in ? idx(F, x, y) : 0u;
+    S.h[q] = in ? F.hh[c] : 0.f;
+    S.m[q] = in ? F.m[c] : 0.f;
+    S.dl[q] = in ? F.delta[c] : 0u;
+  }
+  if constexpr (B16) {
+    for (int q = tid; q < 32 * FB; q += 256) {
+      const int x = i0 - 8 + q % 32, y = j0 - 4 + q / 32;
+      const bool in = in_grid(F, x, y);
+      const uint32_t c = in ? idx(F, x, y) : 0u;
+      const uint16_t* pl[3] = {(const uint16_t*)F.mu, (const uint16_t*)F.tau, (const uint16_t*)F.nn};
+#pragma unroll
+      for (int r = 0; r < 3; ++r) reinterpret_cast<uint16_t*>(S.rh[r])[q] = in ? pl[r][c] : (uint16_t)0;
+    }
+  } else {
+    for (int q = tid; q < FB * FB; q += 256) {
+      const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
+      const bool in = in_grid(F, x, y);
+      const uint32_t c = in ? idx(F, x, y) : 0u;
+      const float* pl[3] = {(const float*)F.mu, (const float*)F.tau, (const float*)F.nn};
+#pragma unroll
+      for (int r = 0; r < 3; ++r) S.rh[r][q] = in ? __float_as_uint(pl[r][c]) : 0u;
+    }
+  }
+  __syncthreads();
+  return true;
+}
+template <int MODE, bool CLEAR>
+__device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
+  __shared__ __align__(128) FlowSmem S;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const DevParams& D = *F.P;
+  const cf_params& P = D.p;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
+  if (!flow_stage<MODE>(F, S, i0, j0, tid)) return;
+  const float gb = P.phys[0] * D.gxy;
+  auto box = [&](int x, int y) { return (y - j0 + 4) * FB + (x - i0 + 4); };
+  // surface levels (film.wgsl:147-151) of the tile + 2 rings, reflected at the
+  // grid's edges as the laplacian reads them
+  for (int q = tid; q < 20 * 20; q += 256) {
+    const int b = box(refl_i(F, i0 - 2 + q % 20), refl_j(F, j0 - 2 + q / 20));
+    const float hv = S.h[b];
+    int ox, oy;
+    unpack_off(S.dl[b], ox, oy);
+    S.su[q] = S.h[b] + S.m[b] - (hv > 0.f ? hold_level(P, off_len(ox, oy)) : 0.f);
+  }
+  // plug: the HB flux and mass of every window cell (film.wgsl:58-87); on a
+  // flat canvas (gb < 1e-6) every plug mobility is 0 and none is needed
+  if (gb >= 1e-6f) {
+    for (int q = tid; q < FB * FB; q += 256) {
+      const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
+      float qq = 0.f, mass = 0.f;
+      uint8_t yl = 0;
+      const float hn = S.h[q];
+      if (in_grid(F, x, y) && hn > 0.f) {
+        const float rx = staged_rh<MODE>(S, 0, q), ry = staged_rh<MODE>(S, 1, q);
+        yl = (uint8_t)(1u | (ry > 0.f ? 2u : 0u));
+        float yy, up;
+        hb_flux(gb, hn, fmaxf(rx, 1e-4f), ry, staged_rh<MODE>(S, 2, q), qq, yy, up);
+        mass = hn;
+      }
+      S.qm[q] = make_float2(qq, mass);
+      S.yl[q] = yl;
+    }
+  }
+  if (tid < 4) S.faces.count[tid] = 0u;
+  __syncthreads();
+  // pressures (film.wgsl:16-42) and plug mobilities of the tile + 1 ring;
+  // ring cells in inactive tiles keep the planes' values
+  for (int q = tid; q < 18 * 18; q += 256) {
+    const int px = q % 18, py = q / 18, x = i0 - 1 + px, y = j0 - 1 + py;
+    if (!in_grid(F, x, y)) continue;
+    const uint32_t c = idx(F, x, y);
+    if (!cell_active(F, x, y)) {
+      S.pres[q] = F.pres[c];
+      S.tmp[q] = F.tmp[c];
+      continue;
+    }
+    const int b = box(x, y);
+    const float hv = S.h[b];
+    const float* u = &S.su[(py + 1) * 20 + px + 1];
+    const float u0 = u[0];
+    float pl = 0.f;
+    const float ax = u[-1] + u[1] + u[-20] + u[20];
+    const float dg = u[-21] + u[-19] + u[19] + u[21];
+    const float l = (W_AXIS * ax + W_DIAG_LAP * dg - (4.0f * W_AXIS + 4.0f * W_DIAG_LAP) * u0) * P.inv_dx * P.inv_dx;
+    if (hv > 0.f) {
+      int ox, oy;
+      unpack_off(S.dl[b], ox, oy);
+      const float d = off_len(ox, oy);
+      if (d <= 3.0f) {
+        const float2 n = F.fnorm[c];
+        if (n.x * n.x + n.y * n.y > 0.5f) pl = line_pressure(F, P, x, y) * expf(-(d - 1.0f) * 0.7f);
+      }
+    }
+    S.pres[q] = make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * u0 + pl);
+    float t = 0.f;
+    if (hv > 0.f && gb >= 1e-6f) {
+      float sum = 0.f, mass = 0.f;
+      uint32_t fl = 0u;
+      for (int dy = 0; dy < 7; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 7; ++dx) {
+          const int w = (py + dy) * FB + px + dx;
+          const float2 v = S.qm[w];
+          fl |= S.yl[w];
+          sum += v.x;
+          mass += v.y;
+        }
+      if ((fl & 2u) && mass > 0.f) t = sum / mass;
+    }
+    S.tmp[q] = t;
+  }
+  __syncthreads();
+  // the tile's own cells: clear_acc (film.wgsl:1427-1434) with the first
+  // substep, the plug mobility to the plane, the flux zeroed, the live faces
+  // listed by direction
+  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
+  const bool in = i < (int)F.w && j < (int)F.h;
+  const uint32_t c = in ? idx(F, i, j) : 0u;
+  const float hc = in ? S.h[box(i, j)] : 0.f;
+  if (in) {
+    if (CLEAR) {
+      F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+      F.h_frame[c] = hc;
+    }
+    F.tmp[c] = S.tmp[(threadIdx.y + 1) * 18 + threadIdx.x + 1];
+    F.flux[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int x = i + FACE_DI[k], y = j + FACE_DJ[k];
+    tile_faces_add(S.faces, k, in && in_grid(F, x, y) && cell_active(F, x, y) && 0.5f * (hc + S.h[box(x, y)]) > 0.f);
+  }
+  __syncthreads();
+  const PtTile pt{F, S.pres, S.tmp, S.h, i0, j0};
+  float* fl = reinterpret_cast<float*>(F.flux);
+  tile_faces_each(F, T, S.faces, [&](int k, int fi, int fj, uint32_t fc) {
+    fl[4 * (size_t)fc + k] = face_k<MODE>(F, D, pt, fi, fj, k).q;
   });
 }
 
@@ -734,7 +957,7 @@ __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
   const DevParams& D = *F.P;
   tile_faces_each(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
     const float a = sel4(F.acc[fc], k);
-    const FaceOut ff = face_k<MODE>(F, D, fi, fj, k);
+    const FaceOut ff = face_k<MODE>(F, D, PtGlobal{F}, fi, fj, k);
     const uint32_t cb = idx(F, fi + FACE_DI[k], fj + FACE_DJ[k]);
     const uint32_t cu = a < 0.f ? cb : fc;
     const float4 o = band_split(F, cu, 0.5f * (F.hh[fc] + F.hh[cb]), ff.y, ff.up, a, ff.n);
@@ -775,13 +998,18 @@ struct FastShade {
 // renormalised to h into the next generation of thicknesses, its pigments left
 // in place (this path never changes them).  Inactive tiles carry their strata
 // over and are shaded, as the reference's full-grid shade does.  Active wet
-// cells left without strata become strata_fill candidates.  Returns whether
-// the cell needs the shade (shade.wgsl:28-84) and composition aggregates,
-// whose inputs it leaves in the block's FastShade slot (the tile function
-// shades it by lane or by half-warp).
+// cells left without strata become strata_fill candidates.  Returns what the
+// cell's shade (shade.wgsl:28-84) needs, with its inputs left in the block's
+// FastShade slot: FAST_NOTHING (a dry cell whose colour is current, or a cell
+// of the full path), FAST_SHADE (the composite spectrum, the composition
+// aggregates and the colour: the tile function shades it by lane or by
+// half-warp) or FAST_COLOR (a wet cell whose thicknesses came out bit for bit
+// the ones its cached spectrum was composited for: only the surface
+// correction, which follows the cure).
+constexpr int FAST_NOTHING = 0, FAST_SHADE = 1, FAST_COLOR = 2;
 template <int MODE>
-__device__ __forceinline__ bool strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
-                                                 uint32_t c, float hc, FastShade& sh, int tid) {
+__device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& P, TileId T, int i, int j,
+                                                uint32_t c, float hc, FastShade& sh, int tid) {
   const bool act = (F.tile_flags[T.x + T.y * F.tw] & ACTIVE) != 0u;
   // The cell's loads are issued together: strata, dry flag and, in an active
   // tile, the face flags of the cell and of the 4 neighbours whose faces
@@ -790,7 +1018,7 @@ __device__ __forceinline__ bool strata_fast_cell(const Film& F, const cf_params&
   // strata_limit alpha below 1 and does strata_update move material into or
   // out of the cell.
   float4 t4 = F.sh[c], cu = F.scu[c];
-  const uint8_t was_dry = F.dry_shaded[c];
+  const uint8_t state = F.shade_state[c];
   if (act) {
     const bool hl = i > 0, hd = j > 0, hu = j + 1 < (int)F.h;
     const uint32_t f0 = F.fflags[c], fl = hl ? F.fflags[c - 1] : 0u, fd = hd ? F.fflags[c - F.w] : 0u,
@@ -813,7 +1041,7 @@ __device__ __forceinline__ bool strata_fast_cell(const Film& F, const cf_params&
       if (hl && hd && !(fdl & 4u) && cell_active(F, i - 1, j - 1)) F.acc_s[2 * (size_t)F.n + c - F.w - 1] = z4;
       if (hl && hu && !(ful & 8u) && cell_active(F, i - 1, j + 1)) F.acc_s[3 * (size_t)F.n + c + F.w - 1] = z4;
       list_append(F.full_list, &F.stats->full_count, c);
-      return false;
+      return FAST_NOTHING;
     }
   }
   float nt[4] = {t4.x, t4.y, t4.z, t4.w};
@@ -840,17 +1068,45 @@ __device__ __forceinline__ bool strata_fast_cell(const Film& F, const cf_params&
   // A dry cell's colour depends on its substrate reflectance, its relief and
   // the CMF table only (the stack and the params enter wet cells' colour),
   // and those do not change while it stays dry: when the last shade already
-  // saw it dry, its colour is current.
-  if (hc <= 0.f) {
-    if (was_dry) return false;
-    F.dry_shaded[c] = 1u;
-  } else if (was_dry) {
-    F.dry_shaded[c] = 0u;
-  }
+  // saw it dry, its colour is current.  A wet cell's composite spectrum
+  // depends on its thicknesses, pigments and substrate: while the state says
+  // the cached one is current for the thicknesses it entered with, and it
+  // leaves with the same ones, the spectrum is reused (not in the invariant
+  // debug view, which reads the pigments).
   sh.nt[tid] = make_float4(nt[0], nt[1], nt[2], nt[3]);
   sh.cu[tid] = cu;
   sh.h[tid] = hc;
-  return true;
+  if (hc <= 0.f) {
+    if (state == SHADE_DRY) return FAST_NOTHING;
+    F.shade_state[c] = SHADE_DRY;
+    return FAST_SHADE;
+  }
+  if (state == SHADE_WET && P.flags[0] != 1u && nt[0] == t4.x && nt[1] == t4.y && nt[2] == t4.z && nt[3] == t4.w)
+    return FAST_COLOR;
+  if (state != SHADE_WET) F.shade_state[c] = SHADE_WET;  // the shade below caches the spectrum
+  return FAST_SHADE;
+}
+// The colour of a FAST_COLOR cell: its cached composite spectrum through the
+// surface correction with this frame's cure (bit for bit what CellAcc gives
+// for the same strata; the aggregates do not depend on the cure and stay).
+__device__ __forceinline__ void fast_color_cached(const Film& F, uint32_t c, const FastShade& sh, int tid) {
+  const float4 nt = sh.nt[tid], cu = sh.cu[tid];
+  float wet = 0.f, cure_top = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (sel4(nt, k) > 0.f) {
+      wet = 1.0f - sel4(cu, k);
+      cure_top = sel4(cu, k);
+    }
+  float r[16];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 v = F.spec[(size_t)q * F.n + c];
+    r[4 * q] = v.x; r[4 * q + 1] = v.y; r[4 * q + 2] = v.z; r[4 * q + 3] = v.w;
+  }
+  float rgb[3];
+  surface_rgb(sh.cm, r, wet, rgb);
+  F.color[c] = pack_color(rgb, surface_rough(cure_top, sh.h[tid], F.m[c]));
 }
 // The shade and aggregates of one cell the fast path left to shade, by its
 // own lane (CellAcc).
@@ -873,8 +1129,14 @@ __device__ __forceinline__ void fast_shade_lane(const Film& F, const cf_params& 
       acc.ssum += tk;
     }
   }
-  // the next cure reads the aggregates of wet cells only
-  if (hc > 0.f) F.agg[c] = acc.agg(P);
+  // the next cure reads the aggregates of wet cells only; a wet cell's
+  // composite spectrum is cached for the frames its strata stay as they are
+  if (hc > 0.f) {
+    F.agg[c] = acc.agg(P);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      F.spec[(size_t)q * F.n + c] = make_float4(acc.r[4 * q], acc.r[4 * q + 1], acc.r[4 * q + 2], acc.r[4 * q + 3]);
+  }
   F.color[c] = acc.color(P, sh.cm, hc, F.m[c]);
 }
 // The shade (shade.wgsl:28-84) and composition aggregates (cure.wgsl:3-48)
@@ -903,6 +1165,7 @@ __device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params&
     }
     const float4 agg = acc.agg(P);
     const ushort4 col = acc.color(H, P, sh.cm, hc, F.m[c]);
+    if (hc > 0.f) reinterpret_cast<float*>(F.spec)[((size_t)(H.q >> 2) * F.n + c) * 4 + (H.q & 3)] = acc.r;
     if (H.q == 0) {
       if (hc > 0.f) F.agg[c] = agg;  // the next cure reads the aggregates of wet cells only
       F.color[c] = col;
@@ -927,14 +1190,16 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   const cf_params& P = F.P->p;
   float hm = 0.f, mm = 1e9f;
-  bool shade = false;
+  int need = FAST_NOTHING;
   uint32_t c = 0u;
   if (i < (int)F.w && j < (int)F.h) {
     c = idx(F, i, j);
     const float hc = F.hh[c];
     if (hc > 4.0f * P.ein[3]) { hm = hc; mm = rmu<MODE>(F, c); }
-    shade = strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
+    need = strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
   }
+  if (need == FAST_COLOR) fast_color_cached(F, c, sh, tid);
+  const bool shade = need == FAST_SHADE;
   // Where at least FAST_SHADE_LANES lanes of the warp have a cell to shade,
   // each shades its own; where fewer do, the cells are shaded after the
   // tile's pass by half-warps (fast_shade_cells), which costs about 1/20 of a
@@ -1103,7 +1368,7 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     if (H.q == 0) {
       F.agg[c] = agg;
       F.color[c] = col;
-      F.dry_shaded[c] = hc <= 0.f ? 1u : 0u;
+      F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
     }
   }
 }
@@ -1169,7 +1434,7 @@ __device__ __forceinline__ void fill_list_film(const Film& F, float* lt) {
       finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
       F.agg[c] = agg;
       F.color[c] = col;
-      F.dry_shaded[c] = hc <= 0.f ? 1u : 0u;
+      F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
     }
     __syncthreads();
   }
@@ -1216,7 +1481,7 @@ __device__ __forceinline__ void fill_apply_tile(const Film& F, TileId T) {
   finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
   F.agg[c] = agg;
   F.color[c] = col;
-  F.dry_shaded[c] = hc <= 0.f ? 1u : 0u;
+  F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
 }
 
 // Aggregates and colour of the current state (after a state upload, or for
@@ -1237,7 +1502,7 @@ __device__ __forceinline__ void compose_tile(const Film& F, TileId T, int shade)
   F.agg[c] = agg;
   if (shade) {
     F.color[c] = col;
-    F.dry_shaded[c] = F.hh[c] <= 0.f ? 1u : 0u;
+    F.shade_state[c] = F.hh[c] <= 0.f ? SHADE_DRY : SHADE_NONE;
   }
 }
 
@@ -1456,6 +1721,8 @@ __global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILE plug_t
 // the occupancy hides its dependent loads
 template <int MODE>
 __global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
+template <int MODE, bool CLEAR>
+__global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILE flow_tile<MODE, CLEAR>(F, T); }
 template <int MODE>
 __global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
@@ -1571,14 +1838,14 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     n += 1 + launch_cg_step(V, MODE, s, V.implicit_iters, V.cap_implicit, st);
   }
   for (uint32_t s = 0; s < substeps; ++s) {
-    if (s == 0 && isteps == 0) kp_laplacian<true><<<nt, b, 0, st>>>(A, T, nt);
-    else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
-    kp_plug<MODE><<<nt, b, 0, st>>>(A, T, nt);
-    kp_fluxes<MODE><<<nt, b, 0, st>>>(A, T, nt);
+    // laplacian + plug + fluxes as one flow launch (with clear_acc on the
+    // frame's first)
+    if (s == 0 && isteps == 0) kp_flow<MODE, true><<<nt, b, 0, st>>>(A, T, nt);
+    else kp_flow<MODE, false><<<nt, b, 0, st>>>(A, T, nt);
     kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
     kp_apply<MODE><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
     kp_nose<<<nt, b, 0, st>>>(A, T, nt);
-    n += 6;
+    n += 4;
   }
   kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
   kp_strata_split<MODE><<<nt, b, 0, st>>>(A, T, nt);
@@ -1661,6 +1928,11 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "laplacian") kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
   else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
   else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
+  else if (n == "flow") {  // laplacian + plug + fluxes fused, as the frame runs them
+    if (mode == CF_PREC_REFERENCE) kp_flow<CF_PREC_REFERENCE, false><<<nt, b, 0, st>>>(A, T, nt);
+    else if (mode == CF_PREC_FP32) kp_flow<CF_PREC_FP32, false><<<nt, b, 0, st>>>(A, T, nt);
+    else kp_flow<CF_PREC_BF16, false><<<nt, b, 0, st>>>(A, T, nt);
+  }
   else if (n == "limiter") kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
   else if (n == "apply") CFK_LAUNCH(kp_apply, nt, dim3(16, 8), st, A, T, nt);
   else if (n == "nose") {

@@ -174,6 +174,43 @@ __device__ __forceinline__ void layer_ks_band_t(const float w[12], float scale, 
   s = s * scale;
 }
 
+// shade.wgsl:51-56 for a composite spectrum r: the surface correction
+// (Saunderson, k1 = 0.04, k2 from 0.4 dry to 0.6 wet), the CMF x D65 sums to
+// XYZ and XYZ -> linear sRGB (km.wgsl:51-62), clamped at 0.
+__device__ __forceinline__ void surface_rgb(const float* cm, const float r[16], float wt, float rgb[3]) {
+  const float k1 = 0.04f;
+  const float k2 = 0.4f * (1.0f - wt) + 0.6f * wt;
+  float X = 0.f, Y = 0.f, Z = 0.f;
+#pragma unroll
+  for (int b = 0; b < 16; ++b) {
+    const float rb = __fdividef((1.0f - k1) * (1.0f - k2) * r[b], fmaxf(1.0f - k2 * r[b], 1e-3f));  // colour is stored as f16
+    X += rb * cm[3 * b];
+    Y += rb * cm[3 * b + 1];
+    Z += rb * cm[3 * b + 2];
+  }
+  rgb[0] = fmaxf(3.2406f * X - 1.5372f * Y - 0.4986f * Z, 0.f);
+  rgb[1] = fmaxf(-0.9689f * X + 1.8758f * Y + 0.0415f * Z, 0.f);
+  rgb[2] = fmaxf(0.0557f * X - 0.2040f * Y + 1.0570f * Z, 0.f);
+}
+// shade.wgsl:57-62: the roughness from the top stratum's cure, the relief m
+// and the film height h.
+__device__ __forceinline__ float surface_rough(float cure_top, float hv, float mv) {
+  auto smooth = [](float e0, float e1, float x) {
+    float t = fminf(fmaxf((x - e0) / (e1 - e0), 0.f), 1.f);
+    return t * t * (3.0f - 2.0f * t);
+  };
+  const float painted = smooth(60e-6f, 150e-6f, mv);
+  const float ct = fmaxf(hv > 0.f ? cure_top : 0.f, painted * (1.0f - smooth(0.f, 50e-6f, hv)));
+  const float sq = sqrtf(ct);
+  float rough = 0.06f * (1.0f - sq) + 0.35f * sq;
+  if (hv <= 0.f) rough = 0.85f * (1.0f - painted) + 0.35f * painted;
+  return rough;
+}
+__device__ __forceinline__ ushort4 pack_color(const float rgb[3], float rough) {
+  return make_ushort4((unsigned short)f_to_h16(rgb[0]), (unsigned short)f_to_h16(rgb[1]),
+                      (unsigned short)f_to_h16(rgb[2]), (unsigned short)f_to_h16(rough));
+}
+
 // Per-cell accumulation over the final strata, bottom to top, of
 //  - the pigment part of the rheology composition (cure.wgsl:3-48), kept as
 //    agg = (mu_base, 3 ln(1 - tf), tau_base (1 - tf)^4, n) for the next cure
@@ -281,30 +318,9 @@ struct CellAcc {
     return make_float4(mu, 3.0f * logf(1.0f - tf), ty * powf(1.0f - tf, 4.0f), nw > 0.f ? nsum / nw : P.phys[2]);
   }
   __device__ __forceinline__ ushort4 color(const cf_params& P, const float* cm, float hv, float mv) const {
-    const float k1 = 0.04f;
-    float wt = hv > 0.f ? wet : 0.f;
-    float k2 = 0.4f * (1.0f - wt) + 0.6f * wt;
-    float X = 0.f, Y = 0.f, Z = 0.f;
-#pragma unroll
-    for (int b = 0; b < 16; ++b) {
-      float rb = __fdividef((1.0f - k1) * (1.0f - k2) * r[b], fmaxf(1.0f - k2 * r[b], 1e-3f));  // colour is stored as f16
-      X += rb * cm[3 * b];
-      Y += rb * cm[3 * b + 1];
-      Z += rb * cm[3 * b + 2];
-    }
-    float rgb[3] = {3.2406f * X - 1.5372f * Y - 0.4986f * Z, -0.9689f * X + 1.8758f * Y + 0.0415f * Z,
-                    0.0557f * X - 0.2040f * Y + 1.0570f * Z};
-#pragma unroll
-    for (int q = 0; q < 3; ++q) rgb[q] = fmaxf(rgb[q], 0.f);
-    auto smooth = [](float e0, float e1, float x) {
-      float t = fminf(fmaxf((x - e0) / (e1 - e0), 0.f), 1.f);
-      return t * t * (3.0f - 2.0f * t);
-    };
-    float painted = smooth(60e-6f, 150e-6f, mv);
-    float ct = fmaxf(hv > 0.f ? cure_top : 0.f, painted * (1.0f - smooth(0.f, 50e-6f, hv)));
-    float sq = sqrtf(ct);
-    float rough = 0.06f * (1.0f - sq) + 0.35f * sq;
-    if (hv <= 0.f) rough = 0.85f * (1.0f - painted) + 0.35f * painted;
+    float rgb[3];
+    surface_rgb(cm, r, hv > 0.f ? wet : 0.f, rgb);
+    const float rough = surface_rough(cure_top, hv, mv);
     if (P.flags[0] == 1u && hv > 0.f) {  // shade.wgsl:65-82 invariant view
       if (ssum <= 0.f) { rgb[0] = 0.f; rgb[1] = 0.f; rgb[2] = 1.f; }
       else if (bad) { rgb[0] = 1.f; rgb[1] = 0.f; rgb[2] = 0.f; }
