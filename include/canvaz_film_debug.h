@@ -4,8 +4,10 @@
  * These have no counterpart in the reference's Film API; they expose the
  * scratch planes the reference keeps in wgpu buffers (pres, flux, acc, alpha,
  * delta, tmp, acc_s, alpha_s, strata_*2, h_frame, fnorm, tile flags;
- * src/film/mod.rs:586-628) so that a single dispatch can be checked against
- * a CPU oracle.  All calls are synchronous.
+ * src/film/mod.rs:586-628), and this library's own per-cell face flags
+ * ("fflags": bit f set where strata_split wrote a nonzero face f), so that a
+ * single dispatch can be checked against a CPU oracle.  All calls are
+ * synchronous.
  */
 #ifndef CANVAZ_FILM_DEBUG_H
 #define CANVAZ_FILM_DEBUG_H
@@ -32,7 +34,9 @@ cf_status cf_debug_write(cf_film* film, const char* name, const void* host, size
 
 /* Runs one dispatch of Film::encode_frame by its WGSL entry-point name
  * ("laplacian", "fluxes", "strata_update", "shade_full", ...; "deposit" lays
- * the deposits uploaded since the last frame and drops them). */
+ * the deposits uploaded since the last frame and drops them), or one of the
+ * fused kernels the frame runs: "flow" (laplacian + plug + fluxes) and
+ * "split" (laplacian + strata_split). */
 cf_status cf_debug_run(cf_film* film, const char* kernel, void* stream);
 
 /* Overwrites the device params with `params` (no re-packing). */

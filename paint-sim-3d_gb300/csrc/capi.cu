@@ -903,6 +903,7 @@ bool find_plane(cf_film* f, const std::string& n, PlaneRef& r) {
       {"strata_pig2", F.pig2, 64 * pb * N, pe}, {"sub_refl", F.refl, 32 * N, CF_ELEM_F16},
       {"color", F.color, 8 * N, CF_ELEM_F16}, {"tile_flags", F.tile_flags, 4 * nt, CF_ELEM_U32},
       {"tile_moved", F.tile_moved, 4 * nt, CF_ELEM_U32}, {"fill_src", F.fill_src, 4 * N, CF_ELEM_I32},
+      {"fflags", F.fflags, 4 * N, CF_ELEM_U32},
       {"agg", F.agg, 16 * N, CF_ELEM_F32},
   };
   for (auto& e : tab)

@@ -159,7 +159,11 @@ struct Film {
 // Every other writer of a cell's strata, pigments or substrate resets the
 // state to SHADE_NONE.  SHADE_DRY: the colour holds the dry cell's colour,
 // which depends only on the substrate, the relief and the CMF table.
-constexpr uint8_t SHADE_NONE = 0, SHADE_DRY = 1, SHADE_WET = 2;
+// SHADE_DRY2: the same, and the strata pass has written zero thicknesses and
+// cure fractions for the cell into both strata generations (it was dry in an
+// active tile two passes running), so a pass that finds it dry again has
+// nothing to read or write for it.
+constexpr uint8_t SHADE_NONE = 0, SHADE_DRY = 1, SHADE_WET = 2, SHADE_DRY2 = 3;
 // Planes staged by the flow kernel's tensor loads, in Film::tmap order.
 enum FlowMap { MAP_H = 0, MAP_M, MAP_DELTA, MAP_MU, MAP_TAU, MAP_N, FLOW_MAPS };
 

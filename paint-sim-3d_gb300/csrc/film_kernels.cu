@@ -747,12 +747,27 @@ __device__ __forceinline__ float staged_rh(const FlowSmem& S, int plane, int b) 
     return __uint_as_float(S.rh[plane][b]);
   }
 }
-// The tile's box of the six planes into shared memory: tensor loads when the
-// film has descriptors, else loads by the block's threads (zero outside the
-// grid, as the tensor loads fill).  Returns false (counted in the film's
+// Shared memory of a split block (laplacian + strata_split of one tile): the
+// staged h, m and front offsets, surface levels, pressures and the plane's
+// plug mobilities on the tile + 1 ring, the face lists and face flags.
+struct SplitSmem {
+  float h[FB * FB];
+  float m[FB * FB];
+  uint32_t dl[FB * FB];
+  float su[20 * 20];
+  float2 pres[18 * 18];
+  float tmp[18 * 18];
+  TileFaces faces;
+  uint32_t flags[256];
+  uint64_t bar;
+};
+// The tile's box of h, m and the front offsets (and with RHEO, where `rheo`
+// is set, the three rheology planes) into shared memory: tensor loads when
+// the film has descriptors, else loads by the block's threads (zero outside
+// the grid, as the tensor loads fill).  Returns false (counted in the film's
 // stats) when the tensor loads did not arrive within the wait limit.
-template <int MODE>
-__device__ __forceinline__ bool flow_stage(const Film& F, FlowSmem& S, int i0, int j0, int tid) {
+template <int MODE, bool RHEO, class Smem>
+__device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0, int tid, bool rheo = RHEO) {
   constexpr bool B16 = MODE == CF_PREC_BF16;
   if (F.tmap != nullptr) {
     if (tid == 0) {
@@ -762,14 +777,18 @@ __device__ __forceinline__ bool flow_stage(const Film& F, FlowSmem& S, int i0, i
     __syncthreads();
     if (tid == 0) {
       const uint32_t rb = B16 ? 32 * FB * 2 : FB * FB * 4;
-      mbar_arrive_expect_tx(&S.bar, 3u * FB * FB * 4u + 3u * rb);
+      mbar_arrive_expect_tx(&S.bar, 3u * FB * FB * 4u + (RHEO && rheo ? 3u * rb : 0u));
       tma_load_2d(S.h, F.tmap + MAP_H, i0 - 4, j0 - 4, &S.bar);
       tma_load_2d(S.m, F.tmap + MAP_M, i0 - 4, j0 - 4, &S.bar);
       tma_load_2d(S.dl, F.tmap + MAP_DELTA, i0 - 4, j0 - 4, &S.bar);
-      const int rx = B16 ? i0 - 8 : i0 - 4;
-      tma_load_2d(S.rh[0], F.tmap + MAP_MU, rx, j0 - 4, &S.bar);
-      tma_load_2d(S.rh[1], F.tmap + MAP_TAU, rx, j0 - 4, &S.bar);
-      tma_load_2d(S.rh[2], F.tmap + MAP_N, rx, j0 - 4, &S.bar);
+      if constexpr (RHEO) {
+        if (rheo) {
+          const int rx = B16 ? i0 - 8 : i0 - 4;
+          tma_load_2d(S.rh[0], F.tmap + MAP_MU, rx, j0 - 4, &S.bar);
+          tma_load_2d(S.rh[1], F.tmap + MAP_TAU, rx, j0 - 4, &S.bar);
+          tma_load_2d(S.rh[2], F.tmap + MAP_N, rx, j0 - 4, &S.bar);
+        }
+      }
     }
     const bool arrived = __syncthreads_and(mbar_wait_bounded(&S.bar, 0, FLOW_WAIT_POLLS));
     if (!arrived) {
@@ -792,27 +811,67 @@ __device__ __forceinline__ bool flow_stage(const Film& F, FlowSmem& S, int i0, i
     S.m[q] = in ? F.m[c] : 0.f;
     S.dl[q] = in ? F.delta[c] : 0u;
   }
-  if constexpr (B16) {
-    for (int q = tid; q < 32 * FB; q += 256) {
-      const int x = i0 - 8 + q % 32, y = j0 - 4 + q / 32;
-      const bool in = in_grid(F, x, y);
-      const uint32_t c = in ? idx(F, x, y) : 0u;
-      const uint16_t* pl[3] = {(const uint16_t*)F.mu, (const uint16_t*)F.tau, (const uint16_t*)F.nn};
+  if constexpr (RHEO) {
+    if (rheo) {
+      if constexpr (B16) {
+        for (int q = tid; q < 32 * FB; q += 256) {
+          const int x = i0 - 8 + q % 32, y = j0 - 4 + q / 32;
+          const bool in = in_grid(F, x, y);
+          const uint32_t c = in ? idx(F, x, y) : 0u;
+          const uint16_t* pl[3] = {(const uint16_t*)F.mu, (const uint16_t*)F.tau, (const uint16_t*)F.nn};
 #pragma unroll
-      for (int r = 0; r < 3; ++r) reinterpret_cast<uint16_t*>(S.rh[r])[q] = in ? pl[r][c] : (uint16_t)0;
-    }
-  } else {
-    for (int q = tid; q < FB * FB; q += 256) {
-      const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
-      const bool in = in_grid(F, x, y);
-      const uint32_t c = in ? idx(F, x, y) : 0u;
-      const float* pl[3] = {(const float*)F.mu, (const float*)F.tau, (const float*)F.nn};
+          for (int r = 0; r < 3; ++r) reinterpret_cast<uint16_t*>(S.rh[r])[q] = in ? pl[r][c] : (uint16_t)0;
+        }
+      } else {
+        for (int q = tid; q < FB * FB; q += 256) {
+          const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
+          const bool in = in_grid(F, x, y);
+          const uint32_t c = in ? idx(F, x, y) : 0u;
+          const float* pl[3] = {(const float*)F.mu, (const float*)F.tau, (const float*)F.nn};
 #pragma unroll
-      for (int r = 0; r < 3; ++r) S.rh[r][q] = in ? __float_as_uint(pl[r][c]) : 0u;
+          for (int r = 0; r < 3; ++r) S.rh[r][q] = in ? __float_as_uint(pl[r][c]) : 0u;
+        }
+      }
     }
   }
   __syncthreads();
   return true;
+}
+// Surface levels (film.wgsl:147-151) of the tile + 2 rings, reflected at the
+// grid's edges as the laplacian reads them.
+template <class Smem>
+__device__ __forceinline__ void tile_surface(const Film& F, const cf_params& P, Smem& S, int i0, int j0, int tid) {
+  for (int q = tid; q < 20 * 20; q += 256) {
+    const int b = (refl_j(F, j0 - 2 + q / 20) - j0 + 4) * FB + (refl_i(F, i0 - 2 + q % 20) - i0 + 4);
+    const float hv = S.h[b];
+    int ox, oy;
+    unpack_off(S.dl[b], ox, oy);
+    S.su[q] = S.h[b] + S.m[b] - (hv > 0.f ? hold_level(P, off_len(ox, oy)) : 0.f);
+  }
+}
+// The laplacian's pressure (film.wgsl:16-42) of cell (x, y) at (px, py) of the
+// tile's 18 x 18 box, from the surface levels in shared memory.
+template <class Smem>
+__device__ __forceinline__ float2 tile_pres(const Film& F, const cf_params& P, const Smem& S, int i0, int j0, int px,
+                                            int py, int x, int y, uint32_t c) {
+  const int b = (y - j0 + 4) * FB + (x - i0 + 4);
+  const float hv = S.h[b];
+  const float* u = &S.su[(py + 1) * 20 + px + 1];
+  const float u0 = u[0];
+  float pl = 0.f;
+  const float ax = u[-1] + u[1] + u[-20] + u[20];
+  const float dg = u[-21] + u[-19] + u[19] + u[21];
+  const float l = (W_AXIS * ax + W_DIAG_LAP * dg - (4.0f * W_AXIS + 4.0f * W_DIAG_LAP) * u0) * P.inv_dx * P.inv_dx;
+  if (hv > 0.f) {
+    int ox, oy;
+    unpack_off(S.dl[b], ox, oy);
+    const float d = off_len(ox, oy);
+    if (d <= 3.0f) {
+      const float2 n = F.fnorm[c];
+      if (n.x * n.x + n.y * n.y > 0.5f) pl = line_pressure(F, P, x, y) * expf(-(d - 1.0f) * 0.7f);
+    }
+  }
+  return make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * u0 + pl);
 }
 template <int MODE, bool CLEAR>
 __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
@@ -822,18 +881,12 @@ __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
   const cf_params& P = D.p;
   const int tid = threadIdx.y * 16 + threadIdx.x;
   const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
-  if (!flow_stage<MODE>(F, S, i0, j0, tid)) return;
+  // the rheology is read from shared memory only by the plug window, which a
+  // flat canvas (gb < 1e-6) skips
   const float gb = P.phys[0] * D.gxy;
+  if (!stage_box<MODE, true>(F, S, i0, j0, tid, gb >= 1e-6f)) return;
   auto box = [&](int x, int y) { return (y - j0 + 4) * FB + (x - i0 + 4); };
-  // surface levels (film.wgsl:147-151) of the tile + 2 rings, reflected at the
-  // grid's edges as the laplacian reads them
-  for (int q = tid; q < 20 * 20; q += 256) {
-    const int b = box(refl_i(F, i0 - 2 + q % 20), refl_j(F, j0 - 2 + q / 20));
-    const float hv = S.h[b];
-    int ox, oy;
-    unpack_off(S.dl[b], ox, oy);
-    S.su[q] = S.h[b] + S.m[b] - (hv > 0.f ? hold_level(P, off_len(ox, oy)) : 0.f);
-  }
+  tile_surface(F, P, S, i0, j0, tid);
   // plug: the HB flux and mass of every window cell (film.wgsl:58-87); on a
   // flat canvas (gb < 1e-6) every plug mobility is 0 and none is needed
   if (gb >= 1e-6f) {
@@ -866,24 +919,8 @@ __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
       S.tmp[q] = F.tmp[c];
       continue;
     }
-    const int b = box(x, y);
-    const float hv = S.h[b];
-    const float* u = &S.su[(py + 1) * 20 + px + 1];
-    const float u0 = u[0];
-    float pl = 0.f;
-    const float ax = u[-1] + u[1] + u[-20] + u[20];
-    const float dg = u[-21] + u[-19] + u[19] + u[21];
-    const float l = (W_AXIS * ax + W_DIAG_LAP * dg - (4.0f * W_AXIS + 4.0f * W_DIAG_LAP) * u0) * P.inv_dx * P.inv_dx;
-    if (hv > 0.f) {
-      int ox, oy;
-      unpack_off(S.dl[b], ox, oy);
-      const float d = off_len(ox, oy);
-      if (d <= 3.0f) {
-        const float2 n = F.fnorm[c];
-        if (n.x * n.x + n.y * n.y > 0.5f) pl = line_pressure(F, P, x, y) * expf(-(d - 1.0f) * 0.7f);
-      }
-    }
-    S.pres[q] = make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * u0 + pl);
+    S.pres[q] = tile_pres(F, P, S, i0, j0, px, py, x, y, c);
+    const float hv = S.h[box(x, y)];
     float t = 0.f;
     if (hv > 0.f && gb >= 1e-6f) {
       float sum = 0.f, mass = 0.f;
@@ -969,6 +1006,60 @@ __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
   if (in) F.fflags[c] = flags[tid];
 }
 
+// The laplacian after the substeps and strata_split (film.wgsl:16-42,
+// 457-514), fused per tile like the flow tile: h, m and the front offsets of
+// the tile and its halo staged in shared memory, the surface levels and
+// pressures of the tile + 1 ring evaluated there (the tile's own pressures
+// also go to the plane: ring cells of tiles that fall asleep read them
+// later), then every face with a frame flux recomputed and its flux split
+// over the upstream cell's strata, as strata_split_tile does.
+template <int MODE>
+__device__ __forceinline__ void split_tile(const Film& F, TileId T) {
+  __shared__ __align__(128) SplitSmem S;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const DevParams& D = *F.P;
+  const cf_params& P = D.p;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
+  if (!stage_box<MODE, false>(F, S, i0, j0, tid)) return;
+  tile_surface(F, P, S, i0, j0, tid);
+  if (tid < 4) S.faces.count[tid] = 0u;
+  S.flags[tid] = 0u;
+  __syncthreads();
+  for (int q = tid; q < 18 * 18; q += 256) {
+    const int px = q % 18, py = q / 18, x = i0 - 1 + px, y = j0 - 1 + py;
+    if (!in_grid(F, x, y)) continue;
+    const uint32_t c = idx(F, x, y);
+    S.tmp[q] = F.tmp[c];  // the last substep's plug mobilities
+    S.pres[q] = cell_active(F, x, y) ? tile_pres(F, P, S, i0, j0, px, py, x, y, c) : F.pres[c];
+  }
+  __syncthreads();
+  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
+  const bool in = i < (int)F.w && j < (int)F.h;
+  const uint32_t c = in ? idx(F, i, j) : 0u;
+  if (in) F.pres[c] = S.pres[(threadIdx.y + 1) * 18 + threadIdx.x + 1];
+  const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    tile_faces_add(S.faces, k, in && sel4(a4, k) != 0.f && in_grid(F, i + FACE_DI[k], j + FACE_DJ[k]));
+  __syncthreads();
+  const PtTile pt{F, S.pres, S.tmp, S.h, i0, j0};
+  tile_faces_each(F, T, S.faces, [&](int k, int fi, int fj, uint32_t fc) {
+    const float a = sel4(F.acc[fc], k);
+    const FaceOut ff = face_k<MODE>(F, D, pt, fi, fj, k);
+    const int bi = fi + FACE_DI[k], bj = fj + FACE_DJ[k];
+    const uint32_t cb = idx(F, bi, bj);
+    const uint32_t cu = a < 0.f ? cb : fc;
+    const float ha = S.h[(fj - j0 + 4) * FB + (fi - i0 + 4)], hb = S.h[(bj - j0 + 4) * FB + (bi - i0 + 4)];
+    const float4 o = band_split(F, cu, 0.5f * (ha + hb), ff.y, ff.up, a, ff.n);
+    F.acc_s[(size_t)k * F.n + fc] = o;
+    if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f)
+      atomicOr(&S.flags[(fj - j0) * 16 + (fi - i0)], 1u << k);
+  });
+  __syncthreads();
+  if (in) F.fflags[c] = S.flags[tid];
+}
+
 __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm, float* ltab, int tid, int nthreads) {
   for (int q = tid; q < 480; q += nthreads) tab[q] = F.pigtab[q];
   if (tid < 48) cm[tid] = F.cmf[tid];
@@ -1017,8 +1108,12 @@ __device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& 
   // carries a strata flux (the face flags of strata_split); only then is the
   // strata_limit alpha below 1 and does strata_update move material into or
   // out of the cell.
-  float4 t4 = F.sh[c], cu = F.scu[c];
   const uint8_t state = F.shade_state[c];
+  // a cell dry two passes running in an active tile holds zeros in both
+  // generations: unless a strata flux reaches it below, nothing to do
+  const bool dry2 = act && hc <= 0.f && state == SHADE_DRY2;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 t4 = dry2 ? z4 : F.sh[c], cu = dry2 ? z4 : F.scu[c];
   if (act) {
     const bool hl = i > 0, hd = j > 0, hu = j + 1 < (int)F.h;
     const uint32_t f0 = F.fflags[c], fl = hl ? F.fflags[c - 1] : 0u, fd = hd ? F.fflags[c - F.w] : 0u,
@@ -1032,7 +1127,6 @@ __device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& 
       // strata_split did not write this frame are zeroed here (a face is
       // zeroed by at most its two cells, both writing zero, and read under
       // its flag only until the full path).
-      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int k = 0; k < 4; ++k)
         if (!((f0 >> k) & 1u)) F.acc_s[(size_t)k * F.n + c] = z4;
@@ -1043,6 +1137,7 @@ __device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& 
       list_append(F.full_list, &F.stats->full_count, c);
       return FAST_NOTHING;
     }
+    if (dry2) return FAST_NOTHING;
   }
   float nt[4] = {t4.x, t4.y, t4.z, t4.w};
   if (act) {
@@ -1077,9 +1172,14 @@ __device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& 
   sh.cu[tid] = cu;
   sh.h[tid] = hc;
   if (hc <= 0.f) {
-    if (state == SHADE_DRY) return FAST_NOTHING;
-    F.shade_state[c] = SHADE_DRY;
-    return FAST_SHADE;
+    // zeros now in both generations when this pass wrote zeros and the
+    // current one held zeros
+    const bool zeros = act && t4.x == 0.f && t4.y == 0.f && t4.z == 0.f && t4.w == 0.f && cu.x == 0.f &&
+                       cu.y == 0.f && cu.z == 0.f && cu.w == 0.f;
+    const bool shaded = state == SHADE_DRY || state == SHADE_DRY2;
+    const uint8_t next = shaded && zeros ? SHADE_DRY2 : SHADE_DRY;
+    if (next != state) F.shade_state[c] = next;
+    return shaded ? FAST_NOTHING : FAST_SHADE;
   }
   if (state == SHADE_WET && P.flags[0] != 1u && nt[0] == t4.x && nt[1] == t4.y && nt[2] == t4.z && nt[3] == t4.w)
     return FAST_COLOR;
@@ -1724,6 +1824,8 @@ __global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILE f
 template <int MODE, bool CLEAR>
 __global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILE flow_tile<MODE, CLEAR>(F, T); }
 template <int MODE>
+__global__ void __launch_bounds__(256, 6) kp_split(PACKED_ARGS) { PACKED_TILE split_tile<MODE>(F, T); }
+template <int MODE>
 __global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
@@ -1847,13 +1949,12 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     kp_nose<<<nt, b, 0, st>>>(A, T, nt);
     n += 4;
   }
-  kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
-  kp_strata_split<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  kp_split<MODE><<<nt, b, 0, st>>>(A, T, nt);  // laplacian + strata_split
   kp_strata_fast<MODE><<<nt, b, 0, st>>>(A, T, nt);  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_fill_list<MODE><<<nf, 1024, 0, st>>>(V.films_next, nf);
-  return n + 6;
+  return n + 5;
 }
 
 uint32_t launch_frame_packed(const PackedFrame& V, int mode, uint32_t substeps, int adaptive, cudaStream_t st) {
@@ -1928,6 +2029,7 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "laplacian") kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
   else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
   else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
+  else if (n == "split") CFK_LAUNCH(kp_split, nt, b, st, A, T, nt);  // laplacian + strata_split fused
   else if (n == "flow") {  // laplacian + plug + fluxes fused, as the frame runs them
     if (mode == CF_PREC_REFERENCE) kp_flow<CF_PREC_REFERENCE, false><<<nt, b, 0, st>>>(A, T, nt);
     else if (mode == CF_PREC_FP32) kp_flow<CF_PREC_FP32, false><<<nt, b, 0, st>>>(A, T, nt);
