@@ -34,9 +34,9 @@ cf_status cf_debug_write(cf_film* film, const char* name, const void* host, size
 
 /* Runs one dispatch of Film::encode_frame by its WGSL entry-point name
  * ("laplacian", "fluxes", "strata_update", "shade_full", ...; "deposit" lays
- * the deposits uploaded since the last frame and drops them), or one of the
- * fused kernels the frame runs: "flow" (laplacian + plug + fluxes) and
- * "split" (laplacian + strata_split). */
+ * the deposits uploaded since the last frame and drops them), or the fused
+ * kernel the frame runs for the head of each substep: "flow" (laplacian +
+ * plug + fluxes). */
 cf_status cf_debug_run(cf_film* film, const char* kernel, void* stream);
 
 /* Overwrites the device params with `params` (no re-packing). */

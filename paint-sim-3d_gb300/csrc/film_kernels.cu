@@ -747,20 +747,6 @@ __device__ __forceinline__ float staged_rh(const FlowSmem& S, int plane, int b) 
     return __uint_as_float(S.rh[plane][b]);
   }
 }
-// Shared memory of a split block (laplacian + strata_split of one tile): the
-// staged h, m and front offsets, surface levels, pressures and the plane's
-// plug mobilities on the tile + 1 ring, the face lists and face flags.
-struct SplitSmem {
-  float h[FB * FB];
-  float m[FB * FB];
-  uint32_t dl[FB * FB];
-  float su[20 * 20];
-  float2 pres[18 * 18];
-  float tmp[18 * 18];
-  TileFaces faces;
-  uint32_t flags[256];
-  uint64_t bar;
-};
 // The tile's box of h, m and the front offsets (and with RHEO, where `rheo`
 // is set, the three rheology planes) into shared memory: tensor loads when
 // the film has descriptors, else loads by the block's threads (zero outside
@@ -1004,60 +990,6 @@ __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
   });
   __syncthreads();
   if (in) F.fflags[c] = flags[tid];
-}
-
-// The laplacian after the substeps and strata_split (film.wgsl:16-42,
-// 457-514), fused per tile like the flow tile: h, m and the front offsets of
-// the tile and its halo staged in shared memory, the surface levels and
-// pressures of the tile + 1 ring evaluated there (the tile's own pressures
-// also go to the plane: ring cells of tiles that fall asleep read them
-// later), then every face with a frame flux recomputed and its flux split
-// over the upstream cell's strata, as strata_split_tile does.
-template <int MODE>
-__device__ __forceinline__ void split_tile(const Film& F, TileId T) {
-  __shared__ __align__(128) SplitSmem S;
-  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
-  const DevParams& D = *F.P;
-  const cf_params& P = D.p;
-  const int tid = threadIdx.y * 16 + threadIdx.x;
-  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
-  if (!stage_box<MODE, false>(F, S, i0, j0, tid)) return;
-  tile_surface(F, P, S, i0, j0, tid);
-  if (tid < 4) S.faces.count[tid] = 0u;
-  S.flags[tid] = 0u;
-  __syncthreads();
-  for (int q = tid; q < 18 * 18; q += 256) {
-    const int px = q % 18, py = q / 18, x = i0 - 1 + px, y = j0 - 1 + py;
-    if (!in_grid(F, x, y)) continue;
-    const uint32_t c = idx(F, x, y);
-    S.tmp[q] = F.tmp[c];  // the last substep's plug mobilities
-    S.pres[q] = cell_active(F, x, y) ? tile_pres(F, P, S, i0, j0, px, py, x, y, c) : F.pres[c];
-  }
-  __syncthreads();
-  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
-  const bool in = i < (int)F.w && j < (int)F.h;
-  const uint32_t c = in ? idx(F, i, j) : 0u;
-  if (in) F.pres[c] = S.pres[(threadIdx.y + 1) * 18 + threadIdx.x + 1];
-  const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    tile_faces_add(S.faces, k, in && sel4(a4, k) != 0.f && in_grid(F, i + FACE_DI[k], j + FACE_DJ[k]));
-  __syncthreads();
-  const PtTile pt{F, S.pres, S.tmp, S.h, i0, j0};
-  tile_faces_each(F, T, S.faces, [&](int k, int fi, int fj, uint32_t fc) {
-    const float a = sel4(F.acc[fc], k);
-    const FaceOut ff = face_k<MODE>(F, D, pt, fi, fj, k);
-    const int bi = fi + FACE_DI[k], bj = fj + FACE_DJ[k];
-    const uint32_t cb = idx(F, bi, bj);
-    const uint32_t cu = a < 0.f ? cb : fc;
-    const float ha = S.h[(fj - j0 + 4) * FB + (fi - i0 + 4)], hb = S.h[(bj - j0 + 4) * FB + (bi - i0 + 4)];
-    const float4 o = band_split(F, cu, 0.5f * (ha + hb), ff.y, ff.up, a, ff.n);
-    F.acc_s[(size_t)k * F.n + fc] = o;
-    if (o.x != 0.f || o.y != 0.f || o.z != 0.f || o.w != 0.f)
-      atomicOr(&S.flags[(fj - j0) * 16 + (fi - i0)], 1u << k);
-  });
-  __syncthreads();
-  if (in) F.fflags[c] = S.flags[tid];
 }
 
 __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm, float* ltab, int tid, int nthreads) {
@@ -1824,8 +1756,6 @@ __global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILE f
 template <int MODE, bool CLEAR>
 __global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILE flow_tile<MODE, CLEAR>(F, T); }
 template <int MODE>
-__global__ void __launch_bounds__(256, 6) kp_split(PACKED_ARGS) { PACKED_TILE split_tile<MODE>(F, T); }
-template <int MODE>
 __global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
 template <int MODE>
@@ -1949,12 +1879,13 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     kp_nose<<<nt, b, 0, st>>>(A, T, nt);
     n += 4;
   }
-  kp_split<MODE><<<nt, b, 0, st>>>(A, T, nt);  // laplacian + strata_split
+  kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+  kp_strata_split<MODE><<<nt, b, 0, st>>>(A, T, nt);
   kp_strata_fast<MODE><<<nt, b, 0, st>>>(A, T, nt);  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_fill_list<MODE><<<nf, 1024, 0, st>>>(V.films_next, nf);
-  return n + 5;
+  return n + 6;
 }
 
 uint32_t launch_frame_packed(const PackedFrame& V, int mode, uint32_t substeps, int adaptive, cudaStream_t st) {
@@ -2029,7 +1960,6 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "laplacian") kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
   else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
   else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
-  else if (n == "split") CFK_LAUNCH(kp_split, nt, b, st, A, T, nt);  // laplacian + strata_split fused
   else if (n == "flow") {  // laplacian + plug + fluxes fused, as the frame runs them
     if (mode == CF_PREC_REFERENCE) kp_flow<CF_PREC_REFERENCE, false><<<nt, b, 0, st>>>(A, T, nt);
     else if (mode == CF_PREC_FP32) kp_flow<CF_PREC_FP32, false><<<nt, b, 0, st>>>(A, T, nt);

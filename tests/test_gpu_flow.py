@@ -69,32 +69,3 @@ def test_flow_equals_separate_dispatches(gp, prec):
         print("%s prec %d: fluxes %d of %d differ in the last bits, tmp %d" % (name, prec, nflux, flux_f.size, ntmp))
         assert np.abs(flux_s).max() > 0.0
         f.close()
-
-
-@pytest.mark.parametrize("prec", [capi.CF_PREC_REFERENCE, capi.CF_PREC_FP32, capi.CF_PREC_BF16])
-def test_split_equals_separate_dispatches(gp, prec):
-    """The fused split kernel (the laplacian after the substeps + strata_split)
-    against the two separate dispatches: the per-stratum face splits, the face
-    flags (exactly) and the tile's pressures, which the fused kernel still
-    writes to the plane."""
-    from canvaz_film.film import Film
-    for name, (cv, sched) in cases(gp):
-        o = gp.oracle_state(cv, sched)
-        o.run("clear_acc")
-        for k in ("laplacian", "plug", "fluxes", "limiter", "apply", "nose"):  # a frame flux to split
-            o.run(k)
-        f = Film(po.make_settings(cv.settings), cv.w, cv.h, prec)
-        f.set_tables(cv.pigtab, cv.cmf)
-        gp.transfer(o, f)
-        f.run("split")
-        acc_f, fl_f, pres_f = f.plane("acc_s"), f.plane("fflags"), f.plane("pres")
-        gp.transfer(o, f)
-        f.run("laplacian")
-        f.run("strata_split")
-        acc_s, fl_s, pres_s = f.plane("acc_s"), f.plane("fflags"), f.plane("pres")
-        assert np.abs(acc_s).max() > 0.0, name
-        n_acc = close(acc_f, acc_s, name + " acc_s")
-        close(pres_f, pres_s, name + " pres")
-        np.testing.assert_array_equal(fl_f, fl_s, err_msg=name)
-        print("%s prec %d: splits %d of %d differ in the last bits" % (name, prec, n_acc, acc_f.size))
-        f.close()
