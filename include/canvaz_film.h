@@ -414,7 +414,10 @@ typedef struct cf_batch_tuning {
     uint32_t list_blocks_per_sm;  /* grid of the strata list kernels, blocks per SM (default 8) */
     uint32_t use_graph;           /* 1: frames replay a captured CUDA graph (default 1)       */
     uint32_t frames_per_graph;    /* frames captured in one graph launch (default 1)          */
-    uint32_t reserved;
+    uint32_t tiles_per_block;     /* consecutive 16x16 tiles a block of the per-tile kernels
+                                   * walks: 1 (default; 0 reads as 1), 2 or 4 (launch tiles of
+                                   * 32x16 or 64x16 cells), up to 4096 (a grid of a few blocks
+                                   * per SM walking the table: persistent)                    */
 } cf_batch_tuning;
 
 cf_status cf_batch_create(cf_batch** out);

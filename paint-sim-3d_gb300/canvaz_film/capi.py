@@ -126,7 +126,7 @@ class ReliefView(C.Structure):
 class BatchTuning(C.Structure):
     """cf_batch_tuning."""
     _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("tiles_per_block", C.c_uint32)]
 
 
 class Stats(C.Structure):

@@ -356,7 +356,7 @@ class Batch:
     def tuning(self):
         t = BatchTuning()
         self._check(self.L.cf_batch_get_tuning(self.p, C.byref(t)), "cf_batch_get_tuning")
-        return {k: getattr(t, k) for k, _ in BatchTuning._fields_ if k != "reserved"}
+        return {k: getattr(t, k) for k, _ in BatchTuning._fields_}
 
     @tuning.setter
     def tuning(self, d):
@@ -368,7 +368,7 @@ class Batch:
         t, ms = BatchTuning(), C.c_float()
         self._check(self.L.cf_batch_autotune(self.p, frames_per_trial, substeps, dt_max, stream, C.byref(t),
                                              C.byref(ms)), "cf_batch_autotune")
-        return {k: getattr(t, k) for k, _ in BatchTuning._fields_ if k != "reserved"}, ms.value
+        return {k: getattr(t, k) for k, _ in BatchTuning._fields_}, ms.value
 
     def close(self):
         if self.p:

@@ -26,7 +26,7 @@ struct cf_batch {
   };
   std::vector<cf_film*> films;
   std::vector<Group> groups;
-  cf_batch_tuning tune{8u, 1u, 1u, 0u};
+  cf_batch_tuning tune{8u, 1u, 1u, 1u};
   bool built = false;
   int parity = 0;  // which half of every d_films the films are in now
   int device = -1, sms = 1;
@@ -146,6 +146,8 @@ uint64_t enqueue(cf_batch* b, int p, uint32_t frames, uint32_t substeps, int ada
       V.ntiles = g.ntiles;
       V.nfilms = nf;
       V.persist_blocks = blocks;
+      const uint32_t tpb = std::max(b->tune.tiles_per_block, 1u);
+      V.tile_grid = tpb > 1u ? (g.ntiles + tpb - 1u) / tpb : 0u;
       n += cfk::launch_frame_packed(V, g.mode, substeps, adaptive, st);
     }
     p ^= 1;
@@ -295,7 +297,7 @@ cf_status cf_batch_info(cf_batch* b, uint32_t* films, uint64_t* cells, uint64_t*
 
 cf_status cf_batch_set_tuning(cf_batch* b, const cf_batch_tuning* t) {
   if (!b || !t || t->list_blocks_per_sm == 0 || t->list_blocks_per_sm > 64 || t->frames_per_graph == 0 ||
-      t->frames_per_graph > 64)
+      t->frames_per_graph > 64 || t->tiles_per_block > 4096)
     return bfail(b, CF_ERR_INVALID_ARG, "cf_batch_set_tuning");
   b->tune = *t;
   drop_graphs(b);
@@ -338,17 +340,33 @@ cf_status cf_batch_autotune(cf_batch* b, uint32_t frames_per_trial, uint32_t sub
   float top_ms = 3.4e38f;
   cf_status s = CF_OK;
   // stage 1: the list-kernel grid; stage 2: how the frames are launched
+  // (direct, or graphs of 1, 2 or 4 frames); stage 3: the launch tile of the
+  // per-tile kernels (16x16, 32x16, 64x16, or a persistent walk with about
+  // 8 blocks per SM)
   for (uint32_t bps : {4u, 8u, 16u}) {
-    cf_batch_tuning t{bps, 1u, 1u, 0u};
+    cf_batch_tuning t{bps, 1u, 1u, 1u};
     float ms = 0.f;
     if ((s = trial(t, ms)) != CF_OK) break;
     if (ms < top_ms) { top_ms = ms; top = t; }
   }
   if (s == CF_OK) {
-    const cf_batch_tuning stage2[] = {{top.list_blocks_per_sm, 0u, 1u, 0u},
-                                      {top.list_blocks_per_sm, 1u, 2u, 0u},
-                                      {top.list_blocks_per_sm, 1u, 4u, 0u}};
+    const cf_batch_tuning stage2[] = {{top.list_blocks_per_sm, 0u, 1u, 1u},
+                                      {top.list_blocks_per_sm, 1u, 2u, 1u},
+                                      {top.list_blocks_per_sm, 1u, 4u, 1u}};
     for (const auto& t : stage2) {
+      float ms = 0.f;
+      if ((s = trial(t, ms)) != CF_OK) break;
+      if (ms < top_ms) { top_ms = ms; top = t; }
+    }
+  }
+  if (s == CF_OK) {
+    uint32_t tiles = 0;
+    for (const auto& g : b->groups) tiles = std::max(tiles, g.ntiles);
+    const uint32_t persistent = std::min(4096u, std::max(1u, tiles / (8u * (uint32_t)std::max(b->sms, 1))));
+    for (uint32_t tpb : {2u, 4u, persistent}) {
+      if (tpb <= 1u) continue;
+      cf_batch_tuning t = top;
+      t.tiles_per_block = tpb;
       float ms = 0.f;
       if ((s = trial(t, ms)) != CF_OK) break;
       if (ms < top_ms) { top_ms = ms; top = t; }

@@ -1737,43 +1737,73 @@ __device__ __forceinline__ void copy_delta_tile(const Film& F, TileId T) {
 // The film records are read-only for the launch.
 
 #define PACKED_ARGS const Film* __restrict__ films, const uint2* __restrict__ tiles, uint32_t ntiles
-#define PACKED_TILE                    \
-  if (blockIdx.x >= ntiles) return;    \
-  const uint2 pe_ = tiles[blockIdx.x]; \
-  const Film& F = films[pe_.x];        \
-  const TileId T{pe_.y % F.tw, pe_.y / F.tw};
-template <int MODE>
-__global__ void __launch_bounds__(256, 4) kp_cure(PACKED_ARGS) { PACKED_TILE cure_tile<MODE>(F, T); }
-__global__ void __launch_bounds__(256) kp_clear_acc(PACKED_ARGS) { PACKED_TILE clear_acc_tile(F, T); }
-template <bool CLEAR>
-__global__ void __launch_bounds__(256) kp_laplacian(PACKED_ARGS) { PACKED_TILE laplacian_tile<CLEAR>(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILE plug_tile<MODE>(F, T); }
+// Without WALK, block b is table entry b (one 16x16 tile).  With WALK (the
+// instances a batch launches when its tuning groups tiles), block b takes
+// the run of consecutive entries [b * per, (b + 1) * per) with per =
+// ceil(ntiles / gridDim.x): a strip of tiles along a row (a 32 x 16 or
+// 64 x 16 launch tile), or, with a grid of a few blocks per SM, the table in
+// long runs (persistent).  The loop is a separate instance because the
+// registers it keeps live slowed the one-tile kernels by 12-25 %; each tile's
+// body is the same code in both.
+#define PACKED_TILES(WALK, ...)                                                 \
+  {                                                                             \
+    if constexpr (!(WALK)) {                                                    \
+      if (blockIdx.x >= ntiles) return;                                         \
+      const uint2 pe_ = tiles[blockIdx.x];                                      \
+      const Film& F = films[pe_.x];                                             \
+      const TileId T{pe_.y % F.tw, pe_.y / F.tw};                               \
+      __VA_ARGS__;                                                              \
+    } else {                                                                    \
+      const uint32_t per_ = (ntiles + gridDim.x - 1u) / gridDim.x;              \
+      const uint32_t e0_ = blockIdx.x * per_, e1_ = min(ntiles, e0_ + per_);    \
+      for (uint32_t e_ = e0_; e_ < e1_; ++e_) {                                 \
+        if (e_ != e0_) __syncthreads(); /* shared memory of the last tile */    \
+        const uint2 pe_ = tiles[e_];                                            \
+        const Film& F = films[pe_.x];                                           \
+        const TileId T{pe_.y % F.tw, pe_.y / F.tw};                             \
+        __VA_ARGS__;                                                            \
+      }                                                                         \
+    }                                                                           \
+  }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256, 4) kp_cure(PACKED_ARGS) { PACKED_TILES(WALK, cure_tile<MODE>(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(256) kp_clear_acc(PACKED_ARGS) { PACKED_TILES(WALK, clear_acc_tile(F, T)) }
+template <bool CLEAR, bool WALK = false>
+__global__ void __launch_bounds__(256) kp_laplacian(PACKED_ARGS) { PACKED_TILES(WALK, laplacian_tile<CLEAR>(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILES(WALK, plug_tile<MODE>(F, T)) }
 // three blocks per SM: the face code needs no more than 64 registers, and
 // the occupancy hides its dependent loads
-template <int MODE>
-__global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILE fluxes_tile<MODE>(F, T); }
-template <int MODE, bool CLEAR>
-__global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILE flow_tile<MODE, CLEAR>(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILE strata_split_tile<MODE>(F, T); }
-__global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILE limiter_tile(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(128) kp_apply(PACKED_ARGS) { PACKED_TILE apply_tile<MODE>(F, T); }
-__global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILE copy_delta_tile(F, T); }
-__global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILE nose_tile(F, T); }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILES(WALK, fluxes_tile<MODE>(F, T)) }
+template <int MODE, bool CLEAR, bool WALK = false>
+__global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILES(WALK, flow_tile<MODE, CLEAR>(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILES(WALK, strata_split_tile<MODE>(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILES(WALK, limiter_tile(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(128) kp_apply(PACKED_ARGS) { PACKED_TILES(WALK, apply_tile<MODE>(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILES(WALK, copy_delta_tile(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILES(WALK, nose_tile(F, T)) }
 
-template <int MODE>
-__global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILE reduce16_tile<MODE>(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(256, 5) kp_strata_fast(PACKED_ARGS) { PACKED_TILE strata_fast_tile<MODE>(F, T); }
-__global__ void __launch_bounds__(256) kp_strata_limit(PACKED_ARGS) { PACKED_TILE strata_limit_tile(F, T); }
-__global__ void __launch_bounds__(256) kp_face_flags(PACKED_ARGS) { PACKED_TILE face_flags_tile(F, T); }
-__global__ void __launch_bounds__(256) kp_fill_select(PACKED_ARGS) { PACKED_TILE fill_select_tile(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(256) kp_fill_apply(PACKED_ARGS) { PACKED_TILE fill_apply_tile<MODE>(F, T); }
-template <int MODE>
-__global__ void __launch_bounds__(256) kp_compose(PACKED_ARGS, int shade) { PACKED_TILE compose_tile<MODE>(F, T, shade); }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILES(WALK, reduce16_tile<MODE>(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256, 6) kp_strata_fast(PACKED_ARGS) { PACKED_TILES(WALK, strata_fast_tile<MODE>(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(256) kp_strata_limit(PACKED_ARGS) { PACKED_TILES(WALK, strata_limit_tile(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(256) kp_face_flags(PACKED_ARGS) { PACKED_TILES(WALK, face_flags_tile(F, T)) }
+template <bool WALK = false>
+__global__ void __launch_bounds__(256) kp_fill_select(PACKED_ARGS) { PACKED_TILES(WALK, fill_select_tile(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256) kp_fill_apply(PACKED_ARGS) { PACKED_TILES(WALK, fill_apply_tile<MODE>(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256) kp_compose(PACKED_ARGS, int shade) { PACKED_TILES(WALK, compose_tile<MODE>(F, T, shade)) }
 __global__ void __launch_bounds__(256) kp_mark_tiles(PACKED_ARGS) {
   const uint32_t e = blockIdx.x * 8u + (threadIdx.x >> 5);
   if (e >= ntiles) return;
@@ -1795,7 +1825,7 @@ __global__ void __launch_bounds__(256) kp_compact_tiles(PACKED_ARGS) {
       atomicAdd(&films[pe.x].stats->active_tiles, (uint32_t)__popc(same));
   }
 }
-#undef PACKED_TILE
+#undef PACKED_TILES
 #undef PACKED_ARGS
 // per film: one thread each
 __global__ void kp_stats_reset(const Film* __restrict__ films, uint32_t nfilms) {
@@ -1852,18 +1882,27 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
   const uint32_t nt = V.ntiles, nf = V.nfilms;
   if (nf == 0u || nt == 0u) return 0u;
   const uint32_t fb = (nf + 127u) / 128u;
+  // blocks of the per-tile kernels (see PACKED_TILES); the implicit steps'
+  // kernels keep one block per tile
+  const uint32_t tg = V.tile_grid != 0u && V.tile_grid < nt ? V.tile_grid : nt;
   uint32_t n = 0;
   dim3 b(16, 16);
+  using TileKernel = void (*)(const Film*, const uint2*, uint32_t);
+  // the one-tile instance, or the walking one over a grid of tg blocks
+  auto tl = [&](TileKernel one, TileKernel walk, dim3 B) {
+    if (tg < nt) walk<<<tg, B, 0, st>>>(A, T, nt);
+    else one<<<nt, B, 0, st>>>(A, T, nt);
+  };
   if (adaptive) { kp_adaptive_params<<<fb, 128, 0, st>>>(A, nf); ++n; }
   kp_stats_reset<<<fb, 128, 0, st>>>(A, nf);
   kp_mark_tiles<<<(nt + 7u) / 8u, 256, 0, st>>>(A, T, nt);
   kp_compact_tiles<<<(nt + 255u) / 256u, 256, 0, st>>>(A, T, nt);
-  kp_cure<MODE><<<nt, b, 0, st>>>(A, T, nt);
+  tl(kp_cure<MODE, false>, kp_cure<MODE, true>, b);
   n += 4;
   // clear_acc runs with the first laplacian of the frame: the first implicit
   // step's (src/film/mod.rs:1371-1376) or the first substep's
   const uint32_t isteps = V.implicit_steps;
-  if (substeps == 0 && isteps == 0) { kp_clear_acc<<<nt, b, 0, st>>>(A, T, nt); ++n; }
+  if (substeps == 0 && isteps == 0) { tl(kp_clear_acc<false>, kp_clear_acc<true>, b); ++n; }
   for (uint32_t s = 0; s < isteps; ++s) {
     if (s == 0) kp_laplacian<true><<<nt, b, 0, st>>>(A, T, nt);
     else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
@@ -1872,16 +1911,16 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
   for (uint32_t s = 0; s < substeps; ++s) {
     // laplacian + plug + fluxes as one flow launch (with clear_acc on the
     // frame's first)
-    if (s == 0 && isteps == 0) kp_flow<MODE, true><<<nt, b, 0, st>>>(A, T, nt);
-    else kp_flow<MODE, false><<<nt, b, 0, st>>>(A, T, nt);
-    kp_limiter<<<nt, dim3(16, 4), 0, st>>>(A, T, nt);
-    kp_apply<MODE><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
-    kp_nose<<<nt, b, 0, st>>>(A, T, nt);
+    if (s == 0 && isteps == 0) tl(kp_flow<MODE, true, false>, kp_flow<MODE, true, true>, b);
+    else tl(kp_flow<MODE, false, false>, kp_flow<MODE, false, true>, b);
+    tl(kp_limiter<false>, kp_limiter<true>, dim3(16, 4));
+    tl(kp_apply<MODE, false>, kp_apply<MODE, true>, dim3(16, 8));
+    tl(kp_nose<false>, kp_nose<true>, b);
     n += 4;
   }
-  kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
-  kp_strata_split<MODE><<<nt, b, 0, st>>>(A, T, nt);
-  kp_strata_fast<MODE><<<nt, b, 0, st>>>(A, T, nt);  // with the CFL reduction
+  tl(kp_laplacian<false, false>, kp_laplacian<false, true>, b);
+  tl(kp_strata_split<MODE, false>, kp_strata_split<MODE, true>, b);
+  tl(kp_strata_fast<MODE, false>, kp_strata_fast<MODE, true>, b);  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_fill_list<MODE><<<nf, 1024, 0, st>>>(V.films_next, nf);

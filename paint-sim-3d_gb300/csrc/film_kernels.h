@@ -19,6 +19,9 @@ struct PackedFrame {
   uint32_t ntiles;
   uint32_t nfilms;
   uint32_t persist_blocks; // grid of the strata list kernels
+  // blocks of the per-tile kernels: 0 = one per tile entry; fewer make each
+  // block walk a run of consecutive entries (a strip of tiles along a row)
+  uint32_t tile_grid = 0;
   // implicit hydrostatic steps launched (each film's kernels skip the steps
   // beyond its own count), CG iterations per step (each film stops at its
   // own), and whether any film has the implicit capillary term

@@ -68,13 +68,18 @@ def solo(cv, prec, fdt, substeps, frames, dt_max=0.0):
 
 
 TUNINGS = [
-    {"use_graph": 0, "frames_per_graph": 1, "list_blocks_per_sm": 8},
-    {"use_graph": 1, "frames_per_graph": 1, "list_blocks_per_sm": 8},
-    {"use_graph": 1, "frames_per_graph": 2, "list_blocks_per_sm": 4},
+    {"use_graph": 0, "frames_per_graph": 1, "list_blocks_per_sm": 8, "tiles_per_block": 1},
+    {"use_graph": 1, "frames_per_graph": 1, "list_blocks_per_sm": 8, "tiles_per_block": 1},
+    {"use_graph": 1, "frames_per_graph": 2, "list_blocks_per_sm": 4, "tiles_per_block": 1},
+    # launch tiles of 32x16 and 64x16 cells, and a walk of 37 tiles per block
+    # (runs crossing tile rows and films)
+    {"use_graph": 0, "frames_per_graph": 1, "list_blocks_per_sm": 8, "tiles_per_block": 2},
+    {"use_graph": 1, "frames_per_graph": 1, "list_blocks_per_sm": 8, "tiles_per_block": 4},
+    {"use_graph": 1, "frames_per_graph": 2, "list_blocks_per_sm": 8, "tiles_per_block": 37},
 ]
 
 
-@pytest.mark.parametrize("tuning", TUNINGS, ids=["direct", "graph1", "graph2"])
+@pytest.mark.parametrize("tuning", TUNINGS, ids=["direct", "graph1", "graph2", "tiles2", "tiles4-graph", "walk37"])
 def test_batch_equals_films_alone_fixed_dt(built, tuning):
     from canvaz_film.film import Batch
     cs = cases()
@@ -142,6 +147,7 @@ def test_autotune_picks_a_candidate(built):
     assert ms > 0
     assert tuning["list_blocks_per_sm"] in (4, 8, 16)
     assert (tuning["use_graph"], tuning["frames_per_graph"]) in ((1, 1), (0, 1), (1, 2), (1, 4))
+    assert 1 <= tuning["tiles_per_block"] <= 4096
     b.step(3)  # keeps stepping with the chosen tuning
     b.close()
 
