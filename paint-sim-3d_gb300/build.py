@@ -17,7 +17,7 @@ CSRC = HERE / "csrc"
 OUT = CSRC / "_build"
 LIB = OUT / "libcanvaz_film.so"
 SOURCES = ["capi.cu", "capi_batch.cu", "film_kernels.cu", "film_noalloc.cu", "resolve.cu", "snapshot.cu", "deposit.cu", "cg.cu", "relief.cu"]
-HEADERS = ["film_device.cuh", "strata_device.cuh", "strata_lane.cuh", "film_kernels.h", "film_handle.h"]
+HEADERS = ["film_device.cuh", "strata_device.cuh", "strata_lane.cuh", "film_kernels.h", "film_handle.h", "tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr"]

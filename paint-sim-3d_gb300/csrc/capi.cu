@@ -188,9 +188,10 @@ static EncodeTiledFn encode_tiled() {
   return fn;
 }
 
-// The flow tile's descriptors (cfk::FlowMap order): h, m and the front
-// offsets as 24 x 24 boxes of 4-byte cells, the rheology planes as 24 x 24
-// boxes of f32 or 32 x 24 boxes of bf16; zero fill outside the grid.  Each
+// The tile kernels' descriptors (cfk::FlowMap order): h, m, the front
+// offsets and their snapshot as 24 x 24 boxes of 4-byte cells, the rheology
+// planes as 24 x 24 boxes of f32 or 32 x 24 boxes of bf16; zero fill outside
+// the grid.  Each
 // row pitch must be a multiple of 16 bytes, and the grid at least one box:
 // returns false otherwise (the tile then stages with plain loads).
 static bool encode_flow_maps(const cfk::Film& F, int precision, CUtensorMap maps[cfk::FLOW_MAPS]) {
@@ -212,7 +213,8 @@ static bool encode_flow_maps(const cfk::Film& F, int precision, CUtensorMap maps
          one(&maps[cfk::MAP_M], F.m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 24) &&
          one(&maps[cfk::MAP_DELTA], F.delta, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, 24) &&
          one(&maps[cfk::MAP_MU], F.mu, rt, rb, rw) && one(&maps[cfk::MAP_TAU], F.tau, rt, rb, rw) &&
-         one(&maps[cfk::MAP_N], F.nn, rt, rb, rw);
+         one(&maps[cfk::MAP_N], F.nn, rt, rb, rw) &&
+         one(&maps[cfk::MAP_DELTA_OLD], F.delta_old, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, 24);
 }
 
 // The device planes of a film (n cells, nt tiles) in arena order; add(p, bytes)
@@ -326,15 +328,12 @@ cf_status cf_create(const cf_settings* s, uint32_t w, uint32_t h, int32_t precis
       F.tmap = f->d_tmaps;
     }
   }
-  {  // the film's own packed view (see solo_view)
+  {  // the film's own packed view (see solo_view; its tile table is implicit)
     cfk::Film rec[2] = {F, F};
     std::swap(rec[1].sh, rec[1].sh2);
     std::swap(rec[1].scu, rec[1].scu2);
-    std::vector<uint2> tiles(nt);
-    for (size_t t = 0; t < nt; ++t) tiles[t] = make_uint2(0u, (uint32_t)t);
-    if (cudaMalloc(&f->d_recs, sizeof(rec)) != cudaSuccess || cudaMalloc(&f->d_tiles, sizeof(uint2) * nt) != cudaSuccess ||
-        cudaMemcpy(f->d_recs, rec, sizeof(rec), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(f->d_tiles, tiles.data(), sizeof(uint2) * nt, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMalloc(&f->d_recs, sizeof(rec)) != cudaSuccess ||
+        cudaMemcpy(f->d_recs, rec, sizeof(rec), cudaMemcpyHostToDevice) != cudaSuccess) {
       f->err = "cudaMalloc film records";
       cudaGetLastError();
       return bail(CF_ERR_OUT_OF_MEMORY);
@@ -420,7 +419,6 @@ cf_status cf_destroy(cf_film* f) {
   if (f->params_ev) cudaEventDestroy(f->params_ev);
   if (f->d_recs) cudaFree(f->d_recs);
   if (f->d_tmaps) cudaFree(f->d_tmaps);
-  if (f->d_tiles) cudaFree(f->d_tiles);
   if (f->d_deps) cudaFree(f->d_deps);
   if (f->d_dep_tiles) cudaFree(f->d_dep_tiles);
   if (f->d_dep_items) cudaFree(f->d_dep_items);

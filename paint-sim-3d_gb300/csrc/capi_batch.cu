@@ -20,7 +20,7 @@ struct cf_batch {
     int mode = 0;
     std::vector<cf_film*> films;
     cfk::Film* d_films = nullptr;  // [2][nfilms]: records as built, then swapped
-    uint2* d_tiles = nullptr;      // (film index, tile index)
+    uint2* d_tiles = nullptr;      // (film index, tile index); null for a group of one film (identity)
     uint32_t ntiles = 0;
     std::vector<float4*> sh_built;  // each film's current thickness plane at build
   };
@@ -103,9 +103,11 @@ cf_status build(cf_batch* b) {
     b->groups.push_back(g);
     cf_batch::Group& G = b->groups.back();
     BATCH_TRY(b, cudaMalloc(&G.d_films, sizeof(cfk::Film) * 2 * nf));
-    BATCH_TRY(b, cudaMalloc(&G.d_tiles, sizeof(uint2) * tiles.size()));
     BATCH_TRY(b, cudaMemcpy(G.d_films, rec.data(), sizeof(cfk::Film) * 2 * nf, cudaMemcpyHostToDevice));
-    BATCH_TRY(b, cudaMemcpy(G.d_tiles, tiles.data(), sizeof(uint2) * tiles.size(), cudaMemcpyHostToDevice));
+    if (nf > 1) {  // a group of one film uses the implicit identity table, as the film alone does
+      BATCH_TRY(b, cudaMalloc(&G.d_tiles, sizeof(uint2) * tiles.size()));
+      BATCH_TRY(b, cudaMemcpy(G.d_tiles, tiles.data(), sizeof(uint2) * tiles.size(), cudaMemcpyHostToDevice));
+    }
   }
   b->parity = 0;
   b->built = true;

@@ -192,7 +192,7 @@ __device__ __forceinline__ float film_total(const Film& F, const float* part, fl
 #define CG_ARGS const Film* __restrict__ films, const uint2* __restrict__ tiles, uint32_t ntiles
 #define CG_TILE                                                          \
   if (blockIdx.x >= ntiles) return;                                      \
-  const uint2 pe_ = tiles[blockIdx.x];                                   \
+  const uint2 pe_ = tile_entry(tiles, blockIdx.x);                       \
   const Film& F = films[pe_.x];                                          \
   const DevParams& D = *F.P;                                             \
   const cf_params& P = D.p;                                              \

@@ -143,9 +143,10 @@ struct Film {
   uint32_t all_active;      // keep every tile active (settings.all_active)
   const float* pigtab;  // 12 x 40
   const float* cmf;     // 16 x 3
-  // TMA descriptors of the planes a flow tile stages (FLOW_MAPS of them, in
-  // that order), 64-byte aligned in device memory; null where the grid's row
-  // pitch is not a multiple of 16 bytes (the tile then loads them itself)
+  // TMA descriptors of the planes the tile kernels stage (FLOW_MAPS of them,
+  // in that order), 64-byte aligned in device memory; null where the grid's
+  // row pitch is not a multiple of 16 bytes (the tiles then load them
+  // themselves)
   const CUtensorMap* tmap;
 };
 // Film::shade_state of a cell.  The KM shade of a wet cell composites each
@@ -164,10 +165,17 @@ struct Film {
 // active tile two passes running), so a pass that finds it dry again has
 // nothing to read or write for it.
 constexpr uint8_t SHADE_NONE = 0, SHADE_DRY = 1, SHADE_WET = 2, SHADE_DRY2 = 3;
-// Planes staged by the flow kernel's tensor loads, in Film::tmap order.
-enum FlowMap { MAP_H = 0, MAP_M, MAP_DELTA, MAP_MU, MAP_TAU, MAP_N, FLOW_MAPS };
+// Planes staged by tensor loads (the flow, laplacian and nose tiles), in
+// Film::tmap order.
+enum FlowMap { MAP_H = 0, MAP_M, MAP_DELTA, MAP_MU, MAP_TAU, MAP_N, MAP_DELTA_OLD, FLOW_MAPS };
 
 __device__ __forceinline__ uint32_t idx(const Film& F, int i, int j) { return (uint32_t)j * F.w + (uint32_t)i; }
+// Entry e of a packed tile table (film index, tile index).  A null table is
+// the identity over film 0, the view of a film stepped alone: its blocks
+// take their tile from the block index and skip the table's load.
+__device__ __forceinline__ uint2 tile_entry(const uint2* tiles, uint32_t e) {
+  return tiles != nullptr ? tiles[e] : make_uint2(0u, e);
+}
 __device__ __forceinline__ bool in_grid(const Film& F, int i, int j) {
   return i >= 0 && j >= 0 && i < (int)F.w && j < (int)F.h;
 }
@@ -415,9 +423,10 @@ __device__ __forceinline__ uint32_t feeders(const Film& F, const cf_params& P, u
   if (j + 1 < (int)F.h && F.hh[idx(F, i, j + 1)] > thr) n++;
   return n;
 }
-// film.wgsl:160-180
-static __device__ __noinline__ float2 front_normal(const Film& F, const cf_params& P, uint32_t c) {
-  int i = (int)(c % F.w), j = (int)(c / F.w);
+// film.wgsl:160-180, with the heights of the 5 x 5 neighbourhood read through
+// hgt(x, y) (the plane, or a tile's box staged in shared memory)
+template <class HF>
+__device__ __forceinline__ float2 front_normal_at(const Film& F, const cf_params& P, int i, int j, HF hgt) {
   float dx = 0.f, dy = 0.f;
 #pragma unroll
   for (int dj = -2; dj <= 2; ++dj)
@@ -427,7 +436,7 @@ static __device__ __noinline__ float2 front_normal(const Film& F, const cf_param
       if (di * di + dj * dj > 5) continue;
       int x = i + di, y = j + dj;
       if (!in_grid(F, x, y)) continue;
-      if (F.hh[idx(F, x, y)] <= P.ein[3]) {
+      if (hgt(x, y) <= P.ein[3]) {
         float dd = (float)(di * di + dj * dj);
         dx += (float)di / dd;
         dy += (float)dj / dd;
@@ -436,6 +445,9 @@ static __device__ __noinline__ float2 front_normal(const Film& F, const cf_param
   float l = sqrtf(dx * dx + dy * dy);
   if (l < 1e-6f) return make_float2(0.f, 0.f);
   return make_float2(dx / l, dy / l);
+}
+static __device__ __noinline__ float2 front_normal(const Film& F, const cf_params& P, uint32_t c) {
+  return front_normal_at(F, P, (int)(c % F.w), (int)(c / F.w), [&](int x, int y) { return F.hh[idx(F, x, y)]; });
 }
 // film.wgsl:182-188
 __device__ __forceinline__ float wet_gain(float2 n) {

@@ -39,7 +39,6 @@ struct cf_film {
   // generations swapped, and a table of its tiles
   cfk::Film* d_recs = nullptr;
   CUtensorMap* d_tmaps = nullptr;  // the flow tile's tensor-load descriptors (cfk::FLOW_MAPS), or none
-  uint2* d_tiles = nullptr;
   float4* sh_created = nullptr;  // F.sh at create: tells which record is current
   // deposits for the next frame (cf_upload_deposits)
   cf_deposit* d_deps = nullptr;
@@ -57,7 +56,7 @@ inline cfk::PackedFrame solo_view(const cf_film* f) {
   cfk::PackedFrame V;
   V.films = f->d_recs + p;
   V.films_next = f->d_recs + (1 - p);
-  V.tiles = f->d_tiles;
+  V.tiles = nullptr;  // the identity table over this film
   V.ntiles = f->tw * f->th;
   V.nfilms = 1;
   V.persist_blocks = f->F.persist_blocks;

@@ -200,58 +200,6 @@ __device__ __forceinline__ void clear_acc_tile(const Film& F, TileId T) {
   F.h_frame[c] = F.hh[c];
 }
 
-// film.wgsl:16-42; with CLEAR the kernel also does clear_acc (film.wgsl:1427-1434)
-// for its cell, which the reference dispatches just before the first laplacian.
-// The surface level usurf (film.wgsl:147-151, one exp each) of the tile and
-// its 1-cell halo is evaluated once into shared memory, so a cell costs about
-// 1.3 evaluations instead of 9; the 9-point sum keeps the reference's order.
-template <bool CLEAR>
-__device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
-  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
-  __shared__ float su[18][18];
-  __shared__ float sh[16][16], sd[16][16];  // h and nose distance of the tile's own cells
-  const cf_params& P = F.P->p;
-  const int i0 = (int)T.x * 16 - 1, j0 = (int)T.y * 16 - 1;
-  for (int q = threadIdx.y * 16 + threadIdx.x; q < 18 * 18; q += 256) {
-    // usurf (film.wgsl:147-151) with its three loads issued together
-    const int qx = q % 18, qy = q / 18;
-    const uint32_t n = idx(F, refl_i(F, i0 + qx), refl_j(F, j0 + qy));
-    const float hv = F.hh[n], mv = F.m[n];
-    const uint32_t dl = F.delta[n];
-    int ox, oy;
-    unpack_off(dl, ox, oy);
-    const float d = off_len(ox, oy);
-    su[qy][qx] = hv + mv - (hv > 0.f ? hold_level(P, d) : 0.f);
-    if (qx >= 1 && qx <= 16 && qy >= 1 && qy <= 16) {  // the tile's own cells (in the grid: no reflection)
-      sh[qy - 1][qx - 1] = hv;
-      sd[qy - 1][qx - 1] = d;
-    }
-  }
-  __syncthreads();
-  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
-  if (i >= (int)F.w || j >= (int)F.h) return;
-  const uint32_t c = idx(F, i, j);
-  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
-  const float hv = sh[threadIdx.y][threadIdx.x];
-  if (CLEAR) {
-    F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-    F.h_frame[c] = hv;
-  }
-  const float u0 = su[y][x];  // = s0 - hold_level of this cell
-  float pl = 0.f;
-  float ax = su[y][x - 1] + su[y][x + 1] + su[y - 1][x] + su[y + 1][x];
-  float dg = su[y - 1][x - 1] + su[y - 1][x + 1] + su[y + 1][x - 1] + su[y + 1][x + 1];
-  float l = (W_AXIS * ax + W_DIAG_LAP * dg - (4.0f * W_AXIS + 4.0f * W_DIAG_LAP) * u0) * P.inv_dx * P.inv_dx;
-  if (hv > 0.f) {
-    const float d = sd[threadIdx.y][threadIdx.x];
-    if (d <= 3.0f) {
-      float2 n = F.fnorm[c];
-      if (n.x * n.x + n.y * n.y > 0.5f) pl = line_pressure(F, P, i, j) * expf(-(d - 1.0f) * 0.7f);
-    }
-  }
-  F.pres[c] = make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * u0 + pl);
-}
-
 // film.wgsl:58-87.  The HB flux of every cell of the tile and its 3-cell
 // halo is evaluated once into shared memory; each cell then sums its 7x7
 // window in the reference's row-major order, so the result is identical to
@@ -469,59 +417,6 @@ __device__ __forceinline__ void apply_tile(const Film& F, TileId T) {
   }
   if (__syncthreads_or(moved) && threadIdx.x == 0 && threadIdx.y == 0)
     F.tile_moved[T.x + T.y * F.tw] = 1u;
-}
-
-// film.wgsl:680-723, reading delta_old (Jacobi)
-__device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
-  TILE_PROLOGUE
-  if (F.hh[c] <= 0.f) {
-    F.delta[c] = 0u;
-    F.fnorm[c] = make_float2(0.f, 0.f);
-    return;
-  }
-  // the 3x3 neighbourhood's h and delta_old are loaded before the scan
-  float hn9[9];
-  uint32_t dn9[9];
-#pragma unroll
-  for (int e = 0; e < 9; ++e) {
-    const int x = i + e % 3 - 1, y = j + e / 3 - 1;
-    const uint32_t n = in_grid(F, x, y) ? idx(F, x, y) : c;
-    hn9[e] = F.hh[n];
-    dn9[e] = F.delta_old[n];
-  }
-  int bx = 64, by = 64;
-  float bd = 1e9f;
-#pragma unroll
-  for (int dj = -1; dj <= 1; ++dj)
-#pragma unroll
-    for (int di = -1; di <= 1; ++di) {
-      int x = i + di, y = j + dj;
-      if (!in_grid(F, x, y)) continue;
-      const int e = (dj + 1) * 3 + di + 1;
-      int cx = di, cy = dj;
-      if (hn9[e] > 0.f) {
-        uint32_t dn = dn9[e];
-        if ((dn & 0x10000u) == 0u) continue;
-        int ox, oy;
-        unpack_off(dn, ox, oy);
-        cx = ox + di;
-        cy = oy + dj;
-        int tx = i + cx, ty = j + cy;
-        if (!in_grid(F, tx, ty)) continue;
-        if (F.hh[idx(F, tx, ty)] > 0.f) continue;
-      } else if (di == 0 && dj == 0) {
-        continue;
-      }
-      float d = off_len(cx, cy);
-      if (d < bd) { bd = d; bx = cx; by = cy; }
-    }
-  if (bd > 1e8f) {
-    F.delta[c] = 0u;
-    F.fnorm[c] = make_float2(0.f, 0.f);
-    return;
-  }
-  F.delta[c] = pack_off(bx, by);
-  F.fnorm[c] = bd <= 3.0f ? front_normal(F, P, c) : make_float2(0.f, 0.f);
 }
 
 // film.wgsl:457-473
@@ -859,6 +754,145 @@ __device__ __forceinline__ float2 tile_pres(const Film& F, const cf_params& P, c
   }
   return make_float2(-P.phys[1] * l + disjoining(P, hv), P.phys[0] * P.g[2] * u0 + pl);
 }
+// film.wgsl:16-42; with CLEAR the kernel also does clear_acc (film.wgsl:1427-1434)
+// for its cell, which the reference dispatches just before the first laplacian.
+// The tile's box of h, m and the front offsets is staged as the flow tile
+// stages it (tensor loads, a 4-cell halo), the surface levels of the tile + 2
+// rings are evaluated once into shared memory (one exp each instead of 9 per
+// cell), and each cell's pressure is the flow tile's expression over them,
+// the 9-point sum in the reference's order.
+struct LapSmem {
+  float h[FB * FB];                    // box origin (i0 - 4, j0 - 4)
+  float m[FB * FB];
+  uint32_t dl[FB * FB];
+  float su[20 * 20];                   // surface levels, origin (i0 - 2, j0 - 2)
+  uint64_t bar;
+};
+template <bool CLEAR>
+__device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
+  __shared__ __align__(128) LapSmem S;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const cf_params& P = F.P->p;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
+  if (!stage_box<CF_PREC_FP32, false>(F, S, i0, j0, tid)) return;
+  tile_surface(F, P, S, i0, j0, tid);
+  __syncthreads();
+  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const uint32_t c = idx(F, i, j);
+  if (CLEAR) {
+    F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    F.h_frame[c] = S.h[(threadIdx.y + 4) * FB + threadIdx.x + 4];
+  }
+  F.pres[c] = tile_pres(F, P, S, i0, j0, (int)threadIdx.x + 1, (int)threadIdx.y + 1, i, j, c);
+}
+
+// Boxes of two 4-byte planes (24 x 24 cells from (i0 - 4, j0 - 4), zero
+// outside the grid) into shared memory, as stage_box does: tensor loads
+// where the film has descriptors, else loads by the block's threads.
+// Returns false (counted in the film's stats) when the tensor loads did not
+// arrive within the wait limit.
+__device__ __forceinline__ bool stage_pair(const Film& F, uint64_t* bar, int i0, int j0, int tid, uint32_t* da,
+                                           int ma, const uint32_t* sa, uint32_t* db, int mb, const uint32_t* sb) {
+  if (F.tmap != nullptr) {
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, 2u * FB * FB * 4u);
+      tma_load_2d(da, F.tmap + ma, i0 - 4, j0 - 4, bar);
+      tma_load_2d(db, F.tmap + mb, i0 - 4, j0 - 4, bar);
+    }
+    const bool arrived = __syncthreads_and(mbar_wait_bounded(bar, 0, FLOW_WAIT_POLLS));
+    if (!arrived) {
+      if (tid == 0) {
+        atomicAdd(&F.stats->tma_timeouts, 1u);
+        mbar_wait_bounded(bar, 0, FLOW_WAIT_POLLS);  // let loads still in flight land
+      }
+      __syncthreads();
+      return false;
+    }
+    __syncthreads();
+    if (tid == 0) mbar_inval(bar);
+    return true;
+  }
+  for (int q = tid; q < FB * FB; q += 256) {
+    const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
+    const bool in = in_grid(F, x, y);
+    const uint32_t c = in ? idx(F, x, y) : 0u;
+    da[q] = in ? sa[c] : 0u;
+    db[q] = in ? sb[c] : 0u;
+  }
+  __syncthreads();
+  return true;
+}
+
+// film.wgsl:680-723, reading delta_old (Jacobi).  The tile's box of h and
+// delta_old (4-cell halo) is staged in shared memory; the 3 x 3 scan and the
+// front normal's 5 x 5 neighbourhood read it there, and a candidate's target
+// cell outside the box reads the plane.
+struct NoseSmem {
+  float h[FB * FB];                    // box origin (i0 - 4, j0 - 4)
+  uint32_t dl[FB * FB];                // delta_old
+  uint64_t bar;
+};
+__device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
+  __shared__ __align__(128) NoseSmem S;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const cf_params& P = F.P->p;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
+  if (!stage_pair(F, &S.bar, i0, j0, tid, reinterpret_cast<uint32_t*>(S.h), MAP_H,
+                  reinterpret_cast<const uint32_t*>(F.hh), S.dl, MAP_DELTA_OLD, F.delta_old))
+    return;
+  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
+  if (i >= (int)F.w || j >= (int)F.h) return;
+  const uint32_t c = idx(F, i, j);
+  auto at = [&](int x, int y) { return (y - j0 + 4) * FB + (x - i0 + 4); };
+  if (S.h[at(i, j)] <= 0.f) {
+    F.delta[c] = 0u;
+    F.fnorm[c] = make_float2(0.f, 0.f);
+    return;
+  }
+  int bx = 64, by = 64;
+  float bd = 1e9f;
+#pragma unroll
+  for (int dj = -1; dj <= 1; ++dj)
+#pragma unroll
+    for (int di = -1; di <= 1; ++di) {
+      int x = i + di, y = j + dj;
+      if (!in_grid(F, x, y)) continue;
+      int cx = di, cy = dj;
+      if (S.h[at(x, y)] > 0.f) {
+        uint32_t dn = S.dl[at(x, y)];
+        if ((dn & 0x10000u) == 0u) continue;
+        int ox, oy;
+        unpack_off(dn, ox, oy);
+        cx = ox + di;
+        cy = oy + dj;
+        int tx = i + cx, ty = j + cy;
+        if (!in_grid(F, tx, ty)) continue;
+        const bool boxed = tx >= i0 - 4 && tx < i0 + 20 && ty >= j0 - 4 && ty < j0 + 20;
+        if ((boxed ? S.h[at(tx, ty)] : F.hh[idx(F, tx, ty)]) > 0.f) continue;
+      } else if (di == 0 && dj == 0) {
+        continue;
+      }
+      float d = off_len(cx, cy);
+      if (d < bd) { bd = d; bx = cx; by = cy; }
+    }
+  if (bd > 1e8f) {
+    F.delta[c] = 0u;
+    F.fnorm[c] = make_float2(0.f, 0.f);
+    return;
+  }
+  F.delta[c] = pack_off(bx, by);
+  F.fnorm[c] = bd <= 3.0f ? front_normal_at(F, P, i, j, [&](int x, int y) { return S.h[at(x, y)]; })
+                          : make_float2(0.f, 0.f);
+}
+
 template <int MODE, bool CLEAR>
 __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
   __shared__ __align__(128) FlowSmem S;
@@ -1749,7 +1783,7 @@ __device__ __forceinline__ void copy_delta_tile(const Film& F, TileId T) {
   {                                                                             \
     if constexpr (!(WALK)) {                                                    \
       if (blockIdx.x >= ntiles) return;                                         \
-      const uint2 pe_ = tiles[blockIdx.x];                                      \
+      const uint2 pe_ = tile_entry(tiles, blockIdx.x);                          \
       const Film& F = films[pe_.x];                                             \
       const TileId T{pe_.y % F.tw, pe_.y / F.tw};                               \
       __VA_ARGS__;                                                              \
@@ -1758,15 +1792,17 @@ __device__ __forceinline__ void copy_delta_tile(const Film& F, TileId T) {
       const uint32_t e0_ = blockIdx.x * per_, e1_ = min(ntiles, e0_ + per_);    \
       for (uint32_t e_ = e0_; e_ < e1_; ++e_) {                                 \
         if (e_ != e0_) __syncthreads(); /* shared memory of the last tile */    \
-        const uint2 pe_ = tiles[e_];                                            \
+        const uint2 pe_ = tile_entry(tiles, e_);                                \
         const Film& F = films[pe_.x];                                           \
         const TileId T{pe_.y % F.tw, pe_.y / F.tw};                             \
         __VA_ARGS__;                                                            \
       }                                                                         \
     }                                                                           \
   }
+// eight blocks per SM (32 registers): the common path is a handful of loads
+// and an exp; the rare commit branch is out of line and may spill
 template <int MODE, bool WALK = false>
-__global__ void __launch_bounds__(256, 4) kp_cure(PACKED_ARGS) { PACKED_TILES(WALK, cure_tile<MODE>(F, T)) }
+__global__ void __launch_bounds__(256, 8) kp_cure(PACKED_ARGS) { PACKED_TILES(WALK, cure_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(256) kp_clear_acc(PACKED_ARGS) { PACKED_TILES(WALK, clear_acc_tile(F, T)) }
 template <bool CLEAR, bool WALK = false>
@@ -1783,8 +1819,9 @@ template <int MODE, bool WALK = false>
 __global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILES(WALK, strata_split_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILES(WALK, limiter_tile(F, T)) }
+// eight blocks of 128 per SM (64 registers for the two cells' loads in flight)
 template <int MODE, bool WALK = false>
-__global__ void __launch_bounds__(128) kp_apply(PACKED_ARGS) { PACKED_TILES(WALK, apply_tile<MODE>(F, T)) }
+__global__ void __launch_bounds__(128, 8) kp_apply(PACKED_ARGS) { PACKED_TILES(WALK, apply_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILES(WALK, copy_delta_tile(F, T)) }
 template <bool WALK = false>
@@ -1807,7 +1844,7 @@ __global__ void __launch_bounds__(256) kp_compose(PACKED_ARGS, int shade) { PACK
 __global__ void __launch_bounds__(256) kp_mark_tiles(PACKED_ARGS) {
   const uint32_t e = blockIdx.x * 8u + (threadIdx.x >> 5);
   if (e >= ntiles) return;
-  const uint2 pe = tiles[e];
+  const uint2 pe = tile_entry(tiles, e);
   mark_tile(films[pe.x], pe.y);
 }
 // One thread per tile; the active tiles of a warp are counted with one atomic
@@ -1816,7 +1853,7 @@ __global__ void __launch_bounds__(256) kp_mark_tiles(PACKED_ARGS) {
 __global__ void __launch_bounds__(256) kp_compact_tiles(PACKED_ARGS) {
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
   const bool in = e < ntiles;
-  const uint2 pe = in ? tiles[e] : make_uint2(0u, 0u);
+  const uint2 pe = in ? tile_entry(tiles, e) : make_uint2(0u, 0u);
   const bool act = in && compact_tile(films[pe.x], pe.y, (int)films[pe.x].all_active);
   const unsigned m = __ballot_sync(0xffffffffu, act);
   if (act) {
