@@ -6,8 +6,9 @@
  * delta, tmp, acc_s, alpha_s, strata_*2, h_frame, fnorm, tile flags;
  * src/film/mod.rs:586-628), and this library's own per-cell face flags
  * ("fflags": bit f set where strata_split wrote a nonzero face f), so that a
- * single dispatch can be checked against a CPU oracle.  All calls are
- * synchronous.
+ * single dispatch can be checked against a CPU oracle, and "h_next" and
+ * "delta_old", where the frame's fused limiter + apply leaves the new heights
+ * and the front-offset snapshot for the nose.  All calls are synchronous.
  */
 #ifndef CANVAZ_FILM_DEBUG_H
 #define CANVAZ_FILM_DEBUG_H
@@ -35,8 +36,8 @@ cf_status cf_debug_write(cf_film* film, const char* name, const void* host, size
 /* Runs one dispatch of Film::encode_frame by its WGSL entry-point name
  * ("laplacian", "fluxes", "strata_update", "shade_full", ...; "deposit" lays
  * the deposits uploaded since the last frame and drops them), or the fused
- * kernel the frame runs for the head of each substep: "flow" (laplacian +
- * plug + fluxes). */
+ * kernels the frame runs in each substep: "flow" (laplacian + plug +
+ * fluxes) and "limit_apply" (limiter + apply, the new heights in "h_next"). */
 cf_status cf_debug_run(cf_film* film, const char* kernel, void* stream);
 
 /* Overwrites the device params with `params` (no re-packing). */

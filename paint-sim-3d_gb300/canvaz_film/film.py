@@ -19,7 +19,7 @@ DEBUG_PER_CELL = {
     "h": 1, "m": 1, "mu": 1, "tau": 1, "nn": 1, "delta": 1, "lay": 1, "pres": 2, "fnorm": 2, "flux": 4, "acc": 4,
     "acc_s": 16, "alpha_s": 4, "alpha": 1, "tmp": 1, "h_frame": 1, "strata_h": 4, "strata_cure": 4,
     "strata_h2": 4, "strata_cure2": 4, "strata_pig": 64, "strata_pig2": 64, "sub_refl": 16, "color": 4,
-    "fill_src": 1, "fflags": 1,
+    "fill_src": 1, "fflags": 1, "h_next": 1, "delta_old": 1,
 }
 _ELEM_DTYPE = {0: np.float32, 1: np.uint32, 2: np.float16, 3: "bf16", 4: np.int32}
 

@@ -189,9 +189,10 @@ static EncodeTiledFn encode_tiled() {
 }
 
 // The tile kernels' descriptors (cfk::FlowMap order): h, m, the front
-// offsets and their snapshot as 24 x 24 boxes of 4-byte cells, the rheology
-// planes as 24 x 24 boxes of f32 or 32 x 24 boxes of bf16; zero fill outside
-// the grid.  Each
+// offsets, their snapshot and the heights after apply as 24 x 24 boxes of
+// 4-byte cells, the rheology planes as 24 x 24 boxes of f32 or 32 x 24 boxes
+// of bf16, the flux as 20 x 20 boxes of 16-byte cells; zero fill outside the
+// grid.  Each
 // row pitch must be a multiple of 16 bytes, and the grid at least one box:
 // returns false otherwise (the tile then stages with plain loads).
 static bool encode_flow_maps(const cfk::Film& F, int precision, CUtensorMap maps[cfk::FLOW_MAPS]) {
@@ -207,6 +208,17 @@ static bool encode_flow_maps(const cfk::Film& F, int precision, CUtensorMap maps
     return enc(m, t, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   };
+  // the flux plane (4 floats a cell) as a 4w x h grid of floats, in 80 x 20
+  // boxes: 20 x 20 cells
+  auto flux_map = [&](CUtensorMap* m) {
+    const cuuint64_t dims[2] = {4ull * F.w, F.h};
+    const cuuint64_t strides[1] = {(cuuint64_t)F.w * 16};
+    const cuuint32_t box[2] = {80, 20};
+    const cuuint32_t es[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, F.flux, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
   const CUtensorMapDataType rt = b16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   const cuuint32_t rw = b16 ? 32 : 24;
   return one(&maps[cfk::MAP_H], F.hh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 24) &&
@@ -214,7 +226,9 @@ static bool encode_flow_maps(const cfk::Film& F, int precision, CUtensorMap maps
          one(&maps[cfk::MAP_DELTA], F.delta, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, 24) &&
          one(&maps[cfk::MAP_MU], F.mu, rt, rb, rw) && one(&maps[cfk::MAP_TAU], F.tau, rt, rb, rw) &&
          one(&maps[cfk::MAP_N], F.nn, rt, rb, rw) &&
-         one(&maps[cfk::MAP_DELTA_OLD], F.delta_old, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, 24);
+         one(&maps[cfk::MAP_DELTA_OLD], F.delta_old, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, 24) &&
+         one(&maps[cfk::MAP_H_NEXT], F.h_next, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 24) &&
+         flux_map(&maps[cfk::MAP_FLUX]);
 }
 
 // The device planes of a film (n cells, nt tiles) in arena order; add(p, bytes)
@@ -227,7 +241,7 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, bool 
   add((void**)&F.lay, 4 * n); add((void**)&F.pres, 8 * n); add((void**)&F.fnorm, 8 * n);
   add((void**)&F.flux, 16 * n); add((void**)&F.acc, 16 * n); add((void**)&F.acc_s, 64 * n);
   add((void**)&F.alpha_s, 16 * n); add((void**)&F.alpha, 4 * n); add((void**)&F.tmp, 4 * n);
-  add((void**)&F.h_frame, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
+  add((void**)&F.h_frame, 4 * n); add((void**)&F.h_next, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
   add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
   add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n);
   add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
@@ -895,6 +909,7 @@ bool find_plane(cf_film* f, const std::string& n, PlaneRef& r) {
       {"flux", F.flux, 16 * N, CF_ELEM_F32}, {"acc", F.acc, 16 * N, CF_ELEM_F32},
       {"acc_s", F.acc_s, 64 * N, CF_ELEM_F32}, {"alpha_s", F.alpha_s, 16 * N, CF_ELEM_F32},
       {"alpha", F.alpha, 4 * N, CF_ELEM_F32}, {"tmp", F.tmp, 4 * N, CF_ELEM_F32},
+      {"h_next", F.h_next, 4 * N, CF_ELEM_F32}, {"delta_old", F.delta_old, 4 * N, CF_ELEM_U32},
       {"h_frame", F.h_frame, 4 * N, CF_ELEM_F32}, {"strata_h", F.sh, 16 * N, CF_ELEM_F32},
       {"strata_cure", F.scu, 16 * N, CF_ELEM_F32}, {"strata_h2", F.sh2, 16 * N, CF_ELEM_F32},
       {"strata_cure2", F.scu2, 16 * N, CF_ELEM_F32}, {"strata_pig", F.pig, 64 * pb * N, pe},

@@ -114,6 +114,7 @@ struct Film {
   float* alpha;
   float* tmp;
   float* h_frame;
+  float* h_next;   // heights after apply, until the nose commits them to h
   float4* sh;      // strata_h, current generation
   float4* scu;     // strata_cure
   uint4* pig;      // pigment chunks
@@ -165,9 +166,9 @@ struct Film {
 // active tile two passes running), so a pass that finds it dry again has
 // nothing to read or write for it.
 constexpr uint8_t SHADE_NONE = 0, SHADE_DRY = 1, SHADE_WET = 2, SHADE_DRY2 = 3;
-// Planes staged by tensor loads (the flow, laplacian and nose tiles), in
-// Film::tmap order.
-enum FlowMap { MAP_H = 0, MAP_M, MAP_DELTA, MAP_MU, MAP_TAU, MAP_N, MAP_DELTA_OLD, FLOW_MAPS };
+// Planes staged by tensor loads (the flow, laplacian, limiter + apply and
+// nose tiles), in Film::tmap order.
+enum FlowMap { MAP_H = 0, MAP_M, MAP_DELTA, MAP_MU, MAP_TAU, MAP_N, MAP_DELTA_OLD, MAP_FLUX, MAP_H_NEXT, FLOW_MAPS };
 
 __device__ __forceinline__ uint32_t idx(const Film& F, int i, int j) { return (uint32_t)j * F.w + (uint32_t)i; }
 // Entry e of a packed tile table (film index, tile index).  A null table is
@@ -556,15 +557,16 @@ struct FaceOut {
   float q, y, up, n;
 };
 
-// Where face() reads the plug mobility tmp of its two cells: a pair source
-// from PtGlobal / PtTile below (tmp(false) = cell a, tmp(true) = cell b).
+// Where face() reads the heights and plug mobilities of its two cells: a
+// pair source from PtGlobal / PtTile below (h(false), tmp(false): cell a;
+// h(true), tmp(true): cell b).
 // film.wgsl:297-372 (face between cell a and neighbour b)
 template <int MODE, class Pair>
 __device__ FaceOut face(const Film& F, const DevParams& D, const Pair& pt, uint32_t ca, uint32_t cb, float2 gcap,
                         float2 ghyd, float2 gtilt, bool diag, float2 fd) {
   const cf_params& P = D.p;
   FaceOut out = {0.f, 0.f, 0.f, 0.f};
-  float ha = F.hh[ca], hb = F.hh[cb];
+  float ha = pt.h(false), hb = pt.h(true);
   float hf = 0.5f * (ha + hb);
   if (hf <= 0.f) return out;
   float shape = 1.f, proj = 1.f;
@@ -572,7 +574,7 @@ __device__ FaceOut face(const Film& F, const DevParams& D, const Pair& pt, uint3
   if (fminf(ha, hb) <= 0.f) {
     uint32_t wet = ha > 0.f ? ca : cb;
     uint32_t dry = ha > 0.f ? cb : ca;
-    if (F.hh[wet] <= wet_threshold<MODE>(F, D, wet)) return out;
+    if ((ha > 0.f ? ha : hb) <= wet_threshold<MODE>(F, D, wet)) return out;
     wetting = true;
     float2 n = F.fnorm[wet];
     if (n.x * n.x + n.y * n.y < 0.5f) n = front_normal(F, P, wet);
@@ -621,8 +623,7 @@ __device__ FaceOut face(const Film& F, const DevParams& D, const Pair& pt, uint3
     if (gb < 1e-6f) mtilt = 0.f;
     else {
       const bool ub = !(gtilt.x >= 0.f);
-      uint32_t up = ub ? cb : ca;
-      mtilt = pt.tmp(ub) * F.hh[up] / gb;
+      mtilt = pt.tmp(ub) * pt.h(ub) / gb;
     }
   }
   if (meff <= 0.f && mtilt <= 0.f) return out;
@@ -631,8 +632,7 @@ __device__ FaceOut face(const Film& F, const DevParams& D, const Pair& pt, uint3
   float2 tr = rim_translation<MODE>(F, D, ca, cb, hf, fd);
   const float vcap = 2.f;
   if (wetting) {
-    uint32_t wet = ha > 0.f ? ca : cb;
-    float want = tr.x * 2.0f * F.hh[wet] / fmaxf(hf, 1e-9f);
+    float want = tr.x * 2.0f * (ha > 0.f ? ha : hb) / fmaxf(hf, 1e-9f);
     qn = tr.y * fmaxf(qn * tr.y * proj, want) * shape;
     if (fabsf(qn) > vcap * hf) qn = sgnf(qn) * vcap * hf;
   } else {
@@ -673,38 +673,51 @@ __device__ __forceinline__ float2 pres_wet(const Film& F, int i, int j, float2 f
 // in inactive tiles hold the planes' values, as the reference leaves them).
 struct PtGlobal {
   const Film& F;
+  // the faces it is given may be of dry pairs or inactive neighbours
+  static constexpr bool kListed = false;
   struct Pair {
     const float* t;
+    const float* hp;
     uint32_t a, b;
     __device__ __forceinline__ float tmp(bool bsel) const { return t[bsel ? b : a]; }
+    __device__ __forceinline__ float h(bool bsel) const { return hp[bsel ? b : a]; }
   };
   __device__ __forceinline__ float2 pres(int i, int j) const { return pres_at(F, i, j); }
   __device__ __forceinline__ float2 pwet(int i, int j, float2 fb) const { return pres_wet(F, i, j, fb); }
-  __device__ __forceinline__ Pair pair(int, int, uint32_t ca, int, int, uint32_t cb) const { return {F.tmp, ca, cb}; }
+  __device__ __forceinline__ float hat(int i, int j) const { return F.hh[idx(F, i, j)]; }
+  __device__ __forceinline__ Pair pair(int, int, uint32_t ca, int, int, uint32_t cb) const {
+    return {F.tmp, F.hh, ca, cb};
+  }
 };
-// Shared-memory boxes of a flow tile: pres and tmp on 18 x 18 cells from
-// (i0 - 1, j0 - 1), the staged h on 24 x 24 cells from (i0 - 4, j0 - 4).
+// Shared-memory boxes of a flow tile on 18 x 18 cells from (i0 - 1, j0 - 1):
+// the pressures, plug mobilities and heights, where the positions outside
+// the grid hold the values of the cells they reflect to (common.wgsl:152-158),
+// so a lookup needs no reflection.  The tile lists only the faces whose
+// neighbour is in the grid and active and whose pair is not dry (kListed).
 struct PtTile {
-  const Film& F;
+  static constexpr bool kListed = true;
   const float2* sp;
   const float* st;
   const float* sh;
   int i0, j0;
   struct Pair {
     const float* t;
+    const float* hp;
     int a, b;
     __device__ __forceinline__ float tmp(bool bsel) const { return t[bsel ? b : a]; }
+    __device__ __forceinline__ float h(bool bsel) const { return hp[bsel ? b : a]; }
   };
   __device__ __forceinline__ int at18(int i, int j) const { return (j - j0 + 1) * 18 + (i - i0 + 1); }
-  __device__ __forceinline__ float2 pres(int i, int j) const { return sp[at18(refl_i(F, i), refl_j(F, j))]; }
+  __device__ __forceinline__ float2 pres(int i, int j) const { return sp[at18(i, j)]; }
   __device__ __forceinline__ float2 pwet(int i, int j, float2 fb) const {
-    const int ri = refl_i(F, i), rj = refl_j(F, j);
-    const float2 p = sp[at18(ri, rj)];
-    if (sh[(rj - j0 + 4) * 24 + (ri - i0 + 4)] > 0.f) return p;
+    const int q = at18(i, j);
+    const float2 p = sp[q];
+    if (sh[q] > 0.f) return p;
     return make_float2(fb.x, p.y);
   }
+  __device__ __forceinline__ float hat(int i, int j) const { return sh[at18(i, j)]; }
   __device__ __forceinline__ Pair pair(int i, int j, uint32_t, int x, int y, uint32_t) const {
-    return {st, at18(i, j), at18(x, y)};
+    return {st, sh, at18(i, j), at18(x, y)};
   }
 };
 
@@ -720,9 +733,11 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, const PT& pt, int i
   const bool diag = k >= 2;
   const int di = k == 1 ? 0 : 1, dj = k == 0 ? 0 : (k == 3 ? -1 : 1);
   const int x = i + di, y = j + dj;
-  if (!(in_grid(F, x, y) && cell_active(F, x, y))) return z;
+  if constexpr (!PT::kListed) {
+    if (!(in_grid(F, x, y) && cell_active(F, x, y))) return z;
+    if (!(0.5f * (F.hh[idx(F, i, j)] + F.hh[idx(F, x, y)]) > 0.f)) return z;  // face() is zero on a dry pair
+  }
   const uint32_t c = idx(F, i, j), cb = idx(F, x, y);
-  if (!(0.5f * (F.hh[c] + F.hh[cb]) > 0.f)) return z;  // face() is zero on a dry pair
   const float2 p00 = pt.pres(i, j), pb = pt.pres(x, y);
   const float2 gxy = make_float2(P.phys[0] * P.g[0], P.phys[0] * P.g[1]);
   float2 gcap, ghyd, gt, fd;
@@ -745,7 +760,7 @@ __device__ FaceOut face_k(const Film& F, const DevParams& D, const PT& pt, int i
     const float2 pa = pt.pwet(i + 1, j, p00), pc = pt.pwet(i, j + dj, pb);
     const float2 gp = make_float2(-(pa.x - pc.x) * P.inv_dx * s2, -(pa.y - pc.y) * P.inv_dx * s2);
     const float hs = P.ein[3];
-    const bool open = fminf(F.hh[c], F.hh[cb]) > 0.f || F.hh[idx(F, i + 1, j)] > hs || F.hh[idx(F, i, j + dj)] > hs;
+    const bool open = fminf(pt.hat(i, j), pt.hat(x, y)) > 0.f || pt.hat(i + 1, j) > hs || pt.hat(i, j + dj) > hs;
     if (!open) return z;
     gcap = make_float2(ga.x, gp.x);
     ghyd = make_float2(ga.y, gp.y);

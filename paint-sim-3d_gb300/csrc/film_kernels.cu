@@ -628,6 +628,7 @@ struct FlowSmem {
   float su[20 * 20];                   // surface levels, origin (i0 - 2, j0 - 2)
   float2 pres[18 * 18];                // origin (i0 - 1, j0 - 1)
   float tmp[18 * 18];
+  float hr[18 * 18];                   // h, positions outside the grid reflected
   float2 qm[FB * FB];                  // plug flux q and mass h of the window cells
   uint8_t yl[FB * FB];
   TileFaces faces;
@@ -647,15 +648,38 @@ __device__ __forceinline__ float staged_rh(const FlowSmem& S, int plane, int b) 
 // the film has descriptors, else loads by the block's threads (zero outside
 // the grid, as the tensor loads fill).  Returns false (counted in the film's
 // stats) when the tensor loads did not arrive within the wait limit.
+// The block's tensor loads into shared memory: tma_block_arm initialises the
+// barrier (every thread calls it; thread 0 then arms it with the expected
+// bytes and issues the loads), tma_block_wait waits for them, bounded.  A
+// block whose loads did not arrive within the limit counts a timeout in the
+// film's stats, lets the loads still in flight land (bounded again) and
+// returns false: the caller leaves the tile.
+__device__ __forceinline__ void tma_block_arm(uint64_t* bar, int tid) {
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+}
+__device__ __forceinline__ bool tma_block_wait(const Film& F, uint64_t* bar, int tid) {
+  const bool arrived = __syncthreads_and(mbar_wait_bounded(bar, 0, FLOW_WAIT_POLLS));
+  if (!arrived) {
+    if (tid == 0) {
+      atomicAdd(&F.stats->tma_timeouts, 1u);
+      mbar_wait_bounded(bar, 0, FLOW_WAIT_POLLS);
+    }
+    __syncthreads();
+    return false;
+  }
+  __syncthreads();
+  if (tid == 0) mbar_inval(bar);
+  return true;
+}
 template <int MODE, bool RHEO, class Smem>
 __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0, int tid, bool rheo = RHEO) {
   constexpr bool B16 = MODE == CF_PREC_BF16;
   if (F.tmap != nullptr) {
-    if (tid == 0) {
-      mbar_init(&S.bar, 1);
-      mbar_fence_init();
-    }
-    __syncthreads();
+    tma_block_arm(&S.bar, tid);
     if (tid == 0) {
       const uint32_t rb = B16 ? 32 * FB * 2 : FB * FB * 4;
       mbar_arrive_expect_tx(&S.bar, 3u * FB * FB * 4u + (RHEO && rheo ? 3u * rb : 0u));
@@ -671,18 +695,7 @@ __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0
         }
       }
     }
-    const bool arrived = __syncthreads_and(mbar_wait_bounded(&S.bar, 0, FLOW_WAIT_POLLS));
-    if (!arrived) {
-      if (tid == 0) {
-        atomicAdd(&F.stats->tma_timeouts, 1u);
-        mbar_wait_bounded(&S.bar, 0, FLOW_WAIT_POLLS);  // let loads still in flight land
-      }
-      __syncthreads();
-      return false;
-    }
-    __syncthreads();
-    if (tid == 0) mbar_inval(&S.bar);
-    return true;
+    return tma_block_wait(F, &S.bar, tid);
   }
   for (int q = tid; q < FB * FB; q += 256) {
     const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
@@ -796,28 +809,13 @@ __device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
 __device__ __forceinline__ bool stage_pair(const Film& F, uint64_t* bar, int i0, int j0, int tid, uint32_t* da,
                                            int ma, const uint32_t* sa, uint32_t* db, int mb, const uint32_t* sb) {
   if (F.tmap != nullptr) {
-    if (tid == 0) {
-      mbar_init(bar, 1);
-      mbar_fence_init();
-    }
-    __syncthreads();
+    tma_block_arm(bar, tid);
     if (tid == 0) {
       mbar_arrive_expect_tx(bar, 2u * FB * FB * 4u);
       tma_load_2d(da, F.tmap + ma, i0 - 4, j0 - 4, bar);
       tma_load_2d(db, F.tmap + mb, i0 - 4, j0 - 4, bar);
     }
-    const bool arrived = __syncthreads_and(mbar_wait_bounded(bar, 0, FLOW_WAIT_POLLS));
-    if (!arrived) {
-      if (tid == 0) {
-        atomicAdd(&F.stats->tma_timeouts, 1u);
-        mbar_wait_bounded(bar, 0, FLOW_WAIT_POLLS);  // let loads still in flight land
-      }
-      __syncthreads();
-      return false;
-    }
-    __syncthreads();
-    if (tid == 0) mbar_inval(bar);
-    return true;
+    return tma_block_wait(F, bar, tid);
   }
   for (int q = tid; q < FB * FB; q += 256) {
     const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
@@ -833,25 +831,30 @@ __device__ __forceinline__ bool stage_pair(const Film& F, uint64_t* bar, int i0,
 // film.wgsl:680-723, reading delta_old (Jacobi).  The tile's box of h and
 // delta_old (4-cell halo) is staged in shared memory; the 3 x 3 scan and the
 // front normal's 5 x 5 neighbourhood read it there, and a candidate's target
-// cell outside the box reads the plane.
+// cell outside the box reads the plane.  With NEXT (the frame) the heights
+// are the ones the fused limiter + apply left in h_next, and each cell's is
+// committed to h here; without it (the single dispatch) they are h.
 struct NoseSmem {
   float h[FB * FB];                    // box origin (i0 - 4, j0 - 4)
   uint32_t dl[FB * FB];                // delta_old
   uint64_t bar;
 };
+template <bool NEXT>
 __device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
   __shared__ __align__(128) NoseSmem S;
   if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
   const cf_params& P = F.P->p;
   const int tid = threadIdx.y * 16 + threadIdx.x;
   const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
-  if (!stage_pair(F, &S.bar, i0, j0, tid, reinterpret_cast<uint32_t*>(S.h), MAP_H,
-                  reinterpret_cast<const uint32_t*>(F.hh), S.dl, MAP_DELTA_OLD, F.delta_old))
+  const float* hs = NEXT ? F.h_next : F.hh;
+  if (!stage_pair(F, &S.bar, i0, j0, tid, reinterpret_cast<uint32_t*>(S.h), NEXT ? MAP_H_NEXT : MAP_H,
+                  reinterpret_cast<const uint32_t*>(hs), S.dl, MAP_DELTA_OLD, F.delta_old))
     return;
   const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
   if (i >= (int)F.w || j >= (int)F.h) return;
   const uint32_t c = idx(F, i, j);
   auto at = [&](int x, int y) { return (y - j0 + 4) * FB + (x - i0 + 4); };
+  if (NEXT) F.hh[c] = S.h[at(i, j)];
   if (S.h[at(i, j)] <= 0.f) {
     F.delta[c] = 0u;
     F.fnorm[c] = make_float2(0.f, 0.f);
@@ -876,7 +879,7 @@ __device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
         int tx = i + cx, ty = j + cy;
         if (!in_grid(F, tx, ty)) continue;
         const bool boxed = tx >= i0 - 4 && tx < i0 + 20 && ty >= j0 - 4 && ty < j0 + 20;
-        if ((boxed ? S.h[at(tx, ty)] : F.hh[idx(F, tx, ty)]) > 0.f) continue;
+        if ((boxed ? S.h[at(tx, ty)] : hs[idx(F, tx, ty)]) > 0.f) continue;
       } else if (di == 0 && dj == 0) {
         continue;
       }
@@ -891,6 +894,138 @@ __device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
   F.delta[c] = pack_off(bx, by);
   F.fnorm[c] = bd <= 3.0f ? front_normal_at(F, P, i, j, [&](int x, int y) { return S.h[at(x, y)]; })
                           : make_float2(0.f, 0.f);
+}
+
+// ---- limiter + apply, fused ----
+// film.wgsl:516-537 (limiter) and 539-561, 803-863 (apply) for one tile.
+// Only apply reads the limiter's alpha, so it stays in shared memory: the
+// block stages the flux of the tile + 2 rings and h with a 4-cell halo
+// (tensor loads), evaluates alpha on the tile + 1 ring (the expression of
+// limiter_tile), then applies the tile's own cells (apply_tile's, from
+// shared memory).  A ring cell's alpha needs its height before apply, which
+// the neighbouring tile's block may already have replaced; so the new heights
+// go to h_next, and the nose (NEXT), which runs next and reads them there,
+// commits them to h.  Every tile, active or not, snapshots delta into
+// delta_old for the nose, and an inactive tile copies h to h_next, so that
+// the nose finds every cell's height there.
+struct LaSmem {
+  float4 fx[20 * 20];                  // flux, origin (i0 - 2, j0 - 2)
+  float h[FB * FB];                    // h, origin (i0 - 4, j0 - 4)
+  float al[18 * 18];                   // alpha, origin (i0 - 1, j0 - 1)
+  uint32_t act[9];                     // ACTIVE of the 3 x 3 tiles around this one
+  uint64_t bar;
+};
+template <int MODE>
+__device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
+  __shared__ __align__(128) LaSmem S;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
+  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
+  const bool in = i < (int)F.w && j < (int)F.h;
+  const uint32_t c = in ? idx(F, i, j) : 0u;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) {
+    if (in) {
+      F.delta_old[c] = F.delta[c];
+      F.h_next[c] = F.hh[c];
+    }
+    return;
+  }
+  const cf_params& P = F.P->p;
+  // the tensor loads first (the flux as floats, 4 a cell), then the block's
+  // own loads while they are in flight
+  const bool tma = F.tmap != nullptr;
+  if (tma) {
+    tma_block_arm(&S.bar, tid);
+    if (tid == 0) {
+      mbar_arrive_expect_tx(&S.bar, 20u * 20u * 16u + FB * FB * 4u);
+      tma_load_2d(S.fx, F.tmap + MAP_FLUX, 4 * (i0 - 2), j0 - 2, &S.bar);
+      tma_load_2d(S.h, F.tmap + MAP_H, i0 - 4, j0 - 4, &S.bar);
+    }
+  }
+  const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (in) F.delta_old[c] = F.delta[c];
+  if (tid < 9) {
+    const int tx = (int)T.x + tid % 3 - 1, ty = (int)T.y + tid / 3 - 1;
+    S.act[tid] = tx >= 0 && ty >= 0 && tx < (int)F.tw && ty < (int)F.th ? F.tile_flags[tx + ty * F.tw] & ACTIVE : 0u;
+  }
+  if (tma) {
+    if (!tma_block_wait(F, &S.bar, tid)) return;
+  } else {
+    for (int q = tid; q < 20 * 20; q += 256) {
+      const int x = i0 - 2 + q % 20, y = j0 - 2 + q / 20;
+      S.fx[q] = in_grid(F, x, y) ? F.flux[idx(F, x, y)] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int q = tid; q < FB * FB; q += 256) {
+      const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
+      S.h[q] = in_grid(F, x, y) ? F.hh[idx(F, x, y)] : 0.f;
+    }
+    __syncthreads();
+  }
+  // cell_active for cells within 2 of the tile: in the grid and in an active tile
+  auto live = [&](int x, int y) {
+    return in_grid(F, x, y) && S.act[((y >> 4) - (int)T.y + 1) * 3 + ((x >> 4) - (int)T.x + 1)] != 0u;
+  };
+  for (int q = tid; q < 18 * 18; q += 256) {
+    const int px = q % 18, py = q / 18, x = i0 - 1 + px, y = j0 - 1 + py;
+    float a = 1.f;  // cells outside the grid or in inactive tiles: apply reads no alpha of them
+    if (live(x, y)) {
+      const float4* f = &S.fx[(py + 1) * 20 + px + 1];
+      float out = fmaxf(f[0].x, 0.f) + fmaxf(f[0].y, 0.f) + fmaxf(f[0].z, 0.f) + fmaxf(f[0].w, 0.f);
+      if (x > 0 && live(x - 1, y)) out += fmaxf(-f[-1].x, 0.f);
+      if (y > 0 && live(x, y - 1)) out += fmaxf(-f[-20].y, 0.f);
+      if (x > 0 && y > 0 && live(x - 1, y - 1)) out += fmaxf(-f[-21].z, 0.f);
+      if (x > 0 && y + 1 < (int)F.h && live(x - 1, y + 1)) out += fmaxf(-f[19].w, 0.f);
+      if (out > 0.f) a = fminf(1.f, 0.5f * S.h[(py + 3) * FB + px + 3] * P.dx / (P.dt * out));
+    }
+    S.al[q] = a;
+  }
+  __syncthreads();
+  bool moved = false;
+  if (in) {
+    const int a0 = ((int)threadIdx.y + 1) * 18 + (int)threadIdx.x + 1;  // the cell in al
+    const int f0 = ((int)threadIdx.y + 2) * 20 + (int)threadIdx.x + 2;  // and in fx
+    const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
+    const bool has[4] = {hx, hy, hx && hy, hx && hm};
+    const uint32_t cbs[4] = {c + 1, c + F.w, c + F.w + 1, c - F.w + 1};
+    const int abx[4] = {a0 + 1, a0 + 18, a0 + 19, a0 - 17};
+    const float ac = S.al[a0];
+    const float4 f4 = S.fx[f0];
+    const float f[4] = {f4.x, f4.y, f4.z, f4.w};
+    float best = 0.f, div = 0.f;
+    uint32_t src = c;
+    float accv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float q = f[k], ab = ac;
+      if (q < 0.f && has[k]) {
+        ab = S.al[abx[k]];
+        if (-q * ab > best) { best = -q * ab; src = cbs[k]; }
+      }
+      div += q * ab;
+      accv[k] = q * ab;
+    }
+    auto nb_face = [&](float q, float an, uint32_t cn) {
+      if (q < 0.f) an = ac;
+      if (q * an > best) { best = q * an; src = cn; }
+      div -= q * an;
+    };
+    if (hl && live(i - 1, j)) nb_face(S.fx[f0 - 1].x, S.al[a0 - 1], c - 1);
+    if (hm && live(i, j - 1)) nb_face(S.fx[f0 - 20].y, S.al[a0 - 18], c - F.w);
+    if (hl && hm && live(i - 1, j - 1)) nb_face(S.fx[f0 - 21].z, S.al[a0 - 19], c - F.w - 1);
+    if (hl && hy && live(i - 1, j + 1)) nb_face(S.fx[f0 + 19].w, S.al[a0 + 17], c + F.w - 1);
+    const float h0 = S.h[((int)threadIdx.y + 4) * FB + (int)threadIdx.x + 4];
+    float hn = fmaxf(h0 - P.dt * div * P.inv_dx, 0.f);
+    if (hn < h0 && hn < DRAINED_FILM) hn = 0.f;
+    F.h_next[c] = hn;
+    moved = fabsf(hn - h0) > MOVE_EPS;
+    if (h0 <= 0.f && src != c) {
+      set_rheo<MODE>(F, c, rmu<MODE>(F, src), rtau<MODE>(F, src), rn<MODE>(F, src));
+      backfill<MODE>(F, c, src, hn);
+    }
+    F.acc[c] = make_float4(a4.x + accv[0] * P.dt, a4.y + accv[1] * P.dt, a4.z + accv[2] * P.dt,
+                           a4.w + accv[3] * P.dt);
+  }
+  if (__syncthreads_or(moved) && tid == 0) F.tile_moved[T.x + T.y * F.tw] = 1u;
 }
 
 template <int MODE, bool CLEAR>
@@ -932,7 +1067,14 @@ __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
   // ring cells in inactive tiles keep the planes' values
   for (int q = tid; q < 18 * 18; q += 256) {
     const int px = q % 18, py = q / 18, x = i0 - 1 + px, y = j0 - 1 + py;
-    if (!in_grid(F, x, y)) continue;
+    if (!in_grid(F, x, y)) {
+      // the height of the cell it reflects to (every such cell the faces
+      // read lies in the staged box)
+      const int rx = refl_i(F, x) - i0 + 4, ry = refl_j(F, y) - j0 + 4;
+      S.hr[q] = rx >= 0 && rx < FB && ry >= 0 && ry < FB ? S.h[ry * FB + rx] : 0.f;
+      continue;
+    }
+    S.hr[q] = S.h[box(x, y)];
     const uint32_t c = idx(F, x, y);
     if (!cell_active(F, x, y)) {
       S.pres[q] = F.pres[c];
@@ -979,8 +1121,18 @@ __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
     const int x = i + FACE_DI[k], y = j + FACE_DJ[k];
     tile_faces_add(S.faces, k, in && in_grid(F, x, y) && cell_active(F, x, y) && 0.5f * (hc + S.h[box(x, y)]) > 0.f);
   }
+  // on the grid's edges: the ring positions outside the grid take the
+  // pressure of the cell they reflect to
+  if (i0 == 0 || j0 == 0 || i0 + 17 > (int)F.w || j0 + 17 > (int)F.h) {
+    for (int q = tid; q < 18 * 18; q += 256) {
+      const int x = i0 - 1 + q % 18, y = j0 - 1 + q / 18;
+      if (in_grid(F, x, y)) continue;
+      const int rx = refl_i(F, x) - i0 + 1, ry = refl_j(F, y) - j0 + 1;
+      if (rx >= 0 && rx < 18 && ry >= 0 && ry < 18) S.pres[q] = S.pres[ry * 18 + rx];
+    }
+  }
   __syncthreads();
-  const PtTile pt{F, S.pres, S.tmp, S.h, i0, j0};
+  const PtTile pt{S.pres, S.tmp, S.hr, i0, j0};
   float* fl = reinterpret_cast<float*>(F.flux);
   tile_faces_each(F, T, S.faces, [&](int k, int fi, int fj, uint32_t fc) {
     fl[4 * (size_t)fc + k] = face_k<MODE>(F, D, pt, fi, fj, k).q;
@@ -1824,8 +1976,10 @@ template <int MODE, bool WALK = false>
 __global__ void __launch_bounds__(128, 8) kp_apply(PACKED_ARGS) { PACKED_TILES(WALK, apply_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILES(WALK, copy_delta_tile(F, T)) }
-template <bool WALK = false>
-__global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILES(WALK, nose_tile(F, T)) }
+template <bool NEXT, bool WALK = false>
+__global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILES(WALK, nose_tile<NEXT>(F, T)) }
+template <int MODE, bool WALK = false>
+__global__ void __launch_bounds__(256, 6) kp_limit_apply(PACKED_ARGS) { PACKED_TILES(WALK, limit_apply_tile<MODE>(F, T)) }
 
 template <int MODE, bool WALK = false>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILES(WALK, reduce16_tile<MODE>(F, T)) }
@@ -1950,10 +2104,11 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     // frame's first)
     if (s == 0 && isteps == 0) tl(kp_flow<MODE, true, false>, kp_flow<MODE, true, true>, b);
     else tl(kp_flow<MODE, false, false>, kp_flow<MODE, false, true>, b);
-    tl(kp_limiter<false>, kp_limiter<true>, dim3(16, 4));
-    tl(kp_apply<MODE, false>, kp_apply<MODE, true>, dim3(16, 8));
-    tl(kp_nose<false>, kp_nose<true>, b);
-    n += 4;
+    // limiter + apply (alpha on chip, new heights to h_next), then the nose,
+    // which commits them
+    tl(kp_limit_apply<MODE, false>, kp_limit_apply<MODE, true>, b);
+    tl(kp_nose<true, false>, kp_nose<true, true>, b);
+    n += 3;
   }
   tl(kp_laplacian<false, false>, kp_laplacian<false, true>, b);
   tl(kp_strata_split<MODE, false>, kp_strata_split<MODE, true>, b);
@@ -2045,8 +2200,10 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "apply") CFK_LAUNCH(kp_apply, nt, dim3(16, 8), st, A, T, nt);
   else if (n == "nose") {
     kp_copy_delta<<<nt, b, 0, st>>>(A, T, nt);  // the snapshot the frame's apply takes
-    kp_nose<<<nt, b, 0, st>>>(A, T, nt);
+    kp_nose<false><<<nt, b, 0, st>>>(A, T, nt);
   }
+  // limiter + apply fused, as the frame runs them: the new heights in h_next
+  else if (n == "limit_apply") CFK_LAUNCH(kp_limit_apply, nt, b, st, A, T, nt);
   else if (n == "strata_split") CFK_LAUNCH(kp_strata_split, nt, b, st, A, T, nt);
   else if (n == "reduce_tiles") launch_reduce(V, mode, st);
   else if (n == "strata_limit") {  // the face flags of the acc_s plane it is given

@@ -69,3 +69,36 @@ def test_flow_equals_separate_dispatches(gp, prec):
         print("%s prec %d: fluxes %d of %d differ in the last bits, tmp %d" % (name, prec, nflux, flux_f.size, ntmp))
         assert np.abs(flux_s).max() > 0.0
         f.close()
+
+
+@pytest.mark.parametrize("prec", [capi.CF_PREC_REFERENCE, capi.CF_PREC_FP32, capi.CF_PREC_BF16])
+def test_limit_apply_equals_separate_dispatches(gp, prec):
+    """The fused limiter + apply (alpha in shared memory, the new heights in
+    h_next) against the limiter and apply dispatches from the same state: the
+    heights, acc, back-filled strata and rheology to rounding, the moved
+    tiles and the nose's delta snapshot exactly."""
+    from canvaz_film.film import Film
+    for name, (cv, sched) in cases(gp):
+        o = gp.oracle_state(cv, sched)
+        f = Film(po.make_settings(cv.settings), cv.w, cv.h, prec)
+        f.set_tables(cv.pigtab, cv.cmf)
+        gp.transfer(o, f)
+        f.set_plane("tile_moved", np.zeros(f.plane("tile_moved").size))
+        f.run("limit_apply")
+        fused = {"h": f.plane("h_next")}
+        for k in ("acc", "mu", "tau", "nn", "strata_h", "strata_cure", "strata_pig", "tile_moved", "delta_old"):
+            fused[k] = f.plane(k)
+        gp.transfer(o, f)
+        f.set_plane("tile_moved", np.zeros(f.plane("tile_moved").size))
+        f.run("limiter")
+        f.run("apply")
+        sep = {k: f.plane(k) for k in fused}
+        for k in ("tile_moved", "delta_old"):
+            np.testing.assert_array_equal(fused[k], sep[k], err_msg="%s %s" % (name, k))
+        diffs = {k: close(fused[k], sep[k], "%s %s" % (name, k)) for k in ("h", "acc", "mu", "tau", "nn", "strata_h",
+                                                                        "strata_cure", "strata_pig")}
+        moved = np.count_nonzero(sep["h"] != o.buf("h"))  # the transferred state holds f32-rounded heights
+        print("%s prec %d: values differing in the last bits %s; cells whose height changed %d"
+              % (name, prec, diffs, moved))
+        assert moved > 0
+        f.close()
