@@ -116,6 +116,7 @@ static void fill_devparams(cf_film* f, DevParams& D, float dt_max) {
   D.cox_theta = std::atan(P.ein[0]);
   D.cox_span = std::fmax(P.front[0] - D.hold1, 1e-6f);
   D.cox_adv = std::fmin(D.cox_theta + P.front2[0], 3.1f);
+  D.gc_max = P.phys[1] / (1e-3f * 1e-3f);  // one f32 division, as each face did it
 }
 
 // Copies the host-packed params to the device on `st`.  The pinned staging

@@ -44,6 +44,7 @@ struct DevParams {
   float cox_theta;      // atan(tan theta) (film.wgsl:236-244)
   float cox_span;       // max(front.x - hold_level(1), 1e-6)
   float cox_adv;        // min(theta + front2.x, 3.1)
+  float gc_max;         // sigma / (1 mm)^2, the capillary gradient cap of yield_cap (film.wgsl:44-49)
 };
 
 // Scalars of a film's implicit CG solve (film.wgsl cg_s[0], cg_s[1]) and the
@@ -596,7 +597,7 @@ __device__ FaceOut face(const Film& F, const DevParams& D, const Pair& pt, uint3
   float2 yc = make_float2(gcap.x * fcap, gcap.y * fcap);
   {
     float gcl = sqrtf(yc.x * yc.x + yc.y * yc.y);
-    float gc_max = P.phys[1] / (1e-3f * 1e-3f);
+    const float gc_max = D.gc_max;
     if (!(ty <= 0.f || gcl <= gc_max)) {
       float sc = gc_max / gcl;
       yc.x = yc.x * sc;

@@ -675,7 +675,7 @@ __device__ __forceinline__ bool tma_block_wait(const Film& F, uint64_t* bar, int
   if (tid == 0) mbar_inval(bar);
   return true;
 }
-template <int MODE, bool RHEO, class Smem>
+template <int MODE, bool RHEO, class Smem, int NT = 256>
 __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0, int tid, bool rheo = RHEO) {
   constexpr bool B16 = MODE == CF_PREC_BF16;
   if (F.tmap != nullptr) {
@@ -697,7 +697,7 @@ __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0
     }
     return tma_block_wait(F, &S.bar, tid);
   }
-  for (int q = tid; q < FB * FB; q += 256) {
+  for (int q = tid; q < FB * FB; q += NT) {
     const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
     const bool in = in_grid(F, x, y);
     const uint32_t c = in ? idx(F, x, y) : 0u;
@@ -708,7 +708,7 @@ __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0
   if constexpr (RHEO) {
     if (rheo) {
       if constexpr (B16) {
-        for (int q = tid; q < 32 * FB; q += 256) {
+        for (int q = tid; q < 32 * FB; q += NT) {
           const int x = i0 - 8 + q % 32, y = j0 - 4 + q / 32;
           const bool in = in_grid(F, x, y);
           const uint32_t c = in ? idx(F, x, y) : 0u;
@@ -717,7 +717,7 @@ __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0
           for (int r = 0; r < 3; ++r) reinterpret_cast<uint16_t*>(S.rh[r])[q] = in ? pl[r][c] : (uint16_t)0;
         }
       } else {
-        for (int q = tid; q < FB * FB; q += 256) {
+        for (int q = tid; q < FB * FB; q += NT) {
           const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
           const bool in = in_grid(F, x, y);
           const uint32_t c = in ? idx(F, x, y) : 0u;
@@ -733,9 +733,9 @@ __device__ __forceinline__ bool stage_box(const Film& F, Smem& S, int i0, int j0
 }
 // Surface levels (film.wgsl:147-151) of the tile + 2 rings, reflected at the
 // grid's edges as the laplacian reads them.
-template <class Smem>
+template <class Smem, int NT = 256>
 __device__ __forceinline__ void tile_surface(const Film& F, const cf_params& P, Smem& S, int i0, int j0, int tid) {
-  for (int q = tid; q < 20 * 20; q += 256) {
+  for (int q = tid; q < 20 * 20; q += NT) {
     const int b = (refl_j(F, j0 - 2 + q / 20) - j0 + 4) * FB + (refl_i(F, i0 - 2 + q % 20) - i0 + 4);
     const float hv = S.h[b];
     int ox, oy;
@@ -783,22 +783,28 @@ struct LapSmem {
 };
 template <bool CLEAR>
 __device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
+  // 128 threads per tile, 2 cells each (rows y and y + 8): twice the tiles
+  // of 256-thread blocks in flight on an SM, to hide the staging's latency
   __shared__ __align__(128) LapSmem S;
   if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
   const cf_params& P = F.P->p;
   const int tid = threadIdx.y * 16 + threadIdx.x;
   const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
-  if (!stage_box<CF_PREC_FP32, false>(F, S, i0, j0, tid)) return;
-  tile_surface(F, P, S, i0, j0, tid);
+  if (!stage_box<CF_PREC_FP32, false, LapSmem, 128>(F, S, i0, j0, tid)) return;
+  tile_surface<LapSmem, 128>(F, P, S, i0, j0, tid);
   __syncthreads();
-  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
-  if (i >= (int)F.w || j >= (int)F.h) return;
-  const uint32_t c = idx(F, i, j);
-  if (CLEAR) {
-    F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-    F.h_frame[c] = S.h[(threadIdx.y + 4) * FB + threadIdx.x + 4];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int ty = (int)threadIdx.y + 8 * r;
+    const int i = i0 + (int)threadIdx.x, j = j0 + ty;
+    if (i >= (int)F.w || j >= (int)F.h) continue;
+    const uint32_t c = idx(F, i, j);
+    if (CLEAR) {
+      F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+      F.h_frame[c] = S.h[(ty + 4) * FB + threadIdx.x + 4];
+    }
+    F.pres[c] = tile_pres(F, P, S, i0, j0, (int)threadIdx.x + 1, ty + 1, i, j, c);
   }
-  F.pres[c] = tile_pres(F, P, S, i0, j0, (int)threadIdx.x + 1, (int)threadIdx.y + 1, i, j, c);
 }
 
 // Boxes of two 4-byte planes (24 x 24 cells from (i0 - 4, j0 - 4), zero
@@ -806,6 +812,7 @@ __device__ __forceinline__ void laplacian_tile(const Film& F, TileId T) {
 // where the film has descriptors, else loads by the block's threads.
 // Returns false (counted in the film's stats) when the tensor loads did not
 // arrive within the wait limit.
+template <int NT = 256>
 __device__ __forceinline__ bool stage_pair(const Film& F, uint64_t* bar, int i0, int j0, int tid, uint32_t* da,
                                            int ma, const uint32_t* sa, uint32_t* db, int mb, const uint32_t* sb) {
   if (F.tmap != nullptr) {
@@ -817,7 +824,7 @@ __device__ __forceinline__ bool stage_pair(const Film& F, uint64_t* bar, int i0,
     }
     return tma_block_wait(F, bar, tid);
   }
-  for (int q = tid; q < FB * FB; q += 256) {
+  for (int q = tid; q < FB * FB; q += NT) {
     const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
     const bool in = in_grid(F, x, y);
     const uint32_t c = in ? idx(F, x, y) : 0u;
@@ -840,18 +847,8 @@ struct NoseSmem {
   uint64_t bar;
 };
 template <bool NEXT>
-__device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
-  __shared__ __align__(128) NoseSmem S;
-  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
-  const cf_params& P = F.P->p;
-  const int tid = threadIdx.y * 16 + threadIdx.x;
-  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
-  const float* hs = NEXT ? F.h_next : F.hh;
-  if (!stage_pair(F, &S.bar, i0, j0, tid, reinterpret_cast<uint32_t*>(S.h), NEXT ? MAP_H_NEXT : MAP_H,
-                  reinterpret_cast<const uint32_t*>(hs), S.dl, MAP_DELTA_OLD, F.delta_old))
-    return;
-  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
-  if (i >= (int)F.w || j >= (int)F.h) return;
+__device__ __forceinline__ void nose_cell(const Film& F, const cf_params& P, const NoseSmem& S, const float* hs, int i0,
+                                          int j0, int i, int j) {
   const uint32_t c = idx(F, i, j);
   auto at = [&](int x, int y) { return (y - j0 + 4) * FB + (x - i0 + 4); };
   if (NEXT) F.hh[c] = S.h[at(i, j)];
@@ -895,6 +892,24 @@ __device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
   F.fnorm[c] = bd <= 3.0f ? front_normal_at(F, P, i, j, [&](int x, int y) { return S.h[at(x, y)]; })
                           : make_float2(0.f, 0.f);
 }
+template <bool NEXT>
+__device__ __forceinline__ void nose_tile(const Film& F, TileId T) {
+  // 128 threads per tile, 2 cells each (rows y and y + 8), as the laplacian
+  __shared__ __align__(128) NoseSmem S;
+  if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
+  const cf_params& P = F.P->p;
+  const int tid = threadIdx.y * 16 + threadIdx.x;
+  const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
+  const float* hs = NEXT ? F.h_next : F.hh;
+  if (!stage_pair<128>(F, &S.bar, i0, j0, tid, reinterpret_cast<uint32_t*>(S.h), NEXT ? MAP_H_NEXT : MAP_H,
+                       reinterpret_cast<const uint32_t*>(hs), S.dl, MAP_DELTA_OLD, F.delta_old))
+    return;
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y + 8 * r;
+    if (i < (int)F.w && j < (int)F.h) nose_cell<NEXT>(F, P, S, hs, i0, j0, i, j);
+  }
+}
 
 // ---- limiter + apply, fused ----
 // film.wgsl:516-537 (limiter) and 539-561, 803-863 (apply) for one tile.
@@ -915,19 +930,80 @@ struct LaSmem {
   uint32_t act[9];                     // ACTIVE of the 3 x 3 tiles around this one
   uint64_t bar;
 };
+// apply (film.wgsl:539-561, 803-863) of cell (i, j) = (i0 + tx, j0 + ty)
+// from the block's shared memory; returns whether its height moved
+template <int MODE>
+__device__ __forceinline__ bool apply_cell(const Film& F, const cf_params& P, const LaSmem& S, TileId T, int tx, int ty,
+                                           float4 a4) {
+  const int i = (int)T.x * 16 + tx, j = (int)T.y * 16 + ty;
+  const uint32_t c = idx(F, i, j);
+  auto live = [&](int x, int y) {
+    return in_grid(F, x, y) && S.act[((y >> 4) - (int)T.y + 1) * 3 + ((x >> 4) - (int)T.x + 1)] != 0u;
+  };
+  const int a0 = (ty + 1) * 18 + tx + 1;  // the cell in al
+  const int f0 = (ty + 2) * 20 + tx + 2;  // and in fx
+  const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
+  const bool has[4] = {hx, hy, hx && hy, hx && hm};
+  const uint32_t cbs[4] = {c + 1, c + F.w, c + F.w + 1, c - F.w + 1};
+  const int abx[4] = {a0 + 1, a0 + 18, a0 + 19, a0 - 17};
+  const float ac = S.al[a0];
+  const float4 f4 = S.fx[f0];
+  const float f[4] = {f4.x, f4.y, f4.z, f4.w};
+  float best = 0.f, div = 0.f;
+  uint32_t src = c;
+  float accv[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float q = f[k], ab = ac;
+    if (q < 0.f && has[k]) {
+      ab = S.al[abx[k]];
+      if (-q * ab > best) { best = -q * ab; src = cbs[k]; }
+    }
+    div += q * ab;
+    accv[k] = q * ab;
+  }
+  auto nb_face = [&](float q, float an, uint32_t cn) {
+    if (q < 0.f) an = ac;
+    if (q * an > best) { best = q * an; src = cn; }
+    div -= q * an;
+  };
+  if (hl && live(i - 1, j)) nb_face(S.fx[f0 - 1].x, S.al[a0 - 1], c - 1);
+  if (hm && live(i, j - 1)) nb_face(S.fx[f0 - 20].y, S.al[a0 - 18], c - F.w);
+  if (hl && hm && live(i - 1, j - 1)) nb_face(S.fx[f0 - 21].z, S.al[a0 - 19], c - F.w - 1);
+  if (hl && hy && live(i - 1, j + 1)) nb_face(S.fx[f0 + 19].w, S.al[a0 + 17], c + F.w - 1);
+  const float h0 = S.h[(ty + 4) * FB + tx + 4];
+  float hn = fmaxf(h0 - P.dt * div * P.inv_dx, 0.f);
+  if (hn < h0 && hn < DRAINED_FILM) hn = 0.f;
+  F.h_next[c] = hn;
+  if (h0 <= 0.f && src != c) {
+    set_rheo<MODE>(F, c, rmu<MODE>(F, src), rtau<MODE>(F, src), rn<MODE>(F, src));
+    backfill<MODE>(F, c, src, hn);
+  }
+  F.acc[c] = make_float4(a4.x + accv[0] * P.dt, a4.y + accv[1] * P.dt, a4.z + accv[2] * P.dt, a4.w + accv[3] * P.dt);
+  return fabsf(hn - h0) > MOVE_EPS;
+}
 template <int MODE>
 __device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
+  // 128 threads per tile, 2 cells each (rows y and y + 8)
   __shared__ __align__(128) LaSmem S;
   const int tid = threadIdx.y * 16 + threadIdx.x;
   const int i0 = (int)T.x * 16, j0 = (int)T.y * 16;
-  const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
-  const bool in = i < (int)F.w && j < (int)F.h;
-  const uint32_t c = in ? idx(F, i, j) : 0u;
+  const int i = i0 + (int)threadIdx.x;
+  bool in[2];
+  uint32_t c[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int j = j0 + (int)threadIdx.y + 8 * r;
+    in[r] = i < (int)F.w && j < (int)F.h;
+    c[r] = in[r] ? idx(F, i, j) : 0u;
+  }
   if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) {
-    if (in) {
-      F.delta_old[c] = F.delta[c];
-      F.h_next[c] = F.hh[c];
-    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+      if (in[r]) {
+        F.delta_old[c[r]] = F.delta[c[r]];
+        F.h_next[c[r]] = F.hh[c[r]];
+      }
     return;
   }
   const cf_params& P = F.P->p;
@@ -942,8 +1018,12 @@ __device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
       tma_load_2d(S.h, F.tmap + MAP_H, i0 - 4, j0 - 4, &S.bar);
     }
   }
-  const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
-  if (in) F.delta_old[c] = F.delta[c];
+  float4 a4[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    a4[r] = in[r] ? F.acc[c[r]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in[r]) F.delta_old[c[r]] = F.delta[c[r]];
+  }
   if (tid < 9) {
     const int tx = (int)T.x + tid % 3 - 1, ty = (int)T.y + tid / 3 - 1;
     S.act[tid] = tx >= 0 && ty >= 0 && tx < (int)F.tw && ty < (int)F.th ? F.tile_flags[tx + ty * F.tw] & ACTIVE : 0u;
@@ -951,11 +1031,11 @@ __device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
   if (tma) {
     if (!tma_block_wait(F, &S.bar, tid)) return;
   } else {
-    for (int q = tid; q < 20 * 20; q += 256) {
+    for (int q = tid; q < 20 * 20; q += 128) {
       const int x = i0 - 2 + q % 20, y = j0 - 2 + q / 20;
       S.fx[q] = in_grid(F, x, y) ? F.flux[idx(F, x, y)] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int q = tid; q < FB * FB; q += 256) {
+    for (int q = tid; q < FB * FB; q += 128) {
       const int x = i0 - 4 + q % FB, y = j0 - 4 + q / FB;
       S.h[q] = in_grid(F, x, y) ? F.hh[idx(F, x, y)] : 0.f;
     }
@@ -965,7 +1045,8 @@ __device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
   auto live = [&](int x, int y) {
     return in_grid(F, x, y) && S.act[((y >> 4) - (int)T.y + 1) * 3 + ((x >> 4) - (int)T.x + 1)] != 0u;
   };
-  for (int q = tid; q < 18 * 18; q += 256) {
+  // limiter (film.wgsl:516-537) on the tile + 1 ring
+  for (int q = tid; q < 18 * 18; q += 128) {
     const int px = q % 18, py = q / 18, x = i0 - 1 + px, y = j0 - 1 + py;
     float a = 1.f;  // cells outside the grid or in inactive tiles: apply reads no alpha of them
     if (live(x, y)) {
@@ -981,50 +1062,9 @@ __device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
   }
   __syncthreads();
   bool moved = false;
-  if (in) {
-    const int a0 = ((int)threadIdx.y + 1) * 18 + (int)threadIdx.x + 1;  // the cell in al
-    const int f0 = ((int)threadIdx.y + 2) * 20 + (int)threadIdx.x + 2;  // and in fx
-    const bool hx = i + 1 < (int)F.w, hy = j + 1 < (int)F.h, hm = j > 0, hl = i > 0;
-    const bool has[4] = {hx, hy, hx && hy, hx && hm};
-    const uint32_t cbs[4] = {c + 1, c + F.w, c + F.w + 1, c - F.w + 1};
-    const int abx[4] = {a0 + 1, a0 + 18, a0 + 19, a0 - 17};
-    const float ac = S.al[a0];
-    const float4 f4 = S.fx[f0];
-    const float f[4] = {f4.x, f4.y, f4.z, f4.w};
-    float best = 0.f, div = 0.f;
-    uint32_t src = c;
-    float accv[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      float q = f[k], ab = ac;
-      if (q < 0.f && has[k]) {
-        ab = S.al[abx[k]];
-        if (-q * ab > best) { best = -q * ab; src = cbs[k]; }
-      }
-      div += q * ab;
-      accv[k] = q * ab;
-    }
-    auto nb_face = [&](float q, float an, uint32_t cn) {
-      if (q < 0.f) an = ac;
-      if (q * an > best) { best = q * an; src = cn; }
-      div -= q * an;
-    };
-    if (hl && live(i - 1, j)) nb_face(S.fx[f0 - 1].x, S.al[a0 - 1], c - 1);
-    if (hm && live(i, j - 1)) nb_face(S.fx[f0 - 20].y, S.al[a0 - 18], c - F.w);
-    if (hl && hm && live(i - 1, j - 1)) nb_face(S.fx[f0 - 21].z, S.al[a0 - 19], c - F.w - 1);
-    if (hl && hy && live(i - 1, j + 1)) nb_face(S.fx[f0 + 19].w, S.al[a0 + 17], c + F.w - 1);
-    const float h0 = S.h[((int)threadIdx.y + 4) * FB + (int)threadIdx.x + 4];
-    float hn = fmaxf(h0 - P.dt * div * P.inv_dx, 0.f);
-    if (hn < h0 && hn < DRAINED_FILM) hn = 0.f;
-    F.h_next[c] = hn;
-    moved = fabsf(hn - h0) > MOVE_EPS;
-    if (h0 <= 0.f && src != c) {
-      set_rheo<MODE>(F, c, rmu<MODE>(F, src), rtau<MODE>(F, src), rn<MODE>(F, src));
-      backfill<MODE>(F, c, src, hn);
-    }
-    F.acc[c] = make_float4(a4.x + accv[0] * P.dt, a4.y + accv[1] * P.dt, a4.z + accv[2] * P.dt,
-                           a4.w + accv[3] * P.dt);
-  }
+  for (int r = 0; r < 2; ++r)
+    if (in[r]) moved = apply_cell<MODE>(F, P, S, T, (int)threadIdx.x, (int)threadIdx.y + 8 * r, a4[r]) || moved;
   if (__syncthreads_or(moved) && tid == 0) F.tile_moved[T.x + T.y * F.tw] = 1u;
 }
 
@@ -1398,13 +1438,10 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   __shared__ FastShade sh;
   __shared__ float red_h[8], red_m[8];
   const int tid = threadIdx.y * 16 + threadIdx.x;
-  load_tables(F, sh.tab, sh.cm, sh.ltab, tid, 256);
-  for (int e = tid; e < 16 * 24; e += 256) {
-    const int b = e / 24, r = e % 24;
-    sh.kst[e] = F.pigtab[(r < 12 ? r : r - 12) * 40 + (r < 12 ? 0 : 16) + b];
-  }
+  // the CMF table (all a cached colour needs) is loaded with the cells' own
+  // loads; the pigment tables only in blocks that shade a cell
+  const float cmv = tid < 48 ? F.cmf[tid] : 0.f;
   if (tid == 0) sh.count = 0u;
-  __syncthreads();
   const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   const cf_params& P = F.P->p;
   float hm = 0.f, mm = 1e9f;
@@ -1415,6 +1452,16 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
     const float hc = F.hh[c];
     if (hc > 4.0f * P.ein[3]) { hm = hc; mm = rmu<MODE>(F, c); }
     need = strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
+  }
+  if (tid < 48) sh.cm[tid] = cmv;
+  if (__syncthreads_or(need == FAST_SHADE)) {
+    for (int q = tid; q < 480; q += 256) sh.tab[q] = F.pigtab[q];
+    if (tid < 12) sh.ltab[tid] = logf(fmaxf(F.pigtab[tid * 40 + 32], 1e-3f));
+    for (int e = tid; e < 16 * 24; e += 256) {
+      const int b = e / 24, r = e % 24;
+      sh.kst[e] = F.pigtab[(r < 12 ? r : r - 12) * 40 + (r < 12 ? 0 : 16) + b];
+    }
+    __syncthreads();
   }
   if (need == FAST_COLOR) fast_color_cached(F, c, sh, tid);
   const bool shade = need == FAST_SHADE;
@@ -1958,7 +2005,7 @@ __global__ void __launch_bounds__(256, 8) kp_cure(PACKED_ARGS) { PACKED_TILES(WA
 template <bool WALK = false>
 __global__ void __launch_bounds__(256) kp_clear_acc(PACKED_ARGS) { PACKED_TILES(WALK, clear_acc_tile(F, T)) }
 template <bool CLEAR, bool WALK = false>
-__global__ void __launch_bounds__(256) kp_laplacian(PACKED_ARGS) { PACKED_TILES(WALK, laplacian_tile<CLEAR>(F, T)) }
+__global__ void __launch_bounds__(128, 16) kp_laplacian(PACKED_ARGS) { PACKED_TILES(WALK, laplacian_tile<CLEAR>(F, T)) }
 template <int MODE, bool WALK = false>
 __global__ void __launch_bounds__(256) kp_plug(PACKED_ARGS) { PACKED_TILES(WALK, plug_tile<MODE>(F, T)) }
 // three blocks per SM: the face code needs no more than 64 registers, and
@@ -1968,7 +2015,7 @@ __global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILES(
 template <int MODE, bool CLEAR, bool WALK = false>
 __global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILES(WALK, flow_tile<MODE, CLEAR>(F, T)) }
 template <int MODE, bool WALK = false>
-__global__ void __launch_bounds__(256, 6) kp_strata_split(PACKED_ARGS) { PACKED_TILES(WALK, strata_split_tile<MODE>(F, T)) }
+__global__ void __launch_bounds__(256, 8) kp_strata_split(PACKED_ARGS) { PACKED_TILES(WALK, strata_split_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILES(WALK, limiter_tile(F, T)) }
 // eight blocks of 128 per SM (64 registers for the two cells' loads in flight)
@@ -1977,9 +2024,9 @@ __global__ void __launch_bounds__(128, 8) kp_apply(PACKED_ARGS) { PACKED_TILES(W
 template <bool WALK = false>
 __global__ void __launch_bounds__(256) kp_copy_delta(PACKED_ARGS) { PACKED_TILES(WALK, copy_delta_tile(F, T)) }
 template <bool NEXT, bool WALK = false>
-__global__ void __launch_bounds__(256, 8) kp_nose(PACKED_ARGS) { PACKED_TILES(WALK, nose_tile<NEXT>(F, T)) }
+__global__ void __launch_bounds__(128, 16) kp_nose(PACKED_ARGS) { PACKED_TILES(WALK, nose_tile<NEXT>(F, T)) }
 template <int MODE, bool WALK = false>
-__global__ void __launch_bounds__(256, 6) kp_limit_apply(PACKED_ARGS) { PACKED_TILES(WALK, limit_apply_tile<MODE>(F, T)) }
+__global__ void __launch_bounds__(128, 16) kp_limit_apply(PACKED_ARGS) { PACKED_TILES(WALK, limit_apply_tile<MODE>(F, T)) }
 
 template <int MODE, bool WALK = false>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILES(WALK, reduce16_tile<MODE>(F, T)) }
@@ -2095,8 +2142,8 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
   const uint32_t isteps = V.implicit_steps;
   if (substeps == 0 && isteps == 0) { tl(kp_clear_acc<false>, kp_clear_acc<true>, b); ++n; }
   for (uint32_t s = 0; s < isteps; ++s) {
-    if (s == 0) kp_laplacian<true><<<nt, b, 0, st>>>(A, T, nt);
-    else kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+    if (s == 0) kp_laplacian<true><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
+    else kp_laplacian<false><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
     n += 1 + launch_cg_step(V, MODE, s, V.implicit_iters, V.cap_implicit, st);
   }
   for (uint32_t s = 0; s < substeps; ++s) {
@@ -2106,11 +2153,11 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     else tl(kp_flow<MODE, false, false>, kp_flow<MODE, false, true>, b);
     // limiter + apply (alpha on chip, new heights to h_next), then the nose,
     // which commits them
-    tl(kp_limit_apply<MODE, false>, kp_limit_apply<MODE, true>, b);
-    tl(kp_nose<true, false>, kp_nose<true, true>, b);
+    tl(kp_limit_apply<MODE, false>, kp_limit_apply<MODE, true>, dim3(16, 8));
+    tl(kp_nose<true, false>, kp_nose<true, true>, dim3(16, 8));
     n += 3;
   }
-  tl(kp_laplacian<false, false>, kp_laplacian<false, true>, b);
+  tl(kp_laplacian<false, false>, kp_laplacian<false, true>, dim3(16, 8));
   tl(kp_strata_split<MODE, false>, kp_strata_split<MODE, true>, b);
   tl(kp_strata_fast<MODE, false>, kp_strata_fast<MODE, true>, b);  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
@@ -2188,7 +2235,7 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   }
   else if (n == "cure_step") { launch_compose(V, mode, 0, st); launch_cure(V, mode, st); }
   else if (n == "clear_acc") kp_clear_acc<<<nt, b, 0, st>>>(A, T, nt);
-  else if (n == "laplacian") kp_laplacian<false><<<nt, b, 0, st>>>(A, T, nt);
+  else if (n == "laplacian") kp_laplacian<false><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
   else if (n == "plug") CFK_LAUNCH(kp_plug, nt, b, st, A, T, nt);
   else if (n == "fluxes") CFK_LAUNCH(kp_fluxes, nt, b, st, A, T, nt);
   else if (n == "flow") {  // laplacian + plug + fluxes fused, as the frame runs them
@@ -2200,10 +2247,10 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "apply") CFK_LAUNCH(kp_apply, nt, dim3(16, 8), st, A, T, nt);
   else if (n == "nose") {
     kp_copy_delta<<<nt, b, 0, st>>>(A, T, nt);  // the snapshot the frame's apply takes
-    kp_nose<false><<<nt, b, 0, st>>>(A, T, nt);
+    kp_nose<false><<<nt, dim3(16, 8), 0, st>>>(A, T, nt);
   }
   // limiter + apply fused, as the frame runs them: the new heights in h_next
-  else if (n == "limit_apply") CFK_LAUNCH(kp_limit_apply, nt, b, st, A, T, nt);
+  else if (n == "limit_apply") CFK_LAUNCH(kp_limit_apply, nt, dim3(16, 8), st, A, T, nt);
   else if (n == "strata_split") CFK_LAUNCH(kp_strata_split, nt, b, st, A, T, nt);
   else if (n == "reduce_tiles") launch_reduce(V, mode, st);
   else if (n == "strata_limit") {  // the face flags of the acc_s plane it is given
