@@ -1267,6 +1267,12 @@ __device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& 
   // strata_limit alpha below 1 and does strata_update move material into or
   // out of the cell.
   const uint8_t state = F.shade_state[c];
+  // a cell whose cached spectrum may be reused: its 64 bytes are fetched
+  // towards L2 while the strata and face flags load
+  if (state == SHADE_WET) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) asm volatile("prefetch.L2 [%0];" ::"l"(F.spec + (size_t)q * F.n + c));
+  }
   // a cell dry two passes running in an active tile holds zeros in both
   // generations: unless a strata flux reaches it below, nothing to do
   const bool dry2 = act && hc <= 0.f && state == SHADE_DRY2;
@@ -1408,7 +1414,7 @@ __device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params&
   const HalfWarp H(tid & 31);
   const bool dbg = P.flags[0] == 1u;
   const uint32_t n = sh.count;
-  for (uint32_t e = (uint32_t)(tid >> 4); e < n; e += 16u) {
+  for (uint32_t e = (uint32_t)(tid >> 4); e < n; e += 8u) {  // the block's 8 half-warps
     const uint32_t t = sh.list[e];
     const uint32_t c = idx(F, (int)(T.x * 16 + (t & 15u)), (int)(T.y * 16 + (t >> 4)));
     const float hc = sh.h[t];
@@ -1435,44 +1441,55 @@ __device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params&
 // order-independent max / min equal the reference's).
 template <int MODE>
 __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
+  // 128 threads per tile, 2 cells each (slots t and t + 128: rows y and y + 8)
   __shared__ FastShade sh;
-  __shared__ float red_h[8], red_m[8];
+  __shared__ float red_h[4], red_m[4];
   const int tid = threadIdx.y * 16 + threadIdx.x;
   // the CMF table (all a cached colour needs) is loaded with the cells' own
   // loads; the pigment tables only in blocks that shade a cell
   const float cmv = tid < 48 ? F.cmf[tid] : 0.f;
   if (tid == 0) sh.count = 0u;
-  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   const cf_params& P = F.P->p;
   float hm = 0.f, mm = 1e9f;
-  int need = FAST_NOTHING;
-  uint32_t c = 0u;
-  if (i < (int)F.w && j < (int)F.h) {
-    c = idx(F, i, j);
-    const float hc = F.hh[c];
-    if (hc > 4.0f * P.ein[3]) { hm = hc; mm = rmu<MODE>(F, c); }
-    need = strata_fast_cell<MODE>(F, P, T, i, j, c, hc, sh, tid);
+  int need[2];
+  uint32_t c[2];
+#pragma unroll 1
+  for (int r = 0; r < 2; ++r) {
+    const int t = tid + 128 * r;
+    const int i = (int)(T.x * 16 + (t & 15)), j = (int)(T.y * 16 + (t >> 4));
+    need[r] = FAST_NOTHING;
+    c[r] = 0u;
+    if (i < (int)F.w && j < (int)F.h) {
+      c[r] = idx(F, i, j);
+      const float hc = F.hh[c[r]];
+      if (hc > 4.0f * P.ein[3]) { hm = fmaxf(hm, hc); mm = fminf(mm, rmu<MODE>(F, c[r])); }
+      need[r] = strata_fast_cell<MODE>(F, P, T, i, j, c[r], hc, sh, t);
+    }
   }
   if (tid < 48) sh.cm[tid] = cmv;
-  if (__syncthreads_or(need == FAST_SHADE)) {
-    for (int q = tid; q < 480; q += 256) sh.tab[q] = F.pigtab[q];
+  if (__syncthreads_or(need[0] == FAST_SHADE || need[1] == FAST_SHADE)) {
+    for (int q = tid; q < 480; q += 128) sh.tab[q] = F.pigtab[q];
     if (tid < 12) sh.ltab[tid] = logf(fmaxf(F.pigtab[tid * 40 + 32], 1e-3f));
-    for (int e = tid; e < 16 * 24; e += 256) {
+    for (int e = tid; e < 16 * 24; e += 128) {
       const int b = e / 24, r = e % 24;
       sh.kst[e] = F.pigtab[(r < 12 ? r : r - 12) * 40 + (r < 12 ? 0 : 16) + b];
     }
     __syncthreads();
   }
-  if (need == FAST_COLOR) fast_color_cached(F, c, sh, tid);
-  const bool shade = need == FAST_SHADE;
-  // Where at least FAST_SHADE_LANES lanes of the warp have a cell to shade,
-  // each shades its own; where fewer do, the cells are shaded after the
-  // tile's pass by half-warps (fast_shade_cells), which costs about 1/20 of a
-  // warp-wide shade per cell.
-  const unsigned want = __ballot_sync(0xffffffffu, shade);
-  if (shade) {
-    if (__popc(want) >= FAST_SHADE_LANES) fast_shade_lane<MODE>(F, P, c, sh, tid);
-    else list_append(sh.list, &sh.count, (uint32_t)tid);
+#pragma unroll 1
+  for (int r = 0; r < 2; ++r) {
+    const int t = tid + 128 * r;
+    if (need[r] == FAST_COLOR) fast_color_cached(F, c[r], sh, t);
+    const bool shade = need[r] == FAST_SHADE;
+    // Where at least FAST_SHADE_LANES lanes of the warp have a cell to
+    // shade, each shades its own; where fewer do, the cells are shaded after
+    // the tile's pass by half-warps (fast_shade_cells), which costs about
+    // 1/20 of a warp-wide shade per cell.
+    const unsigned want = __ballot_sync(0xffffffffu, shade);
+    if (shade) {
+      if (__popc(want) >= FAST_SHADE_LANES) fast_shade_lane<MODE>(F, P, c[r], sh, t);
+      else list_append(sh.list, &sh.count, (uint32_t)t);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
@@ -1482,7 +1499,7 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
   __syncthreads();
   if (tid == 0) {
 #pragma unroll
-    for (int w = 1; w < 8; ++w) { hm = fmaxf(hm, red_h[w]); mm = fminf(mm, red_m[w]); }
+    for (int w = 1; w < 4; ++w) { hm = fmaxf(hm, red_h[w]); mm = fminf(mm, red_m[w]); }
     if (hm > 0.f) fold_cfl(F.stats, hm, mm);
   }
   fast_shade_cells<MODE>(F, P, T, sh, tid);
@@ -2031,7 +2048,7 @@ __global__ void __launch_bounds__(128, 16) kp_limit_apply(PACKED_ARGS) { PACKED_
 template <int MODE, bool WALK = false>
 __global__ void __launch_bounds__(256) kp_reduce(PACKED_ARGS) { PACKED_TILES(WALK, reduce16_tile<MODE>(F, T)) }
 template <int MODE, bool WALK = false>
-__global__ void __launch_bounds__(256, 6) kp_strata_fast(PACKED_ARGS) { PACKED_TILES(WALK, strata_fast_tile<MODE>(F, T)) }
+__global__ void __launch_bounds__(128, 12) kp_strata_fast(PACKED_ARGS) { PACKED_TILES(WALK, strata_fast_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(256) kp_strata_limit(PACKED_ARGS) { PACKED_TILES(WALK, strata_limit_tile(F, T)) }
 template <bool WALK = false>
@@ -2159,7 +2176,7 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
   }
   tl(kp_laplacian<false, false>, kp_laplacian<false, true>, dim3(16, 8));
   tl(kp_strata_split<MODE, false>, kp_strata_split<MODE, true>, b);
-  tl(kp_strata_fast<MODE, false>, kp_strata_fast<MODE, true>, b);  // with the CFL reduction
+  tl(kp_strata_fast<MODE, false>, kp_strata_fast<MODE, true>, dim3(16, 8));  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_fill_list<MODE><<<nf, 1024, 0, st>>>(V.films_next, nf);
@@ -2260,7 +2277,7 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   else if (n == "strata_pass") {
     kp_stats_reset<<<fb, 128, 0, st>>>(A, nf);
     kp_face_flags<<<nt, b, 0, st>>>(A, T, nt);
-    CFK_LAUNCH(kp_strata_fast, nt, b, st, A, T, nt);
+    CFK_LAUNCH(kp_strata_fast, nt, dim3(16, 8), st, A, T, nt);
     CFK_LAUNCH(kp_strata_full, V.persist_blocks, 256, st, A, nf);
     CFK_LAUNCH(kp_strata_commit, V.persist_blocks, 256, st, A, nf);
     return 2;
