@@ -94,7 +94,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, RELIEF_WORKLOAD, SNAPSHOT_WORKLOAD]
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, SERVE_WORKLOAD, RELIEF_WORKLOAD, SNAPSHOT_WORKLOAD,
+                                                 LIT_WORKLOAD]
                     + sorted(DEPOSIT_WORKLOADS))
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="arrival window of the served workload")
     ap.add_argument("--serve-wall", type=float, default=60.0, help="wall-clock cut-off of the served run")
@@ -343,6 +344,10 @@ RELIEF_WORKLOAD = "relief2048_view3840x2160_fp32"
 
 
 SNAPSHOT_WORKLOAD = "snapshot2048_fp32"
+# the renderer's fragment shader over the film (cf_render_lit): a 1920 x 1080
+# perspective view of the default drip canvas, the camera orbiting a little
+# every frame
+LIT_WORKLOAD = "lit2048_persp1920x1080_fp32"
 
 
 def snapshot_arm(args):
@@ -505,6 +510,79 @@ def relief_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def lit_film():
+    """The default drip canvas after 5 adaptive steps, and the top of its relief."""
+    from canvaz_film.film import Film
+    cv = synth.config(1, 0)
+    st = settings_for(cv)
+    film = Film(st, cv.w, cv.h, capi.CF_PREC_FP32)
+    film.set_tables(cv.pigtab, cv.cmf)
+    film.write_state(cv.planes)
+    for _ in range(5):
+        film.step_adaptive(1.0 / 60.0)
+    state = film.read_state()
+    top = float(np.max(np.asarray(state["h"], np.float64) + np.asarray(state["m"], np.float64))) + 0.5e-3
+    return cv, st, film, top
+
+
+def lit_arm(args):
+    """cf_render_lit of a 1920 x 1080 perspective view of the default 2048^2
+    drip canvas, the orbit camera turning 0.02 rad a frame.  `value` = output
+    Mpixel/s of device time; `e2e` adds the read-back of each RGBA8 image."""
+    import torch
+    from canvaz_film import camera
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if not capi.LIB_PATH.exists():
+        import __graft_entry__ as g
+        g.build()
+    cv, st, film, top = lit_film()
+    W, H = 1920, 1080
+    cams = [camera.render_cam(cv.w, cv.h, float(st.width_m), float(st.height_m), top, yaw=0.6 + 0.02 * k,
+                              aspect=W / H) for k in range(16)]
+    img = torch.empty(W * H * 4, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    for k in range(args.warmup):
+        film.render_lit(cams[k % 16], W, H, None, img.data_ptr(), stream=sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for k in range(args.steps):
+            film.render_lit(cams[k % 16], W, H, None, img.data_ptr(), stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    value = W * H * args.steps / t / 1e6
+    host = torch.empty(W * H * 4, dtype=torch.uint8).pin_memory()
+    t0 = time.perf_counter()
+    for k in range(max(args.e2e_steps, 1)):
+        film.render_lit(cams[k % 16], W, H, None, img.data_ptr(), stream=sh)
+        with torch.cuda.stream(stream):
+            host.copy_(img, non_blocking=True)
+        stream.synchronize()
+    te = time.perf_counter() - t0
+    peak, peak_kind = peaks()
+    alg = 4.0  # the RGBA8 pixel written; the film's planes it samples (157 MB) are re-read from L2
+    line = {"metric": "Mpixel/s", "value": value, "unit": "Mpixel/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (the default drip canvas)",
+            "config": {"workload": LIT_WORKLOAD, "view": [W, H], "film": [cv.w, cv.h],
+                       "l2": "the film's h, m, colour and detail planes (101 MB) fit in L2"},
+            "roofline": {"bound": "hbm", "achieved": alg * W * H * args.steps / t / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg * W * H * args.steps / t / 1e9 / peak,
+                         "peak_source": peak_kind, "alg_bytes_per_pixel": alg, "scope": "k_render_lit",
+                         "note": "bound by instruction issue (the march, micro-relief, shadow, occlusion and "
+                                 "lobes per pixel), not by memory", "traffic": None},
+            "gpu_launches": args.steps, "clocks": clk.summary(),
+            "e2e": {"value": W * H * max(args.e2e_steps, 1) / te / 1e6, "unit": "Mpixel/s", "h2d_bytes_per_step": 304,
+                    "d2h_bytes_per_step": W * H * 4, "steps": max(args.e2e_steps, 1),
+                    "path": "cf_render_lit + read back of the RGBA8 image"},
+            "cpu_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
 DEPOSIT_SETS = 4
 DEPOSIT_CPU_SIDE = 1024  # CPU sample: the same stroke density on a 1024^2 film
 
@@ -629,6 +707,11 @@ def reference_arm(args):
                           "config": {"workload": args.workload}, "cpu_baseline": cb,
                           "e2e": {"value": cb["value"], "unit": "Mpixel/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    if args.workload == LIT_WORKLOAD:  # the reference's fragment exists on the host only as its translation
+        print(json.dumps({"impl": "reference", "unavailable": "the renderer's fragment shader runs only through wgpu "
+                          "(no graphics stack on this box); its CPU translation is test infrastructure built from "
+                          "the reference sources where they exist"}), flush=True)
         return
     if args.workload in DEPOSIT_WORKLOADS:
         cb = deposit_cpu(args.workload, min(150.0, 10.0 * (args.steps + args.warmup)))
@@ -1117,6 +1200,8 @@ def main():
         deposit_arm(args)
     elif args.workload == RELIEF_WORKLOAD:
         relief_arm(args)
+    elif args.workload == LIT_WORKLOAD:
+        lit_arm(args)
     elif args.workload == SNAPSHOT_WORKLOAD:
         snapshot_arm(args)
     else:

@@ -352,6 +352,44 @@ typedef struct cf_relief_view {
 } cf_relief_view;
 cf_status cf_render_relief(cf_film* film, const cf_relief_view* view, uint8_t* rgba8, void* stream);
 
+/* The renderer's camera uniform (shaders/render.wgsl:1-15, CamUniform of
+ * src/render/mod.rs:10-24), filled as Renderer::uniform (:162-180) fills
+ * it: inv_vp and vp column-major; canvas = (width_m, height_m, dx,
+ * max(h_max, s_max) + 0.5 mm); light = (direction, intensity); size =
+ * (film w, h, 0, 0); jitter = (ndc offset x, y, beauty mode > 0.5, pixel
+ * footprint in metres); ortho = (orthographic top-down > 0.5, tan of the
+ * contact angle, colour-plane scale (0: the film's resolution), 0); basis_r,
+ * basis_u: the camera's right and up; lens = (aperture offsets x, y, focus
+ * distance, thin lens > 0.5). */
+typedef struct cf_render_cam {
+    float inv_vp[16];
+    float eye[4];
+    float canvas[4];
+    float light[4];
+    uint32_t size[4];
+    float sky[4];
+    float ground[4];
+    float vp[16];
+    float jitter[4];
+    float ortho[4];
+    float basis_r[4];
+    float basis_u[4];
+    float lens[4];
+} cf_render_cam;
+
+/* The renderer's fragment shader over the film (render.wgsl fs :985-1116, lit
+ * :1118-1143): for each pixel of a width x height target (row 0 at the top,
+ * the pixel centre's ndc as the full-screen triangle interpolates it), the
+ * camera ray marched over the relief h + m, the tool micro-relief of the
+ * film's detail texels, the sharpened (or beauty-mode) colour, the canvas
+ * weave, key-light shadow, ambient occlusion, environment, softboxes and GGX
+ * lobes, tonemapped to sRGB (beauty mode: linear, firefly-clamped).  Writes
+ * RGBA as 4 floats a pixel to `rgba_f32` (16-byte aligned) and/or as RGBA8
+ * to `rgba8` (4-byte aligned), device memory, either may be NULL but not
+ * both.  cam->size must be the film's size.  Enqueued on `stream`. */
+cf_status cf_render_lit(cf_film* film, const cf_render_cam* cam, uint32_t width, uint32_t height, float* rgba_f32,
+                        uint8_t* rgba8, void* stream);
+
 /* --- painting files (src/session.rs) ----------------------------------------- */
 
 /* The header fields of a Canvaz painting file (src/session.rs:248-310). */

@@ -311,6 +311,7 @@ struct Film {
   std::vector<uint32_t> delta, tile_flags, tile_moved;
   std::vector<R> stats;  // 2 x tiles64
   std::vector<R> color;  // 4N
+  std::vector<R> detail;  // 4N: the renderer's detail texel (shade.wgsl:61-64)
 
   Film(uint32_t w, uint32_t hh, const cf_settings& s, int pig_storage)
       : W(w), H(hh), TW((w + 15) / 16), TH((hh + 15) / 16), N((size_t)w * hh), pig_mode(pig_storage), S(s) {
@@ -322,6 +323,7 @@ struct Film {
     delta.assign(N, 0); tile_flags.assign((size_t)TW * TH, 0); tile_moved.assign((size_t)TW * TH, 0);
     stats.assign(2 * (size_t)((w + 63) / 64) * ((hh + 63) / 64), 0);
     color.assign(4 * N, 0);
+    detail.assign(4 * N, 0);
     pigtab.assign(NPIG * PIG_STRIDE, 0);
     cmf.assign(NB * 3, 0);
     // Film::new :686-693: substrate refl, weave relief, rheo = (1, 0)
@@ -1321,7 +1323,7 @@ struct Film {
     stack_store_to(c, s, sh, scu, pig);
   }
 
-  // shade.wgsl:28-84 (colour only; the detail texture is render-only)
+  // shade.wgsl:28-84: the colour and the renderer's detail texel
   void k_shade_cell(size_t c) {
     R r[NB];
     for (int b = 0; b < NB; ++b) r[b] = refl[16 * c + b];
@@ -1371,6 +1373,13 @@ struct Film {
       else { R v = F(0.3f) + F(0.15f) * (R)cnt; rgb[0] = v; rgb[1] = v; rgb[2] = v; }
     }
     color[4 * c] = rgb[0]; color[4 * c + 1] = rgb[1]; color[4 * c + 2] = rgb[2]; color[4 * c + 3] = rough;
+    // shade.wgsl:61-64: lay method + stroke turn, cure_top, yield stress, thickness above the weave
+    const uint32_t lv = lay[c];
+    const R turn = (R)(lv >> 8u & 0xffffu) / F(65536.0f);
+    detail[4 * c] = (R)(lv & 0xffu) + turn;
+    detail[4 * c + 1] = cure_top;
+    detail[4 * c + 2] = rheo[3 * c + 1];
+    detail[4 * c + 3] = hv + std::max(m[c] - F(60e-6f), R(0));
   }
 
   // ---- tile activity (film.wgsl:1365-1425) ----

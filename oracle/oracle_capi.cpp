@@ -51,6 +51,7 @@ Buf<R> find(cfo::Film<R>& F, const char* name) {
   else if (n == "tile_moved") b.u = &F.tile_moved;
   else if (n == "stats") b.r = &F.stats;
   else if (n == "color") b.r = &F.color;
+  else if (n == "detail") b.r = &F.detail;
   return b;
 }
 

@@ -25,7 +25,7 @@ PLANES = {
     "h": 1, "m": 1, "rheo": 3, "strata_h": 4, "strata_cure": 4, "strata_pig": 64, "sub_refl": 16,
     "lay": 1, "pres": 2, "flux": 4, "acc": 4, "alpha": 1, "tmp": 1, "acc_s": 16, "alpha_s": 4,
     "strata_h2": 4, "strata_cure2": 4, "strata_pig2": 64, "h_frame": 1, "fnorm": 2, "delta": 1,
-    "color": 4,
+    "color": 4, "detail": 4,
 }
 STATE = ["h", "m", "rheo", "strata_h", "strata_pig", "strata_cure", "sub_refl", "lay"]
 KERNELS = ["mark_tiles", "compact_tiles", "cure_step", "clear_acc", "laplacian", "plug", "fluxes",

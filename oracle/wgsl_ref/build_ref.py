@@ -54,6 +54,12 @@ def build(ref=None):
     (OUT / "render_ref.inc").write_text(src)
     subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", str(OUT), str(HERE / "render_driver.cpp"),
                     "-o", str(OUT / "librenderref.so")], check=True)
+    # the renderer's whole fragment shader (fs, lit and all they reach), in
+    # f32 as the shader computes (one rounding per operation: no contraction)
+    src = translate.translate_subset(str(ref), "render.wgsl", ["fs"], set(), "wgrf", "float")
+    (OUT / "render_fs_ref.inc").write_text(src)
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", str(OUT),
+                    str(HERE / "render_fs_driver.cpp"), "-o", str(OUT / "librenderfsref.so")], check=True)
     # the display fragment of resolve.wgsl, in f32 as the shader computes
     # (one rounding per operation: no contraction), its uniform's fields a, b,
     # c kept as they are named

@@ -16,7 +16,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT = CSRC / "_build"
 LIB = OUT / "libcanvaz_film.so"
-SOURCES = ["capi.cu", "capi_batch.cu", "film_kernels.cu", "film_noalloc.cu", "resolve.cu", "snapshot.cu", "deposit.cu", "cg.cu", "relief.cu"]
+SOURCES = ["capi.cu", "capi_batch.cu", "film_kernels.cu", "film_noalloc.cu", "resolve.cu", "snapshot.cu", "deposit.cu", "cg.cu",
+           "relief.cu", "render.cu"]
 HEADERS = ["film_device.cuh", "strata_device.cuh", "strata_lane.cuh", "film_kernels.h", "film_handle.h", "tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -25,7 +26,10 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
 # lattice point is inside a ribbon (cut planes, x < 1): it keeps one rounding
 # per operation, as the reference's f32 host code and the oracle do, so no
 # fused multiply-add moves a sample across those edges.
-FILE_FLAGS = {"deposit.cu": ["--fmad=false"]}
+# The renderer's fragment (render.cu) follows the shader's f32 arithmetic the
+# same way, so that its image is the shader's up to the last bits of the
+# transcendental functions.
+FILE_FLAGS = {"deposit.cu": ["--fmad=false"], "render.cu": ["--fmad=false"]}
 
 
 def nvcc():

@@ -123,6 +123,22 @@ class ReliefView(C.Structure):
                 ("height", C.c_uint32), ("light", C.c_float * 3), ("ambient", C.c_float), ("reserved", C.c_uint32)]
 
 
+class RenderCam(C.Structure):
+    """cf_render_cam: the renderer's camera uniform (76 words, render.wgsl:1-15)."""
+    _fields_ = [("inv_vp", C.c_float * 16), ("eye", C.c_float * 4), ("canvas", C.c_float * 4), ("light", C.c_float * 4),
+                ("size", C.c_uint32 * 4), ("sky", C.c_float * 4), ("ground", C.c_float * 4), ("vp", C.c_float * 16),
+                ("jitter", C.c_float * 4), ("ortho", C.c_float * 4), ("basis_r", C.c_float * 4),
+                ("basis_u", C.c_float * 4), ("lens", C.c_float * 4)]
+
+    @classmethod
+    def from_words(cls, words):
+        """From the uniform's 76 32-bit words (float32 array; size as u32 bit patterns)."""
+        import numpy as np
+        w = np.ascontiguousarray(np.asarray(words, np.float32))
+        assert w.size == 76
+        return cls.from_buffer_copy(w.tobytes())
+
+
 class BatchTuning(C.Structure):
     """cf_batch_tuning."""
     _fields_ = [("list_blocks_per_sm", C.c_uint32), ("use_graph", C.c_uint32), ("frames_per_graph", C.c_uint32),
@@ -203,6 +219,7 @@ def load_library(path=None):
         "cf_sample_relief": ([vp, vp, u32, vp, vp], i32),
         "cf_relief_shadow": ([vp, vp, u32, C.POINTER(f32), f32, vp, vp], i32),
         "cf_render_relief": ([vp, C.POINTER(ReliefView), vp, vp], i32),
+        "cf_render_lit": ([vp, C.POINTER(RenderCam), C.c_uint32, C.c_uint32, vp, vp, vp], i32),
         "cf_batch_create": ([C.POINTER(vp)], i32),
         "cf_batch_destroy": ([vp], i32),
         "cf_batch_add": ([vp, vp], i32),

@@ -19,7 +19,7 @@ DEBUG_PER_CELL = {
     "h": 1, "m": 1, "mu": 1, "tau": 1, "nn": 1, "delta": 1, "lay": 1, "pres": 2, "fnorm": 2, "flux": 4, "acc": 4,
     "acc_s": 16, "alpha_s": 4, "alpha": 1, "tmp": 1, "h_frame": 1, "strata_h": 4, "strata_cure": 4,
     "strata_h2": 4, "strata_cure2": 4, "strata_pig": 64, "strata_pig2": 64, "sub_refl": 16, "color": 4,
-    "fill_src": 1, "fflags": 1, "h_next": 1, "delta_old": 1,
+    "fill_src": 1, "fflags": 1, "h_next": 1, "delta_old": 1, "detail": 4,
 }
 _ELEM_DTYPE = {0: np.float32, 1: np.uint32, 2: np.float16, 3: "bf16", 4: np.int32}
 
@@ -230,6 +230,15 @@ class Film:
         for k in range(3):
             v.light[k] = light[k]
         self._check(self.L.cf_render_relief(self.p, C.byref(v), out_ptr, stream), "cf_render_relief")
+
+    def render_lit(self, cam, width, height, out_f32_ptr=None, out_rgba8_ptr=None, stream=None):
+        """cf_render_lit: the renderer's fragment shader over the film for a
+        width x height target, into device buffers (RGBA floats and/or RGBA8).
+        `cam` is a capi.RenderCam or the uniform's 76 words."""
+        if not isinstance(cam, capi.RenderCam):
+            cam = capi.RenderCam.from_words(cam)
+        self._check(self.L.cf_render_lit(self.p, C.byref(cam), width, height, out_f32_ptr, out_rgba8_ptr, stream),
+                    "cf_render_lit")
 
     def lay_deposits(self, stream=None):
         """cf_lay_deposits: lays the uploaded deposits now (asynchronous)."""

@@ -245,7 +245,7 @@ static void carve_planes(cfk::Film& F, size_t n, size_t nt, int precision, bool 
   add((void**)&F.h_frame, 4 * n); add((void**)&F.h_next, 4 * n); add((void**)&F.sh, 16 * n); add((void**)&F.scu, 16 * n);
   add((void**)&F.sh2, 16 * n); add((void**)&F.scu2, 16 * n); add((void**)&F.pig, 64 * pig_b * n);
   add((void**)&F.pig2, 64 * pig_b * n); add((void**)&F.agg, 16 * n); add((void**)&F.refl, 32 * n);
-  add((void**)&F.color, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
+  add((void**)&F.color, 8 * n); add((void**)&F.detail, 8 * n); add((void**)&F.tile_flags, 4 * nt); add((void**)&F.tile_moved, 4 * nt);
   add((void**)&F.fill_src, 4 * n); add((void**)&F.fflags, 4 * n); add((void**)&F.shade_state, n);
   add((void**)&F.spec, 64 * n);
   add((void**)&F.full_list, 4 * n); add((void**)&F.fill_list, 4 * n);
@@ -915,7 +915,7 @@ bool find_plane(cf_film* f, const std::string& n, PlaneRef& r) {
       {"strata_cure", F.scu, 16 * N, CF_ELEM_F32}, {"strata_h2", F.sh2, 16 * N, CF_ELEM_F32},
       {"strata_cure2", F.scu2, 16 * N, CF_ELEM_F32}, {"strata_pig", F.pig, 64 * pb * N, pe},
       {"strata_pig2", F.pig2, 64 * pb * N, pe}, {"sub_refl", F.refl, 32 * N, CF_ELEM_F16},
-      {"color", F.color, 8 * N, CF_ELEM_F16}, {"tile_flags", F.tile_flags, 4 * nt, CF_ELEM_U32},
+      {"color", F.color, 8 * N, CF_ELEM_F16}, {"detail", F.detail, 8 * N, CF_ELEM_F16}, {"tile_flags", F.tile_flags, 4 * nt, CF_ELEM_U32},
       {"tile_moved", F.tile_moved, 4 * nt, CF_ELEM_U32}, {"fill_src", F.fill_src, 4 * N, CF_ELEM_I32},
       {"fflags", F.fflags, 4 * N, CF_ELEM_U32},
       {"agg", F.agg, 16 * N, CF_ELEM_F32},

@@ -125,6 +125,7 @@ struct Film {
   float4* agg;     // composition aggregates for the next cure (see composition_parts)
   uint16_t* refl;  // 16 half per cell
   ushort4* color;  // rgba16f
+  ushort4* detail; // rgba16f: the renderer's detail texel (shade.wgsl:61-64)
   uint32_t* tile_flags;
   uint32_t* tile_moved;
   int32_t* fill_src;

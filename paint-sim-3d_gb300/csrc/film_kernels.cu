@@ -1353,6 +1353,7 @@ __device__ __forceinline__ int strata_fast_cell(const Film& F, const cf_params& 
 // The colour of a FAST_COLOR cell: its cached composite spectrum through the
 // surface correction with this frame's cure (bit for bit what CellAcc gives
 // for the same strata; the aggregates do not depend on the cure and stay).
+template <int MODE>
 __device__ __forceinline__ void fast_color_cached(const Film& F, uint32_t c, const FastShade& sh, int tid) {
   const float4 nt = sh.nt[tid], cu = sh.cu[tid];
   float wet = 0.f, cure_top = 0.f;
@@ -1370,7 +1371,9 @@ __device__ __forceinline__ void fast_color_cached(const Film& F, uint32_t c, con
   }
   float rgb[3];
   surface_rgb(sh.cm, r, wet, rgb);
-  F.color[c] = pack_color(rgb, surface_rough(cure_top, sh.h[tid], F.m[c]));
+  const float mv = F.m[c];
+  F.color[c] = pack_color(rgb, surface_rough(cure_top, sh.h[tid], mv));
+  F.detail[c] = detail_texel<MODE>(F, c, cure_top, sh.h[tid], mv);
 }
 // The shade and aggregates of one cell the fast path left to shade, by its
 // own lane (CellAcc).
@@ -1401,7 +1404,9 @@ __device__ __forceinline__ void fast_shade_lane(const Film& F, const cf_params& 
     for (int q = 0; q < 4; ++q)
       F.spec[(size_t)q * F.n + c] = make_float4(acc.r[4 * q], acc.r[4 * q + 1], acc.r[4 * q + 2], acc.r[4 * q + 3]);
   }
-  F.color[c] = acc.color(P, sh.cm, hc, F.m[c]);
+  const float mv = F.m[c];
+  F.color[c] = acc.color(P, sh.cm, hc, mv);
+  F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
 }
 // The shade (shade.wgsl:28-84) and composition aggregates (cure.wgsl:3-48)
 // of the tile's cells that the fast path listed: one cell per half-warp, the
@@ -1428,11 +1433,13 @@ __device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params&
       acc.add(H, k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, dbg);
     }
     const float4 agg = acc.agg(P);
-    const ushort4 col = acc.color(H, P, sh.cm, hc, F.m[c]);
+    const float mv = F.m[c];
+    const ushort4 col = acc.color(H, P, sh.cm, hc, mv);
     if (hc > 0.f) reinterpret_cast<float*>(F.spec)[((size_t)(H.q >> 2) * F.n + c) * 4 + (H.q & 3)] = acc.r;
     if (H.q == 0) {
       if (hc > 0.f) F.agg[c] = agg;  // the next cure reads the aggregates of wet cells only
       F.color[c] = col;
+      F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
     }
   }
 }
@@ -1479,7 +1486,7 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
 #pragma unroll 1
   for (int r = 0; r < 2; ++r) {
     const int t = tid + 128 * r;
-    if (need[r] == FAST_COLOR) fast_color_cached(F, c[r], sh, t);
+    if (need[r] == FAST_COLOR) fast_color_cached<MODE>(F, c[r], sh, t);
     const bool shade = need[r] == FAST_SHADE;
     // Where at least FAST_SHADE_LANES lanes of the warp have a cell to
     // shade, each shades its own; where fewer do, the cells are shaded after
@@ -1646,10 +1653,12 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
       acc.add(H, k, get4(s.th, k), get4(s.cu, k), PigLane<MODE>::round(pk, H.q), hc, ltab, tab, dbg);
     }
     const float4 agg = acc.agg(P);
-    const ushort4 col = acc.color(H, P, cm, hc, F.m[c]);
+    const float mv = F.m[c];
+    const ushort4 col = acc.color(H, P, cm, hc, mv);
     if (H.q == 0) {
       F.agg[c] = agg;
       F.color[c] = col;
+      F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
       F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
     }
   }
@@ -1716,6 +1725,7 @@ __device__ __forceinline__ void fill_list_film(const Film& F, float* lt) {
       finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
       F.agg[c] = agg;
       F.color[c] = col;
+      F.detail[c] = detail_texel<MODE>(F, c, top_cure(s.th, s.cu), hc, F.m[c]);
       F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
     }
     __syncthreads();
@@ -1763,6 +1773,7 @@ __device__ __forceinline__ void fill_apply_tile(const Film& F, TileId T) {
   finish_stack(P, lt, F.pigtab, F.cmf, F.refl + (size_t)c * 16, hc, F.m[c], s, agg, col);
   F.agg[c] = agg;
   F.color[c] = col;
+  F.detail[c] = detail_texel<MODE>(F, c, top_cure(s.th, s.cu), hc, F.m[c]);
   F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
 }
 
@@ -1784,6 +1795,7 @@ __device__ __forceinline__ void compose_tile(const Film& F, TileId T, int shade)
   F.agg[c] = agg;
   if (shade) {
     F.color[c] = col;
+    F.detail[c] = detail_texel<MODE>(F, c, top_cure(s.th, s.cu), F.hh[c], F.m[c]);
     F.shade_state[c] = F.hh[c] <= 0.f ? SHADE_DRY : SHADE_NONE;
   }
 }

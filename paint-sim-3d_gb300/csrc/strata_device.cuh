@@ -206,6 +206,31 @@ __device__ __forceinline__ float surface_rough(float cure_top, float hv, float m
   if (hv <= 0.f) rough = 0.85f * (1.0f - painted) + 0.35f * painted;
   return rough;
 }
+// shade.wgsl:61-64: the detail texel the renderer reads for a cell whose top
+// wet stratum has cure fraction cure_top (0 for a dry cell): the lay method
+// plus the stroke's turn, cure_top as the surface roughness sees it, the
+// yield stress and the paint's thickness above the weave
+template <int MODE>
+__device__ __forceinline__ ushort4 detail_texel(const Film& F, uint32_t c, float cure_top, float hv, float mv) {
+  auto smooth = [](float e0, float e1, float x) {
+    float t = fminf(fmaxf((x - e0) / (e1 - e0), 0.f), 1.f);
+    return t * t * (3.0f - 2.0f * t);
+  };
+  const float painted = smooth(60e-6f, 150e-6f, mv);
+  const float ct = fmaxf(hv > 0.f ? cure_top : 0.f, painted * (1.0f - smooth(0.f, 50e-6f, hv)));
+  const uint32_t lv = F.lay[c];
+  const float turn = (float)((lv >> 8u) & 0xffffu) / 65536.0f;
+  return make_ushort4((unsigned short)f_to_h16((float)(lv & 0xffu) + turn), (unsigned short)f_to_h16(ct),
+                      (unsigned short)f_to_h16(rtau<MODE>(F, c)), (unsigned short)f_to_h16(hv + fmaxf(mv - 60e-6f, 0.f)));
+}
+// the cure fraction of the top stratum with paint (0 when none)
+__device__ __forceinline__ float top_cure(const float th[4], const float cu[4]) {
+  float ct = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (th[k] > 0.f) ct = cu[k];
+  return ct;
+}
 __device__ __forceinline__ ushort4 pack_color(const float rgb[3], float rough) {
   return make_ushort4((unsigned short)f_to_h16(rgb[0]), (unsigned short)f_to_h16(rgb[1]),
                       (unsigned short)f_to_h16(rgb[2]), (unsigned short)f_to_h16(rough));

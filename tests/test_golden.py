@@ -13,9 +13,9 @@ import pytest
 import deposit_ref as dr
 import pyoracle as po
 
-# the frame fixtures (relief_samples.npz and resolve_samples.npz hold render and
+# the frame fixtures (relief_samples.npz, resolve_samples.npz and render_lit.npz hold render and
 # display samples: tests/test_relief.py, tests/test_resolve_fixture.py)
-GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz") if p.stem not in ("relief_samples", "resolve_samples"))
+GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz") if p.stem not in ("relief_samples", "resolve_samples", "render_lit"))
 FIELDS = ["h", "m", "strata_h", "strata_pig", "strata_cure", "sub_refl", "delta", "fnorm", "color", "acc",
           "tile_flags", "pres", "flux", "alpha", "tmp", "acc_s", "alpha_s"]
 

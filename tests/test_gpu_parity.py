@@ -6,7 +6,7 @@ multi-strata stacks and sleeping tiles; that whole internal state is copied
 into the CUDA film, one dispatch runs on both sides from identical f32
 inputs, and every plane it writes is compared value by value: integer planes
 (front offsets, tile bits) exactly, float planes to 1e-5 relative with a
-floor of 1e-6 of the plane's largest value, the colour to one f16 step.  A
+floor of 1e-6 of the plane's largest value, the colour and the renderer's detail texel to one f16 step.  A
 value outside that is counted as a branch flip (a discrete stack decision -
 merge, push - that the last bit of a sum decides differently); the flipped
 cells are reported, and only the strata pass, whose half-warp sums are
@@ -30,9 +30,9 @@ from canvaz_film.deposit import DEPOSIT_DTYPE
 
 pytestmark = pytest.mark.gpu
 
-# the frame fixtures (relief_samples.npz and resolve_samples.npz hold render and
+# the frame fixtures (relief_samples.npz, resolve_samples.npz and render_lit.npz hold render and
 # display samples: tests/test_relief.py, tests/test_resolve_fixture.py)
-GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz") if p.stem not in ("relief_samples", "resolve_samples"))
+GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz") if p.stem not in ("relief_samples", "resolve_samples", "render_lit"))
 
 # oracle plane -> (CUDA plane(s), per-cell count)
 TRANSFER = ["h", "m", "strata_h", "strata_cure", "strata_pig", "sub_refl", "lay", "pres", "flux", "acc", "alpha",
@@ -50,9 +50,9 @@ WRITES = {
     "nose": ["delta", "fnorm"],
     "strata_split": ["acc_s"],
     "strata_limit": ["alpha_s"],
-    "strata_pass": ["strata_h", "strata_cure", "strata_pig", "color"],
+    "strata_pass": ["strata_h", "strata_cure", "strata_pig", "color", "detail"],
     "strata_fill": ["strata_h", "strata_cure", "strata_pig"],
-    "shade_full": ["color"],
+    "shade_full": ["color", "detail"],
 }
 # The CUDA strata pass fuses these reference dispatches (strata.wgsl:157-286,
 # shade.wgsl:28-84) into one kernel writing the other strata generation.
@@ -131,7 +131,7 @@ def cuda_plane(f, name):
 
 # values per cell of each compared plane (oracle layout)
 PER_CELL = {"pres": 2, "flux": 4, "acc": 4, "acc_s": 16, "alpha_s": 4, "strata_h": 4, "strata_cure": 4,
-            "strata_pig": 64, "sub_refl": 16, "rheo": 3, "fnorm": 2, "color": 4}
+            "strata_pig": 64, "sub_refl": 16, "rheo": 3, "fnorm": 2, "color": 4, "detail": 4}
 # dispatches whose half-warp tree sums may flip a discrete stack decision in a
 # few cells, and how many flipped cells a case may have
 FLIP_BUDGET = {"strata_pass": 8}
@@ -140,15 +140,16 @@ RTOL, ATOL = 1e-5, 1e-6
 
 def flipped_cells(name, got, want):
     """Cells where the CUDA plane differs from the FP32 mirror beyond rounding:
-    integer planes at any bit, the colour by more than one f16 step (the
-    mirror's colour rounded to f16 as the plane stores it), other floats by
+    integer planes at any bit, the colour and the detail texel by more than
+    one f16 step (the mirror's values rounded to f16 as the planes store
+    them), other floats by
     more than RTOL relative with a floor of ATOL x the plane's largest value."""
     got = np.asarray(got, np.float64).ravel()
     want = np.asarray(want, np.float64).ravel()
     assert got.shape == want.shape, (name, got.shape, want.shape)
     if name in ("delta", "tile_flags", "tile_moved", "lay"):
         bad = got.astype(np.uint64) != want.astype(np.uint64)
-    elif name == "color":
+    elif name in ("color", "detail"):
         w16 = want.astype(np.float16)
         step = np.spacing(np.abs(w16)).astype(np.float64)
         bad = np.abs(got - w16.astype(np.float64)) > step
