@@ -56,6 +56,8 @@ WORKLOADS = {
     "blobs4096_dt1e-3_fp32": (lambda seed: synth.config(2, seed), capi.CF_PREC_FP32, 1e-3, False),
     # the same field at a quarter of the side (31 blobs): small case for kernel captures
     "blobs1024_dt1e-3_fp32": (lambda seed: synth.config(2, seed, scale=4), capi.CF_PREC_FP32, 1e-3, False),
+    # at half the side: DRAM-traffic captures whose writes do not stay in L2
+    "blobs2048_dt1e-3_fp32": (lambda seed: synth.config(2, seed, scale=2), capi.CF_PREC_FP32, 1e-3, False),
     # thick pours with the implicit hydrostatic CG steps (the reference's default), adaptive
     "pour2048_implicit_fp32": (lambda seed: synth.config(5, seed), capi.CF_PREC_FP32, 1.0 / 60.0, True),
     "pour512_implicit_fp32": (lambda seed: synth.config(5, seed, scale=4), capi.CF_PREC_FP32, 1.0 / 60.0, True),
@@ -472,11 +474,13 @@ def relief_arm(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
+        clk.mark(True)
         e0.record(stream)
         for k in range(args.steps):
             film.render_relief(img.data_ptr(), *view(k), pm, W, H, stream=sh)
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.mark(False)
     t = e0.elapsed_time(e1) / 1e3
     value = W * H * args.steps / t / 1e6
     host = torch.empty(W * H * 4, dtype=torch.uint8).pin_memory()
@@ -548,11 +552,13 @@ def lit_arm(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
+        clk.mark(True)
         e0.record(stream)
         for k in range(args.steps):
             film.render_lit(cams[k % 16], W, H, None, img.data_ptr(), stream=sh)
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.mark(False)
     t = e0.elapsed_time(e1) / 1e3
     value = W * H * args.steps / t / 1e6
     host = torch.empty(W * H * 4, dtype=torch.uint8).pin_memory()

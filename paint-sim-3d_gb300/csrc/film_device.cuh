@@ -160,8 +160,9 @@ struct Film {
 // spectrum in Film::spec, valid for the cell's current thicknesses and
 // pigments: the strata pass reuses it while the thicknesses it computes are
 // bit for bit the current ones, and redoes only the surface correction.
-// Every other writer of a cell's strata, pigments or substrate resets the
-// state to SHADE_NONE.  SHADE_DRY: the colour holds the dry cell's colour,
+// The strata pass's shades (fast path and full path) set it with the spectrum
+// they computed; every other writer of a cell's strata, pigments or substrate
+// resets the state to SHADE_NONE.  SHADE_DRY: the colour holds the dry cell's colour,
 // which depends only on the substrate, the relief and the CMF table.
 // SHADE_DRY2: the same, and the strata pass has written zero thicknesses and
 // cure fractions for the cell into both strata generations (it was dry in an

@@ -555,21 +555,24 @@ struct TileFaces {
   uint8_t cell[4][256];
   uint32_t count[4];
 };
-// Lists face k of this thread's cell when `live` (every thread of the block
-// calls this, with the same k).
-__device__ __forceinline__ void tile_faces_add(TileFaces& S, int k, bool live) {
-  const int tid = threadIdx.y * 16 + threadIdx.x, lane = tid & 31;
+// Lists face k of the cell in slot `slot` of the tile (y * 16 + x) when
+// `live` (every thread of the block calls this, with the same k).
+__device__ __forceinline__ void tile_faces_add(TileFaces& S, int k, bool live, int slot) {
+  const int lane = (int)(threadIdx.y * 16 + threadIdx.x) & 31;
   const unsigned m = __ballot_sync(0xffffffffu, live);
   uint32_t base = 0;
   if (lane == 0 && m) base = atomicAdd(&S.count[k], (uint32_t)__popc(m));
   base = __shfl_sync(0xffffffffu, base, 0);
-  if (live) S.cell[k][base + __popc(m & ((1u << lane) - 1u))] = (uint8_t)tid;
+  if (live) S.cell[k][base + __popc(m & ((1u << lane) - 1u))] = (uint8_t)slot;
 }
-// Runs fn(k, i, j, c) for every listed face, the block's threads in turn.
-template <class Fn>
+__device__ __forceinline__ void tile_faces_add(TileFaces& S, int k, bool live) {
+  tile_faces_add(S, k, live, (int)(threadIdx.y * 16 + threadIdx.x));
+}
+// Runs fn(k, i, j, c) for every listed face, the block's NT threads in turn.
+template <int NT = 256, class Fn>
 __device__ __forceinline__ void tile_faces_each(const Film& F, TileId T, const TileFaces& S, Fn fn) {
   const uint32_t n0 = S.count[0], n1 = n0 + S.count[1], n2 = n1 + S.count[2], n3 = n2 + S.count[3];
-  for (uint32_t e = threadIdx.y * 16 + threadIdx.x; e < n3; e += 256) {
+  for (uint32_t e = threadIdx.y * 16 + threadIdx.x; e < n3; e += NT) {
     const int k = e < n0 ? 0 : e < n1 ? 1 : e < n2 ? 2 : 3;
     const uint32_t base = k == 0 ? 0u : k == 1 ? n0 : k == 2 ? n1 : n2;
     const uint32_t t = S.cell[k][e - base];
@@ -1081,6 +1084,26 @@ __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
   const float gb = P.phys[0] * D.gxy;
   if (!stage_box<MODE, true>(F, S, i0, j0, tid, gb >= 1e-6f)) return;
   auto box = [&](int x, int y) { return (y - j0 + 4) * FB + (x - i0 + 4); };
+  {
+    // a tile whose cells and 1-cell ring are all dry has no face with flux
+    // (every face needs a wet cell) and no plug mobility (only wet cells have
+    // one): its cells take zero flux and mobility, and clear_acc
+    bool wet = false;
+    for (int q = tid; q < 18 * 18; q += 256) wet = wet || S.h[(q / 18 + 3) * FB + q % 18 + 3] > 0.f;
+    if (!__syncthreads_or(wet)) {
+      const int i = i0 + (int)threadIdx.x, j = j0 + (int)threadIdx.y;
+      if (i < (int)F.w && j < (int)F.h) {
+        const uint32_t c = idx(F, i, j);
+        if (CLEAR) {
+          F.acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+          F.h_frame[c] = S.h[box(i, j)];
+        }
+        F.tmp[c] = 0.f;
+        F.flux[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      return;
+    }
+  }
   tile_surface(F, P, S, i0, j0, tid);
   // plug: the HB flux and mass of every window cell (film.wgsl:58-87); on a
   // flat canvas (gb < 1e-6) every plug mobility is 0 and none is needed
@@ -1655,11 +1678,14 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     const float4 agg = acc.agg(P);
     const float mv = F.m[c];
     const ushort4 col = acc.color(H, P, cm, hc, mv);
+    // the composite spectrum of the new stack (its thicknesses and stored
+    // slots) is cached for the next frames' fast path, as its own shades are
+    if (hc > 0.f) reinterpret_cast<float*>(F.spec)[((size_t)(H.q >> 2) * F.n + c) * 4 + (H.q & 3)] = acc.r;
     if (H.q == 0) {
       F.agg[c] = agg;
       F.color[c] = col;
       F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
-      F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_NONE;
+      F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_WET;
     }
   }
 }
