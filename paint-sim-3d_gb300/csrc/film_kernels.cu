@@ -1211,23 +1211,36 @@ __device__ __forceinline__ void flow_tile(const Film& F, TileId T) {
 // zeroing.
 template <int MODE>
 __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
+  // 128 threads per tile, 2 cells each (slots t and t + 128: rows y and y + 8)
   __shared__ TileFaces S;
   __shared__ uint32_t flags[256];
   if ((F.tile_flags[T.x + T.y * F.tw] & ACTIVE) == 0u) return;
-  const int i = (int)(T.x * 16 + threadIdx.x), j = (int)(T.y * 16 + threadIdx.y);
   const int tid = threadIdx.y * 16 + threadIdx.x;
-  const bool in = i < (int)F.w && j < (int)F.h;
+  const int i = (int)(T.x * 16 + threadIdx.x);
   if (tid < 4) S.count[tid] = 0u;
   flags[tid] = 0u;
+  flags[tid + 128] = 0u;
   __syncthreads();
-  const uint32_t c = in ? idx(F, i, j) : 0u;
-  const float4 a4 = in ? F.acc[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+  bool in[2];
+  uint32_t c[2];
+  float4 a4[2];
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    tile_faces_add(S, k, in && sel4(a4, k) != 0.f && in_grid(F, i + FACE_DI[k], j + FACE_DJ[k]));
+  for (int r = 0; r < 2; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 8 * r);
+    in[r] = i < (int)F.w && j < (int)F.h;
+    c[r] = in[r] ? idx(F, i, j) : 0u;
+    a4[r] = in[r] ? F.acc[c[r]] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int j = (int)(T.y * 16 + threadIdx.y + 8 * r);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      tile_faces_add(S, k, in[r] && sel4(a4[r], k) != 0.f && in_grid(F, i + FACE_DI[k], j + FACE_DJ[k]), tid + 128 * r);
+  }
   __syncthreads();
   const DevParams& D = *F.P;
-  tile_faces_each(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
+  tile_faces_each<128>(F, T, S, [&](int k, int fi, int fj, uint32_t fc) {
     const float a = sel4(F.acc[fc], k);
     const FaceOut ff = face_k<MODE>(F, D, PtGlobal{F}, fi, fj, k);
     const uint32_t cb = idx(F, fi + FACE_DI[k], fj + FACE_DJ[k]);
@@ -1238,7 +1251,9 @@ __device__ __forceinline__ void strata_split_tile(const Film& F, TileId T) {
       atomicOr(&flags[(fj - (int)T.y * 16) * 16 + (fi - (int)T.x * 16)], 1u << k);
   });
   __syncthreads();
-  if (in) F.fflags[c] = flags[tid];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+    if (in[r]) F.fflags[c[r]] = flags[tid + 128 * r];
 }
 
 __device__ __forceinline__ void load_tables(const Film& F, float* tab, float* cm, float* ltab, int tid, int nthreads) {
@@ -2070,7 +2085,7 @@ __global__ void __launch_bounds__(256, 6) kp_fluxes(PACKED_ARGS) { PACKED_TILES(
 template <int MODE, bool CLEAR, bool WALK = false>
 __global__ void __launch_bounds__(256, 6) kp_flow(PACKED_ARGS) { PACKED_TILES(WALK, flow_tile<MODE, CLEAR>(F, T)) }
 template <int MODE, bool WALK = false>
-__global__ void __launch_bounds__(256, 8) kp_strata_split(PACKED_ARGS) { PACKED_TILES(WALK, strata_split_tile<MODE>(F, T)) }
+__global__ void __launch_bounds__(128, 16) kp_strata_split(PACKED_ARGS) { PACKED_TILES(WALK, strata_split_tile<MODE>(F, T)) }
 template <bool WALK = false>
 __global__ void __launch_bounds__(64) kp_limiter(PACKED_ARGS) { PACKED_TILES(WALK, limiter_tile(F, T)) }
 // eight blocks of 128 per SM (64 registers for the two cells' loads in flight)
@@ -2213,7 +2228,7 @@ static uint32_t frame_packed_t(const PackedFrame& V, uint32_t substeps, int adap
     n += 3;
   }
   tl(kp_laplacian<false, false>, kp_laplacian<false, true>, dim3(16, 8));
-  tl(kp_strata_split<MODE, false>, kp_strata_split<MODE, true>, b);
+  tl(kp_strata_split<MODE, false>, kp_strata_split<MODE, true>, dim3(16, 8));
   tl(kp_strata_fast<MODE, false>, kp_strata_fast<MODE, true>, dim3(16, 8));  // with the CFL reduction
   kp_strata_full<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
   kp_strata_commit<MODE><<<V.persist_blocks, 256, 0, st>>>(A, nf);
@@ -2306,7 +2321,7 @@ int launch_one(const PackedFrame& V, int mode, const char* name, cudaStream_t st
   }
   // limiter + apply fused, as the frame runs them: the new heights in h_next
   else if (n == "limit_apply") CFK_LAUNCH(kp_limit_apply, nt, dim3(16, 8), st, A, T, nt);
-  else if (n == "strata_split") CFK_LAUNCH(kp_strata_split, nt, b, st, A, T, nt);
+  else if (n == "strata_split") CFK_LAUNCH(kp_strata_split, nt, dim3(16, 8), st, A, T, nt);
   else if (n == "reduce_tiles") launch_reduce(V, mode, st);
   else if (n == "strata_limit") {  // the face flags of the acc_s plane it is given
     kp_face_flags<<<nt, b, 0, st>>>(A, T, nt);
