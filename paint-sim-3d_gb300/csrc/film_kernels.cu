@@ -1556,24 +1556,35 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
 // only when some stratum flows in, and then it is active with its alpha
 // written by part 1 (a nonzero face flags both of its cells), or inactive,
 // where strata_limit leaves alpha at 1.
+// The gathered neighbourhood of a cell of the full path, one per half-warp:
+// the cell's 8 faces (towards the cell positive; zero where absent) and the
+// 8 neighbours' strata thicknesses, cure fractions and strata_limit alphas
+// (1 for a neighbour in an inactive tile, whose alpha is not applied).
+// Lanes 0-7 load face and thicknesses of neighbour q, lanes 8-15 its cure
+// fractions and alpha, so the 32 loads of a cell are 2 load instructions of
+// the half-warp instead of a chain of broadcast loads in the inflow loop.
+struct FullStage {
+  float4 f[8], th[8], cu[8], an[8];
+  uint32_t cn[8];
+};
+// strata_update's inflow from neighbour nb (strata.wgsl:248-262): each of
+// the neighbour's strata that sends a positive flux lays its band over this
+// cell's stack.
 template <int MODE>
 __device__ __forceinline__ void lane_inflow(const Film& F, const cf_params& P, const HalfWarp& H, LaneStack& s,
-                                            int ni, int nj, float4 f) {
+                                            const FullStage& S, int nb) {
+  const float4 f = S.f[nb];
   if (!(f.x > 0.f || f.y > 0.f || f.z > 0.f || f.w > 0.f)) return;
-  const uint32_t cn = idx(F, ni, nj);
-  const bool act = cell_active(F, ni, nj);
-  // the neighbour's stratum values are loaded one at a time in the loop
-  // (scalar loads of lines in L1) rather than held as three float4s, which
-  // keeps the loop under the kernel's register cap
-  const float* th = reinterpret_cast<const float*>(F.sh + cn);
-  const float* cu = reinterpret_cast<const float*>(F.scu + cn);
-  const float* an = reinterpret_cast<const float*>(F.alpha_s + cn);
+  const uint32_t cn = S.cn[nb];
+  const float* th = reinterpret_cast<const float*>(&S.th[nb]);
+  const float* cu = reinterpret_cast<const float*>(&S.cu[nb]);
+  const float* an = reinterpret_cast<const float*>(&S.an[nb]);
   float z0 = 0.f;
 #pragma unroll 1
   for (int k = 0; k < 4; ++k) {
     const float thn = th[k];
     const float z1 = z0 + thn;
-    const float v = sel4(f, k) * (act ? an[k] : 1.f) * P.inv_dx;
+    const float v = sel4(f, k) * an[k] * P.inv_dx;
     if (v > 0.f && thn > 0.f) {
       const float pin = PigLane<MODE>::load(F, F.pig, cn, k, H.q);
       lane_add_band(H, s, z0, z1, v, pin, cu[k], P.misc[0], P.misc[1]);
@@ -1592,7 +1603,7 @@ __device__ __forceinline__ void lane_inflow(const Film& F, const cf_params& P, c
 // shared memory.
 template <int MODE>
 __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab, const float* cm, const float* ltab,
-                                                 uint32_t count, uint32_t first, uint32_t stride) {
+                                                 FullStage& S, uint32_t count, uint32_t first, uint32_t stride) {
   const HalfWarp H((int)(threadIdx.x & 31u));
   const cf_params& P = F.P->p;
   const bool dbg = P.flags[0] == 1u;
@@ -1601,27 +1612,31 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     const uint32_t c = F.full_list[e];
     const int i = (int)(c % F.w), j = (int)(c / F.w);
     const float hc = F.hh[c];
-    const bool hl = i > 0 && cell_active(F, i - 1, j);
-    const bool hd = j > 0 && cell_active(F, i, j - 1);
-    const bool hll = i > 0 && j > 0 && cell_active(F, i - 1, j - 1);
-    const bool hlu = i > 0 && j + 1 < (int)F.h && cell_active(F, i - 1, j + 1);
-    // face nb of the 8 (towards this cell positive): the cell's own 4 faces
-    // (right, up, up-right, down-right) negated, then the 4 faces its left,
-    // lower, lower-left and upper-left neighbours own; zero where absent.
-    // The strata fast path has zeroed those of them strata_split did not
-    // write this frame.
-    auto face_in = [&](int nb) -> float4 {
-      switch (nb) {
-        case 0: return neg4(acc_face(F, c, 0));
-        case 1: return neg4(acc_face(F, c, 1));
-        case 2: return neg4(acc_face(F, c, 2));
-        case 3: return neg4(acc_face(F, c, 3));
-        case 4: return hl ? acc_face(F, c - 1, 0) : z4;
-        case 5: return hd ? acc_face(F, c - F.w, 1) : z4;
-        case 6: return hll ? acc_face(F, c - F.w - 1, 2) : z4;
-        default: return hlu ? acc_face(F, c + F.w - 1, 3) : z4;
-      }
-    };
+    // neighbour nb of lane q & 7, in the reference's order: right, up,
+    // up-right, down-right, left, down, down-left, up-left.  Faces 0-3 are
+    // the cell's own (right, up, up-right, down-right) negated, faces 4-7 the
+    // ones the active left, lower, lower-left and upper-left neighbours own;
+    // the strata fast path has zeroed those strata_split did not write.
+    const int nb = H.q & 7;
+    // (di + 1, dj + 1) of neighbour nb in bits 2 nb, 2 nb + 1
+    const int di = (int)((0x04a6u >> (2 * nb)) & 3u) - 1;
+    const int dj = (int)((0x8129u >> (2 * nb)) & 3u) - 1;
+    const int ni = i + di, nj = j + dj;
+    const bool inb = ni >= 0 && nj >= 0 && ni < (int)F.w && nj < (int)F.h;
+    const bool nact = inb && cell_active(F, ni, nj);
+    const bool ok = nb < 4 ? inb : nact;  // the reference's inflow guards
+    const uint32_t cn = inb ? idx(F, ni, nj) : c;
+    __syncwarp(H.mask);  // the previous cell's stage has been read
+    if (H.q < 8) {
+      const float4 f = nb < 4 ? neg4(acc_face(F, c, nb)) : nact ? acc_face(F, cn, nb - 4) : z4;
+      S.f[nb] = f;
+      S.th[nb] = ok ? F.sh[cn] : z4;
+      S.cn[nb] = cn;
+    } else {
+      S.cu[nb] = ok ? F.scu[cn] : z4;
+      S.an[nb] = nact ? F.alpha_s[cn] : make_float4(1.f, 1.f, 1.f, 1.f);
+    }
+    const uint32_t okm = (__ballot_sync(H.mask, ok) >> (threadIdx.x & 16u)) & 0xffu;
     LaneStack s;
     {
       const float4 t = F.sh[c], u = F.scu[c];
@@ -1630,17 +1645,18 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
 #pragma unroll
       for (int k = 0; k < 4; ++k) s.pg[k] = PigLane<MODE>::load(F, F.pig, c, k, H.q);
     }
+    const float4 a4 = F.alpha_s[c];
+    __syncwarp(H.mask);
     {
       float4 out = z4;
 #pragma unroll
-      for (int nb = 0; nb < 8; ++nb) {
-        const float4 f = face_in(nb);
+      for (int n = 0; n < 8; ++n) {
+        const float4 f = S.f[n];
         out.x += fmaxf(-f.x, 0.f);
         out.y += fmaxf(-f.y, 0.f);
         out.z += fmaxf(-f.z, 0.f);
         out.w += fmaxf(-f.w, 0.f);
       }
-      const float4 a4 = F.alpha_s[c];
       s.th[0] = fmaxf(s.th[0] - out.x * a4.x * P.inv_dx, 0.f);
       s.th[1] = fmaxf(s.th[1] - out.y * a4.y * P.inv_dx, 0.f);
       s.th[2] = fmaxf(s.th[2] - out.z * a4.z * P.inv_dx, 0.f);
@@ -1649,21 +1665,8 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     // the 8 inflows in the reference's order; one copy of the stack code
     // serves all of them
 #pragma unroll 1
-    for (int nb = 0; nb < 8; ++nb) {
-      int di, dj;
-      bool ok;
-      switch (nb) {
-        case 0: di = 1; dj = 0; ok = i + 1 < (int)F.w; break;
-        case 1: di = 0; dj = 1; ok = j + 1 < (int)F.h; break;
-        case 2: di = 1; dj = 1; ok = i + 1 < (int)F.w && j + 1 < (int)F.h; break;
-        case 3: di = 1; dj = -1; ok = i + 1 < (int)F.w && j > 0; break;
-        case 4: di = -1; dj = 0; ok = hl; break;
-        case 5: di = 0; dj = -1; ok = hd; break;
-        case 6: di = -1; dj = -1; ok = hll; break;
-        default: di = -1; dj = 1; ok = hlu; break;
-      }
-      if (ok) lane_inflow<MODE>(F, P, H, s, i + di, j + dj, face_in(nb));
-    }
+    for (int n = 0; n < 8; ++n)
+      if ((okm >> n) & 1u) lane_inflow<MODE>(F, P, H, s, S, n);
     const float sum = s.th[0] + s.th[1] + s.th[2] + s.th[3];
     if (hc <= 0.f) {
 #pragma unroll
@@ -2150,6 +2153,7 @@ __global__ void __launch_bounds__(256, 4) kp_strata_full(const Film* __restrict_
   __shared__ float tab[480];
   __shared__ float cm[48];
   __shared__ float ltab[12];
+  __shared__ FullStage stage[16];  // one per half-warp
   for (uint32_t f = 0; f < nfilms; ++f) {
     const Film& F = films[f];
     const uint32_t count = F.stats->full_count;
@@ -2158,7 +2162,8 @@ __global__ void __launch_bounds__(256, 4) kp_strata_full(const Film* __restrict_
     __syncthreads();
     load_tables(F, tab, cm, ltab, threadIdx.x, 256);
     __syncthreads();
-    strata_full_film<MODE>(F, tab, cm, ltab, count, first + (threadIdx.x >> 4), gridDim.x * (blockDim.x >> 4));
+    strata_full_film<MODE>(F, tab, cm, ltab, stage[threadIdx.x >> 4], count, first + (threadIdx.x >> 4),
+                           gridDim.x * (blockDim.x >> 4));
   }
 }
 template <int MODE>

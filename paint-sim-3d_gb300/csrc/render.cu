@@ -217,7 +217,9 @@ __device__ __noinline__ float canvas_bump_levelled(float2 p, float hp) {
 __device__ __noinline__ float pinholes(float2 p, float hp) {
   const float2 g = floor2(p / PINHOLE_CELL);
   float z = 0.0f;
+#pragma unroll 1
   for (int b = -1; b <= 1; ++b)
+#pragma unroll 1
     for (int a = -1; a <= 1; ++a) {
       const float2 c = g + v2((float)a, (float)b);
       const float2 r = hash22(c * 0.731f + v2(0.17f, 0.61f));
@@ -271,7 +273,9 @@ __device__ __noinline__ bool near_paint(const R& X, float2 p) {
   const int tw = (int)((X.cam.size[0] + 15u) / 16u), th = (int)((X.cam.size[1] + 15u) / 16u);
   const float s = X.cam.canvas[2] * 16.0f;
   const int gx = (int)floorf(p.x / s), gy = (int)floorf(p.y / s);
+#pragma unroll 1
   for (int dj = -2; dj <= 2; ++dj)
+#pragma unroll 1
     for (int di = -2; di <= 2; ++di) {
       const int x = gx + di, y = gy + dj;
       if (x >= 0 && y >= 0 && x < tw && y < th && (X.tile_flags[x + y * tw] & 1u) != 0u) return true;
@@ -441,6 +445,7 @@ __device__ __noinline__ float edge_factor(const R& X, float2 p) {
   const float2 f = floor2(g);
   const int i = (int)f.x, j = (int)f.y;
   float hmax = 0.0f, hmin = 1e9f;
+#pragma unroll 1
   for (int b = -1; b <= 2; ++b)
     for (int a = -1; a <= 2; ++a) {
       const float v = wet_at(X, i + a, j + b);
@@ -617,6 +622,7 @@ __device__ __noinline__ float4 color_sharp(const R& X, float2 p) {
   if (edge <= 0.0f) return cbil;
   const float4 wx = cr_w(t.x), wy = cr_w(t.y);
   float hb = 0.0f, hb2 = 0.0f;
+#pragma unroll 1
   for (int b = -1; b <= 2; ++b)
     for (int a = -1; a <= 2; ++a) {
       const float wv = sel4(wx, a + 1) * sel4(wy, b + 1);
@@ -725,6 +731,7 @@ __device__ __noinline__ float shadow_at(const R& X, float2 p, float z0, float3 l
     zstart = fmaxf(z0, surf_march(X, p)) + SHADOW_BIAS;
   }
   float sh = 1.0f;
+#pragma unroll 1
   for (int k = 1; k <= 20; ++k) {
     const float d = (float)k * step;
     const float2 q = p + v2(l.x, l.y) / l.z * d;
@@ -739,10 +746,12 @@ __device__ __noinline__ float shadow_at(const R& X, float2 p, float z0, float3 l
 __device__ __noinline__ float ambient_occlusion(const R& X, float2 p, float z0, const Detail& d) {
   const float step = X.cam.canvas[2] * 2.0f;
   float open = 0.0f;
+#pragma unroll 1
   for (int k = 0; k < AO_DIRS; ++k) {
     const float ang = ((float)k + 0.5f) * TAU / (float)AO_DIRS;
     const float2 dir = v2(cosf(ang), sinf(ang));
     float horizon = 0.0f;
+#pragma unroll 1
     for (int i = 1; i <= AO_STEPS; ++i) {
       const float dist = (float)i * step;
       const float rise = surf_hit(X, p + dir * dist, d) - z0;
@@ -906,6 +915,7 @@ __device__ float4 fs(const R& X, float2 ndc_in) {
   const float step = span / (float)nsteps;
   float ta = t0, tb = t1;
   bool found = false;
+#pragma unroll 1
   for (int k = 1; k <= nsteps; ++k) {
     const float tk = t0 + (float)k * step;
     const float3 q = a + dir * tk;
@@ -920,6 +930,7 @@ __device__ float4 fs(const R& X, float2 ndc_in) {
   const float3 qb = a + dir * tb;
   const Detail detail = detail_params(X, v2(qb.x, qb.y));
   if (found) {
+#pragma unroll 1
     for (int r = 0; r < 8; ++r) {
       const float tm = 0.5f * (ta + tb);
       const float3 q = a + dir * tm;
