@@ -1276,6 +1276,7 @@ struct FastShade {
   float h[256];
   uint32_t list[256];
   uint32_t count;
+  alignas(16) float xs[8][32];  // per half-warp scratch of the lane shade
 };
 
 // Strata pass, part 1, over every cell.  Active cells with a strata flux on a
@@ -1452,8 +1453,7 @@ __device__ __forceinline__ void fast_shade_lane(const Film& F, const cf_params& 
 // so a warp shades two cells with all of its lanes instead of one lane per
 // wet cell of the tile.
 template <int MODE>
-__device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params& P, TileId T, const FastShade& sh,
-                                                 int tid) {
+__device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params& P, TileId T, FastShade& sh, int tid) {
   const HalfWarp H(tid & 31);
   const bool dbg = P.flags[0] == 1u;
   const uint32_t n = sh.count;
@@ -1468,7 +1468,7 @@ __device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params&
     for (int k = 0; k < 4; ++k) {
       const float tk = sel4(nt, k);
       const float pg = tk > 0.f ? PigLane<MODE>::load(F, F.pig, c, k, H.q) : 0.f;
-      acc.add(H, k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, dbg);
+      acc.add(H, k, tk, sel4(cu, k), pg, hc, sh.ltab, sh.tab, sh.xs[tid >> 4], dbg);
     }
     const float4 agg = acc.agg(P);
     const float mv = F.m[c];
@@ -1691,7 +1691,8 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     for (int k = 0; k < 4; ++k) {
       const float pk = get4(s.pg, k);
       PigLane<MODE>::store(F, F.pig2, c, k, H.q, pk);
-      acc.add(H, k, get4(s.th, k), get4(s.cu, k), PigLane<MODE>::round(pk, H.q), hc, ltab, tab, dbg);
+      acc.add(H, k, get4(s.th, k), get4(s.cu, k), PigLane<MODE>::round(pk, H.q), hc, ltab, tab,
+              reinterpret_cast<float*>(S.f), dbg);
     }
     const float4 agg = acc.agg(P);
     const float mv = F.m[c];

@@ -226,14 +226,23 @@ struct LaneAcc {
     bad = false;
     r = h16_to_f(rf[H.q]);
   }
+  // xs: 32 floats of the half-warp's shared memory, 16-byte aligned, where
+  // the lanes leave their slot and pigment weight for the others to read
+  // (four vector loads instead of sixteen shuffles)
   __device__ __forceinline__ void add(const HalfWarp& H, int k, float t, float u, float pg, float hv,
-                                      const float* lnmu_tab, const float* tab, bool debug) {
+                                      const float* lnmu_tab, const float* tab, float* xs, bool debug) {
     ssum += t;
     if (!(t > 0.f)) return;
     total += t;
     const int q = H.q;
     const float cc = (q < 12 && pg > 0.f) ? pg : 0.f;
-    const float p12 = H.get(pg, 12), p13 = H.get(pg, 13), p14 = H.get(pg, 14), p15 = H.get(pg, 15);
+    const float wq = cc * tab[(q < 12 ? q : 0) * 40 + 34];
+    __syncwarp(H.mask);  // the previous stratum's (or caller's) values have been read
+    xs[q] = pg;
+    xs[16 + q] = wq;
+    __syncwarp(H.mask);
+    const float4 ps = reinterpret_cast<const float4*>(xs)[3];
+    const float p12 = ps.x, p13 = ps.y, p14 = ps.z, p15 = ps.w;
     const float csum = H.sum(cc);
     float lm = H.sum(cc * lnmu_tab[q < 12 ? q : 0]);
     const float ty = H.sum(cc * p13);
@@ -247,14 +256,15 @@ struct LaneAcc {
     thin += t * p12;
     if (hv > 0.f) {
       // km.wgsl:17-33: weights w_p = c_p g_p of the pigment lanes, then band q
-      const float wq = cc * tab[(q < 12 ? q : 0) * 40 + 34];
       const float scale = csum / fmaxf(H.sum(wq), 1e-9f);
+      const float4 w0 = reinterpret_cast<const float4*>(xs)[4], w1 = reinterpret_cast<const float4*>(xs)[5],
+                   w2 = reinterpret_cast<const float4*>(xs)[6];
+      const float w[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
       float kk = 0.f, ss = 0.f;
 #pragma unroll
       for (int p = 0; p < 12; ++p) {
-        const float wp = H.get(wq, p);
-        kk += wp * tab[p * 40 + q];
-        ss += wp * tab[p * 40 + 16 + q];
+        kk += w[p] * tab[p * 40 + q];
+        ss += w[p] * tab[p * 40 + 16 + q];
       }
       float rr, tt;
       km_layer(kk * scale, ss * scale, t, rr, tt);
