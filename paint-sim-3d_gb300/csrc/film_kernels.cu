@@ -1557,41 +1557,21 @@ __device__ __forceinline__ void strata_fast_tile(const Film& F, TileId T) {
 // written by part 1 (a nonzero face flags both of its cells), or inactive,
 // where strata_limit leaves alpha at 1.
 // The gathered neighbourhood of a cell of the full path, one per half-warp:
-// the cell's 8 faces (towards the cell positive; zero where absent) and the
-// 8 neighbours' strata thicknesses, cure fractions and strata_limit alphas
-// (1 for a neighbour in an inactive tile, whose alpha is not applied).
-// Lanes 0-7 load face and thicknesses of neighbour q, lanes 8-15 its cure
-// fractions and alpha, so the 32 loads of a cell are 2 load instructions of
-// the half-warp instead of a chain of broadcast loads in the inflow loop.
+// the cell's 8 faces (towards the cell positive; zero where absent), the 8
+// neighbours' strata thicknesses, cure fractions and strata_limit alphas (1
+// for a neighbour in an inactive tile, whose alpha is not applied), and the
+// pigment slots of the neighbour strata that flow into the cell, in the
+// order strata_update takes them.  Lanes 0-7 load face and thicknesses of
+// neighbour q, lanes 8-15 the same and its cure fractions and alpha, and
+// decide which of its strata flow; then the half-warp loads the flowing
+// strata's slots four at a time.  So a cell's loads are a few instructions
+// of the half-warp whose latencies overlap, instead of a chain of broadcast
+// loads in the inflow loop.
 struct FullStage {
   float4 f[8], th[8], cu[8], an[8];
   uint32_t cn[8];
+  float pin[32][16];
 };
-// strata_update's inflow from neighbour nb (strata.wgsl:248-262): each of
-// the neighbour's strata that sends a positive flux lays its band over this
-// cell's stack.
-template <int MODE>
-__device__ __forceinline__ void lane_inflow(const Film& F, const cf_params& P, const HalfWarp& H, LaneStack& s,
-                                            const FullStage& S, int nb) {
-  const float4 f = S.f[nb];
-  if (!(f.x > 0.f || f.y > 0.f || f.z > 0.f || f.w > 0.f)) return;
-  const uint32_t cn = S.cn[nb];
-  const float* th = reinterpret_cast<const float*>(&S.th[nb]);
-  const float* cu = reinterpret_cast<const float*>(&S.cu[nb]);
-  const float* an = reinterpret_cast<const float*>(&S.an[nb]);
-  float z0 = 0.f;
-#pragma unroll 1
-  for (int k = 0; k < 4; ++k) {
-    const float thn = th[k];
-    const float z1 = z0 + thn;
-    const float v = sel4(f, k) * an[k] * P.inv_dx;
-    if (v > 0.f && thn > 0.f) {
-      const float pin = PigLane<MODE>::load(F, F.pig, cn, k, H.q);
-      lane_add_band(H, s, z0, z1, v, pin, cu[k], P.misc[0], P.misc[1]);
-    }
-    z0 = z1;
-  }
-}
 
 // Strata pass, part 2: the listed cells, one per half-warp, over a grid of a
 // few blocks per SM.  The full strata_update (strata.wgsl:238-273) builds the
@@ -1627,16 +1607,27 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     const bool ok = nb < 4 ? inb : nact;  // the reference's inflow guards
     const uint32_t cn = inb ? idx(F, ni, nj) : c;
     __syncwarp(H.mask);  // the previous cell's stage has been read
+    const float4 f = nb < 4 ? neg4(acc_face(F, c, nb)) : nact ? acc_face(F, cn, nb - 4) : z4;
+    const float4 tn = ok ? F.sh[cn] : z4;
+    uint32_t nib = 0u;
     if (H.q < 8) {
-      const float4 f = nb < 4 ? neg4(acc_face(F, c, nb)) : nact ? acc_face(F, cn, nb - 4) : z4;
       S.f[nb] = f;
-      S.th[nb] = ok ? F.sh[cn] : z4;
+      S.th[nb] = tn;
       S.cn[nb] = cn;
     } else {
+      const float4 an = nact ? F.alpha_s[cn] : make_float4(1.f, 1.f, 1.f, 1.f);
       S.cu[nb] = ok ? F.scu[cn] : z4;
-      S.an[nb] = nact ? F.alpha_s[cn] : make_float4(1.f, 1.f, 1.f, 1.f);
+      S.an[nb] = an;
+      // the strata of neighbour nb that flow into the cell: a positive
+      // limited flux and a positive thickness (strata.wgsl:248-262)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float v = sel4(f, k) * sel4(an, k) * P.inv_dx;
+        if (ok && v > 0.f && sel4(tn, k) > 0.f) nib |= 1u << k;
+      }
     }
-    const uint32_t okm = (__ballot_sync(H.mask, ok) >> (threadIdx.x & 16u)) & 0xffu;
+    // bit 4 nb + k: stratum k of neighbour nb flows in (the inflow order)
+    const uint32_t fm = __reduce_or_sync(H.mask, nib << (4 * nb));
     LaneStack s;
     {
       const float4 t = F.sh[c], u = F.scu[c];
@@ -1646,27 +1637,65 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
       for (int k = 0; k < 4; ++k) s.pg[k] = PigLane<MODE>::load(F, F.pig, c, k, H.q);
     }
     const float4 a4 = F.alpha_s[c];
+    // the flowing strata's pigment slots, four loads in flight at a time
+    {
+      uint32_t m = fm;
+      int slot = 0;
+#pragma unroll 1
+      while (m) {
+        float v[4];
+        int got = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1u;
+            v[u] = PigLane<MODE>::load(F, F.pig, S.cn[b >> 2], b & 3, H.q);
+            got = u + 1;
+          }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < got) S.pin[slot + u][H.q] = v[u];
+        slot += got;
+      }
+    }
     __syncwarp(H.mask);
     {
       float4 out = z4;
 #pragma unroll
       for (int n = 0; n < 8; ++n) {
-        const float4 f = S.f[n];
-        out.x += fmaxf(-f.x, 0.f);
-        out.y += fmaxf(-f.y, 0.f);
-        out.z += fmaxf(-f.z, 0.f);
-        out.w += fmaxf(-f.w, 0.f);
+        const float4 g = S.f[n];
+        out.x += fmaxf(-g.x, 0.f);
+        out.y += fmaxf(-g.y, 0.f);
+        out.z += fmaxf(-g.z, 0.f);
+        out.w += fmaxf(-g.w, 0.f);
       }
       s.th[0] = fmaxf(s.th[0] - out.x * a4.x * P.inv_dx, 0.f);
       s.th[1] = fmaxf(s.th[1] - out.y * a4.y * P.inv_dx, 0.f);
       s.th[2] = fmaxf(s.th[2] - out.z * a4.z * P.inv_dx, 0.f);
       s.th[3] = fmaxf(s.th[3] - out.w * a4.w * P.inv_dx, 0.f);
     }
-    // the 8 inflows in the reference's order; one copy of the stack code
+    // the inflows in the reference's order (neighbours 0-7, each from its
+    // bottom stratum up): stratum k of neighbour nb lays the band [z0, z1)
+    // of the neighbour's stack over this cell's; one copy of the stack code
     // serves all of them
+    {
+      int slot = 0;
 #pragma unroll 1
-    for (int n = 0; n < 8; ++n)
-      if ((okm >> n) & 1u) lane_inflow<MODE>(F, P, H, s, S, n);
+      for (uint32_t m = fm; m; m &= m - 1u, ++slot) {
+        const int b = __ffs(m) - 1, nb = b >> 2, k = b & 3;
+        const float* th = reinterpret_cast<const float*>(&S.th[nb]);
+        float z0 = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+          if (kk < k) z0 = z0 + th[kk];
+        const float z1 = z0 + th[k];
+        const float v = reinterpret_cast<const float*>(&S.f[nb])[k] * reinterpret_cast<const float*>(&S.an[nb])[k] *
+                        P.inv_dx;
+        lane_add_band(H, s, z0, z1, v, S.pin[slot][H.q], reinterpret_cast<const float*>(&S.cu[nb])[k], P.misc[0],
+                      P.misc[1]);
+      }
+    }
     const float sum = s.th[0] + s.th[1] + s.th[2] + s.th[3];
     if (hc <= 0.f) {
 #pragma unroll
