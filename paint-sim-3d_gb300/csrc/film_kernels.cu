@@ -179,14 +179,16 @@ __device__ __forceinline__ void cure_tile(const Film& F, TileId T) {
   float hv = F.hh[c];
   if (hv <= 0.f) { set_rheo<MODE>(F, c, 1.f, 0.f, P.phys[2]); return; }
   float rate = P.cure[0] * P.frame_dt;
-  float4 t4 = F.sh[c], c4 = F.scu[c];
+  // the aggregates load with the strata, ahead of the cure store (which
+  // the compiler could not move them past)
+  const float4 t4 = F.sh[c], c4 = F.scu[c], ag = F.agg[c];
   float t[4] = {t4.x, t4.y, t4.z, t4.w}, u[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
   for (int k = 0; k < 4; ++k) u[k] = t[k] > 0.f ? fminf(u[k] + rate, 1.f) : u[k];
   if (!(t[0] > 0.f && u[0] >= 1.f)) {
     F.scu[c] = make_float4(u[0], u[1], u[2], u[3]);
     float mu, ty, n;
-    rheo_from_parts(P, F.agg[c], t, u, mu, ty, n);
+    rheo_from_parts(P, ag, t, u, mu, ty, n);
     set_rheo<MODE>(F, c, mu, ty, n);
     return;
   }
@@ -1021,12 +1023,17 @@ __device__ __forceinline__ void limit_apply_tile(const Film& F, TileId T) {
       tma_load_2d(S.h, F.tmap + MAP_H, i0 - 4, j0 - 4, &S.bar);
     }
   }
+  // both cells' loads before either store
   float4 a4[2];
+  float dl[2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     a4[r] = in[r] ? F.acc[c[r]] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (in[r]) F.delta_old[c[r]] = F.delta[c[r]];
+    dl[r] = in[r] ? F.delta[c[r]] : 0.f;
   }
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+    if (in[r]) F.delta_old[c[r]] = dl[r];
   if (tid < 9) {
     const int tx = (int)T.x + tid % 3 - 1, ty = (int)T.y + tid / 3 - 1;
     S.act[tid] = tx >= 0 && ty >= 0 && tx < (int)F.tw && ty < (int)F.th ? F.tile_flags[tx + ty * F.tw] & ACTIVE : 0u;
