@@ -1409,6 +1409,10 @@ __device__ __forceinline__ void fast_color_cached(const Film& F, uint32_t c, con
       wet = 1.0f - sel4(cu, k);
       cure_top = sel4(cu, k);
     }
+  // every load (m, the detail texel's lay and yield stress, the spectrum)
+  // goes out before the first store
+  const float mv = F.m[c];
+  const ushort4 dt = detail_texel<MODE>(F, c, cure_top, sh.h[tid], mv);
   float r[16];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -1417,9 +1421,8 @@ __device__ __forceinline__ void fast_color_cached(const Film& F, uint32_t c, con
   }
   float rgb[3];
   surface_rgb(sh.cm, r, wet, rgb);
-  const float mv = F.m[c];
   F.color[c] = pack_color(rgb, surface_rough(cure_top, sh.h[tid], mv));
-  F.detail[c] = detail_texel<MODE>(F, c, cure_top, sh.h[tid], mv);
+  F.detail[c] = dt;
 }
 // The shade and aggregates of one cell the fast path left to shade, by its
 // own lane (CellAcc).
@@ -1444,15 +1447,16 @@ __device__ __forceinline__ void fast_shade_lane(const Film& F, const cf_params& 
   }
   // the next cure reads the aggregates of wet cells only; a wet cell's
   // composite spectrum is cached for the frames its strata stay as they are
+  const float mv = F.m[c];
+  const ushort4 dt = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);  // its loads before the stores
   if (hc > 0.f) {
     F.agg[c] = acc.agg(P);
 #pragma unroll
     for (int q = 0; q < 4; ++q)
       F.spec[(size_t)q * F.n + c] = make_float4(acc.r[4 * q], acc.r[4 * q + 1], acc.r[4 * q + 2], acc.r[4 * q + 3]);
   }
-  const float mv = F.m[c];
   F.color[c] = acc.color(P, sh.cm, hc, mv);
-  F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
+  F.detail[c] = dt;
 }
 // The shade (shade.wgsl:28-84) and composition aggregates (cure.wgsl:3-48)
 // of the tile's cells that the fast path listed: one cell per half-warp, the
@@ -1479,12 +1483,13 @@ __device__ __forceinline__ void fast_shade_cells(const Film& F, const cf_params&
     }
     const float4 agg = acc.agg(P);
     const float mv = F.m[c];
+    const ushort4 dt = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);  // its loads before the stores
     const ushort4 col = acc.color(H, P, sh.cm, hc, mv);
     if (hc > 0.f) reinterpret_cast<float*>(F.spec)[((size_t)(H.q >> 2) * F.n + c) * 4 + (H.q & 3)] = acc.r;
     if (H.q == 0) {
       if (hc > 0.f) F.agg[c] = agg;  // the next cure reads the aggregates of wet cells only
       F.color[c] = col;
-      F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
+      F.detail[c] = dt;
     }
   }
 }
@@ -1732,6 +1737,7 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     }
     const float4 agg = acc.agg(P);
     const float mv = F.m[c];
+    const ushort4 dt = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);  // its loads before the stores
     const ushort4 col = acc.color(H, P, cm, hc, mv);
     // the composite spectrum of the new stack (its thicknesses and stored
     // slots) is cached for the next frames' fast path, as its own shades are
@@ -1739,7 +1745,7 @@ __device__ __forceinline__ void strata_full_film(const Film& F, const float* tab
     if (H.q == 0) {
       F.agg[c] = agg;
       F.color[c] = col;
-      F.detail[c] = detail_texel<MODE>(F, c, acc.cure_top, hc, mv);
+      F.detail[c] = dt;
       F.shade_state[c] = hc <= 0.f ? SHADE_DRY : SHADE_WET;
     }
   }
